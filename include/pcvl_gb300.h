@@ -1,0 +1,113 @@
+/*
+ * pcvl_gb300 — C ABI of the GB300 linear-optics kernels.
+ *
+ * Plain pointers and sizes only.  Every function returns 0 on success and a
+ * non-zero PCVL_ERR_* code otherwise; pcvl_last_error() then gives the message
+ * (per calling thread).  Device pointers (suffix _d) point to memory on the
+ * current CUDA device; `stream` is a cudaStream_t (NULL = legacy default stream).
+ * Complex numbers are complex128 (two interleaved doubles, re then im).
+ *
+ * The functions replace the calls that the reference makes into its closed
+ * native library (exqalibur ~= 1.1.0); each block cites the call site.
+ */
+#ifndef PCVL_GB300_H
+#define PCVL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PCVL_OK 0
+#define PCVL_ERR_ARG 1      /* bad argument: size, pointer, shape */
+#define PCVL_ERR_CUDA 2     /* a CUDA runtime call failed */
+#define PCVL_ERR_MEMORY 3   /* the request does not fit in device memory */
+#define PCVL_ERR_TIMEOUT 4  /* a bounded device-side wait gave up */
+
+/* ------------------------------------------------------------------ errors */
+/* Library version string, e.g. "pcvl_gb300 0.1.0 sm_103a". */
+const char* pcvl_version(void);
+/* Copies the calling thread's last error message into buf (NUL-terminated). */
+int pcvl_last_error(char* buf, size_t len);
+/* Frees every workspace the library cached on the current device. */
+int pcvl_release_workspace(void);
+
+/* ------------------------------------------------------------------ permanents
+ * Replaces xq.permanent_cx(M) (perceval/backends/_naive.py:70-71), called by
+ * NaiveBackend.prob_amplitude (perceval/backends/_naive.py:46-49).
+ *
+ * Batched exact permanents of `count` square complex128 matrices stored row-major
+ * in mats_d; matrix i starts at complex element offsets_h[i] and has size
+ * sizes_h[i] (0 <= n <= 48; the permanent of the 0x0 matrix is 1).  Results go to
+ * out_d[i] (complex128).  method: 0 = Glynn (Gray-code over 2^(n-1) sign
+ * vectors), 1 = Ryser (over 2^n column subsets).  Matrices are binned by size;
+ * each bin's launch spreads Gray-code chunks across the whole chip, so one large
+ * matrix uses every SM.  offsets_h and sizes_h are host arrays.
+ */
+int pcvl_permanent_batch(const double* mats_d, const int64_t* offsets_h, const int32_t* sizes_h,
+                         int32_t count, double* out_d, int32_t method, void* stream);
+
+/* ------------------------------------------------------------------ SLOS
+ * Replaces the numeric SLOS path of perceval/backends/_slos.py:
+ *   _Path._decompose / compute   (:61-102)  -> photon-addition order
+ *   xq.FSArray / xq.FSMap         (:151-168) -> on-the-fly Fock ranking
+ *   FSMap.compute_slos_layer      (:99)      -> pcvl_slos_forward layers
+ *   prob_amplitude / all_prob / prob_distribution (:187-214, with
+ *   xq.all_prob_normalize_output) -> pcvl_slos_amplitudes / pcvl_slos_probabilities
+ *
+ * A plan fixes (m, input state, batch): `batch` circuits share the input state and
+ * each has its own m x m unitary.  Layer k holds the C(m+k-1, k) k-photon
+ * coefficients of every circuit, state-major with the circuit index innermost.
+ * Output index r of a circuit is the rank of the output state in descending
+ * lexicographic order (|n,0,..,0> first), the order of the reference's
+ * allstate_iterator.  keep_layers != 0 keeps every layer resident for
+ * pcvl_slos_backward.
+ */
+typedef struct pcvl_slos_plan pcvl_slos_plan;
+
+int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int32_t* input_state_h,
+                          int32_t batch, int32_t keep_layers);
+int pcvl_slos_plan_destroy(pcvl_slos_plan* plan);
+/* Number of output states C(m+n-1, n) of the plan. */
+int pcvl_slos_output_count(const pcvl_slos_plan* plan, int64_t* count);
+/* Device bytes the plan holds. */
+int pcvl_slos_plan_bytes(const pcvl_slos_plan* plan, int64_t* bytes);
+/* Propagates the input state through u_d (batch x m x m complex128, row = output
+ * mode, column = input mode, circuit-major). */
+int pcvl_slos_forward(pcvl_slos_plan* plan, const double* u_d, void* stream);
+/* probs_d[r * batch + b] = |c|^2 * prod(out!) / prod(in!)   (float64; state-major,
+ * circuit innermost) */
+int pcvl_slos_probabilities(pcvl_slos_plan* plan, double* probs_d, void* stream);
+/* amps_d[r * batch + b] = c * sqrt(prod(out!) / prod(in!))   (complex128) */
+int pcvl_slos_amplitudes(pcvl_slos_plan* plan, double* amps_d, void* stream);
+/* Adjoint of L = sum_{r,b} w[r * batch + b] * p[r, b]: writes dL/dU (torch convention,
+ * dL/dRe + i dL/dIm) to grad_u_d (batch x m x m complex128).  Needs a forward with
+ * keep_layers != 0 on the same plan. */
+int pcvl_slos_backward(pcvl_slos_plan* plan, const double* weights_d, double* grad_u_d,
+                       void* stream);
+
+/* ------------------------------------------------------------------ sampling
+ * Replaces xq.Clifford2017 (perceval/backends/_clifford2017.py:36-57:
+ * set_unitary / set_input_state / sample / samples).
+ *
+ * Draws `count` exact boson samples with the algorithm of Clifford & Clifford
+ * (SODA 2018, "algorithm B"): photons are added one at a time in a uniformly random
+ * order, each output mode drawn from the Laplace expansion of the k x k
+ * sub-permanents.  u_d is the m x m complex128 unitary, input_state_h the input
+ * occupation (host, m entries).  Sample s writes its m output counts to
+ * out_counts_d[s * m .. s * m + m - 1] (int32).  Sample s uses Philox4x32-10 with
+ * key (seed, 0) and counters (first_sample + s, step, draw), so results are
+ * reproducible and independent of scheduling.  precision: 0 = float-float
+ * (FP64-class), 1 = FP32 with compensated sums.
+ */
+int pcvl_cc2017_sample(const double* u_d, int32_t m, const int32_t* input_state_h, int64_t count,
+                       uint64_t seed, uint64_t first_sample, int32_t precision,
+                       int32_t* out_counts_d, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PCVL_GB300_H */

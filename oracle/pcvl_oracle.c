@@ -1,0 +1,497 @@
+/*
+ * CPU oracle for the linear-optics hot path.  TEST INFRASTRUCTURE ONLY: the
+ * library's product path never calls into this file; tests, the smoke check and
+ * the benchmark's CPU baseline use it as the checker.
+ *
+ * Plain FP64 restatement of the reference semantics (the reference's arithmetic
+ * lives in the closed exqalibur~=1.1.0 library; its call sites and tests fix what
+ * is computed):
+ *  - permanents: perceval/backends/_naive.py:46-71 (xq.permanent_cx), Glynn (2010)
+ *    Gray-code formula and Ryser (1963) formula, docs/source/backends.rst:160-167;
+ *  - SLOS: perceval/backends/_slos.py:37-223 (path order :61-86, layer update
+ *    :93-99, normalisation :187-214);
+ *  - Clifford & Clifford (2018) algorithm B: perceval/backends/_clifford2017.py,
+ *    docs/source/backends.rst:104-116, with the same Philox4x32-10 stream and
+ *    draw procedure as the GPU sampler so samples can be compared one by one.
+ * Fock states of n photons on m modes are ranked in descending lexicographic order
+ * (tests/utils/test_statevector.py:430-438).
+ */
+#include <complex.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef double complex cplx;
+
+/* ---------------------------------------------------------------- combinatorics */
+static uint64_t fock_count(int M, int k) {
+  if (k < 0) return 0;
+  if (M <= 0) return k == 0 ? 1 : 0;
+  uint64_t r = 1;
+  for (int i = 1; i <= k; ++i) r = r * (uint64_t)(M - 1 + i) / (uint64_t)i;
+  return r;
+}
+
+uint64_t oracle_fock_count(int m, int n) { return fock_count(m, n); }
+
+/* rank in descending-lex order: sum_i Cn(m - i, R_{i+1} - 1) */
+uint64_t oracle_fock_rank(int m, const int* s) {
+  int rest = 0;
+  for (int i = 0; i < m; ++i) rest += s[i];
+  uint64_t r = 0;
+  for (int i = 0; i < m; ++i) {
+    rest -= s[i];
+    if (rest > 0) r += fock_count(m - i, rest - 1);
+  }
+  return r;
+}
+
+void oracle_fock_unrank(int m, int n, uint64_t rank, int* s) {
+  int rest = n;
+  for (int i = 0; i < m - 1; ++i) {
+    int v = rest;
+    for (;;) {
+      uint64_t blk = fock_count(m - i - 1, rest - v);
+      if (rank < blk) break;
+      rank -= blk;
+      --v;
+    }
+    s[i] = v;
+    rest -= v;
+  }
+  s[m - 1] = rest;
+}
+
+/* next state in descending-lex order; returns 0 after the last one */
+static int fock_next(int m, int* s) {
+  int tail = 0;
+  for (int i = m - 2; i >= 0; --i) {
+    tail += s[i + 1];
+    if (s[i] > 0) {
+      s[i] -= 1;
+      s[i + 1] = tail + 1;
+      for (int j = i + 2; j < m; ++j) s[j] = 0;
+      return 1;
+    }
+  }
+  return 0;
+}
+
+/* ---------------------------------------------------------------- permanents */
+static void neumaier(double* s, double* c, double x) {
+  double t = *s + x;
+  if (fabs(*s) >= fabs(x))
+    *c += (*s - t) + x;
+  else
+    *c += (x - t) + *s;
+  *s = t;
+}
+
+/* Glynn with Gray-code order, restarted from exact row sums every 2^12 steps;
+ * a: n x n complex128 row-major (interleaved re, im); out: 2 doubles */
+void oracle_perm_glynn(int n, const double* a_, double* out) {
+  const cplx* a = (const cplx*)a_;
+  if (n == 0) {
+    out[0] = 1;
+    out[1] = 0;
+    return;
+  }
+  const uint64_t total = 1ull << (n - 1);
+  const uint64_t chunk = 1ull << 12;
+  const int64_t nchunks = (int64_t)((total + chunk - 1) / chunk);
+  double sr = 0, cr = 0, si = 0, ci = 0;
+#pragma omp parallel
+  {
+    double lsr = 0, lcr = 0, lsi = 0, lci = 0;
+    cplx* r = (cplx*)malloc(sizeof(cplx) * n);
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t q = 0; q < nchunks; ++q) {
+      const uint64_t g0 = (uint64_t)q * chunk;
+      const uint64_t g1 = g0 + chunk < total ? g0 + chunk : total;
+      /* delta for Gray code g(k) = k ^ (k >> 1): bit t set -> column t + 1 negative */
+      uint64_t gc = g0 ^ (g0 >> 1);
+      for (int i = 0; i < n; ++i) {
+        cplx v = a[i * n];
+        for (int j = 1; j < n; ++j) v += ((gc >> (j - 1)) & 1) ? -a[i * n + j] : a[i * n + j];
+        r[i] = v;
+      }
+      int sign = __builtin_popcountll(gc) & 1;
+      for (uint64_t k = g0; k < g1; ++k) {
+        if (k > g0) {
+          const int t = __builtin_ctzll(k);
+          const int j = t + 1;
+          gc ^= 1ull << t;
+          const int neg = (gc >> t) & 1;
+          for (int i = 0; i < n; ++i) r[i] += neg ? -2.0 * a[i * n + j] : 2.0 * a[i * n + j];
+          sign ^= 1;
+        }
+        cplx p = r[0];
+        for (int i = 1; i < n; ++i) p *= r[i];
+        if (sign) p = -p;
+        neumaier(&lsr, &lcr, creal(p));
+        neumaier(&lsi, &lci, cimag(p));
+      }
+    }
+    free(r);
+#pragma omp critical
+    {
+      neumaier(&sr, &cr, lsr);
+      neumaier(&sr, &cr, lcr);
+      neumaier(&si, &ci, lsi);
+      neumaier(&si, &ci, lci);
+    }
+  }
+  out[0] = ldexp(sr + cr, -(n - 1));
+  out[1] = ldexp(si + ci, -(n - 1));
+}
+
+/* Ryser: (-1)^n sum_S (-1)^|S| prod_i sum_{j in S} a_ij, Gray-code over subsets */
+void oracle_perm_ryser(int n, const double* a_, double* out) {
+  const cplx* a = (const cplx*)a_;
+  if (n == 0) {
+    out[0] = 1;
+    out[1] = 0;
+    return;
+  }
+  const uint64_t total = 1ull << n;
+  const uint64_t chunk = 1ull << 12;
+  const int64_t nchunks = (int64_t)((total + chunk - 1) / chunk);
+  double sr = 0, cr = 0, si = 0, ci = 0;
+#pragma omp parallel
+  {
+    double lsr = 0, lcr = 0, lsi = 0, lci = 0;
+    cplx* r = (cplx*)malloc(sizeof(cplx) * n);
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t q = 0; q < nchunks; ++q) {
+      const uint64_t g0 = (uint64_t)q * chunk;
+      const uint64_t g1 = g0 + chunk < total ? g0 + chunk : total;
+      uint64_t gc = g0 ^ (g0 >> 1);
+      for (int i = 0; i < n; ++i) {
+        cplx v = 0;
+        for (int j = 0; j < n; ++j)
+          if ((gc >> j) & 1) v += a[i * n + j];
+        r[i] = v;
+      }
+      for (uint64_t k = g0; k < g1; ++k) {
+        if (k > g0) {
+          const int t = __builtin_ctzll(k);
+          gc ^= 1ull << t;
+          const int in = (gc >> t) & 1;
+          for (int i = 0; i < n; ++i) r[i] += in ? a[i * n + t] : -a[i * n + t];
+        }
+        cplx p = r[0];
+        for (int i = 1; i < n; ++i) p *= r[i];
+        if (__builtin_popcountll(gc) & 1) p = -p;
+        neumaier(&lsr, &lcr, creal(p));
+        neumaier(&lsi, &lci, cimag(p));
+      }
+    }
+    free(r);
+#pragma omp critical
+    {
+      neumaier(&sr, &cr, lsr);
+      neumaier(&sr, &cr, lcr);
+      neumaier(&si, &ci, lsi);
+      neumaier(&si, &ci, lci);
+    }
+  }
+  const double sg = (n & 1) ? -1.0 : 1.0;
+  out[0] = sg * (sr + cr);
+  out[1] = sg * (si + ci);
+}
+
+/* batch of permanents (packed like the GPU entry point) */
+void oracle_perm_batch(const double* mats, const int64_t* offs, const int32_t* sizes, int count, int ryser,
+                       double* out) {
+  for (int i = 0; i < count; ++i) {
+    if (ryser)
+      oracle_perm_ryser(sizes[i], mats + 2 * offs[i], out + 2 * i);
+    else
+      oracle_perm_glynn(sizes[i], mats + 2 * offs[i], out + 2 * i);
+  }
+}
+
+/* ---------------------------------------------------------------- SLOS */
+/* photon order of _Path._decompose for a single input state (_slos.py:61-86) */
+int oracle_slos_order(int m, const int* in, int* order) {
+  int* c = (int*)malloc(sizeof(int) * m);
+  memcpy(c, in, sizeof(int) * m);
+  int k = 0;
+  for (;;) {
+    int best = -1, bv = 0;
+    for (int i = 0; i < m; ++i)
+      if (c[i] > bv) {
+        bv = c[i];
+        best = i;
+      }
+    if (best < 0) break;
+    order[k++] = best;
+    c[best]--;
+  }
+  free(c);
+  return k;
+}
+
+/* one layer: child coefficient = sum_j U[j, mk] * parent(child - e_j), children in
+ * rank order, parallel over children */
+static void slos_layer(int m, int k, const cplx* U, int mk, const cplx* prev, cplx* cur) {
+  const int64_t nc = (int64_t)fock_count(m, k);
+#pragma omp parallel
+  {
+    int* s = (int*)malloc(sizeof(int) * m);
+#pragma omp for schedule(static, 4096)
+    for (int64_t c = 0; c < nc; ++c) {
+      oracle_fock_unrank(m, k, (uint64_t)c, s);
+      cplx acc = 0;
+      for (int j = 0; j < m; ++j) {
+        if (s[j] == 0) continue;
+        s[j]--;
+        acc += U[j * m + mk] * prev[oracle_fock_rank(m, s)];
+        s[j]++;
+      }
+      cur[c] = acc;
+    }
+    free(s);
+  }
+}
+
+/* Final-layer coefficients c_n (rank order) of input `in` through U (m x m). */
+int oracle_slos_coefs(int m, const int* in, const double* U_, double* coefs_out) {
+  const cplx* U = (const cplx*)U_;
+  int n = 0;
+  for (int i = 0; i < m; ++i) n += in[i];
+  int* order = (int*)malloc(sizeof(int) * (n + 1));
+  oracle_slos_order(m, in, order);
+  uint64_t mx = 1;
+  for (int k = 0; k <= n; ++k)
+    if (fock_count(m, k) > mx) mx = fock_count(m, k);
+  cplx* a = (cplx*)malloc(sizeof(cplx) * mx);
+  cplx* b = (cplx*)malloc(sizeof(cplx) * mx);
+  if (!a || !b) {
+    free(a);
+    free(b);
+    free(order);
+    return 1;
+  }
+  a[0] = 1;
+  for (int k = 1; k <= n; ++k) {
+    slos_layer(m, k, U, order[k - 1], a, b);
+    cplx* t = a;
+    a = b;
+    b = t;
+  }
+  memcpy(coefs_out, a, sizeof(cplx) * fock_count(m, n));
+  free(a);
+  free(b);
+  free(order);
+  return 0;
+}
+
+static double prodfact(int m, const int* s) {
+  double p = 1;
+  for (int i = 0; i < m; ++i)
+    for (int v = 2; v <= s[i]; ++v) p *= v;
+  return p;
+}
+
+/* probabilities |c|^2 prod(out!) / prod(in!) and amplitudes c sqrt(prod(out!)/prod(in!)) */
+int oracle_slos(int m, const int* in, const double* U, double* probs, double* amps) {
+  int n = 0;
+  for (int i = 0; i < m; ++i) n += in[i];
+  const int64_t N = (int64_t)fock_count(m, n);
+  double* c = (double*)malloc(sizeof(double) * 2 * N);
+  if (!c) return 1;
+  if (oracle_slos_coefs(m, in, U, c)) {
+    free(c);
+    return 1;
+  }
+  const double pin = prodfact(m, in);
+  int* s = (int*)calloc(m, sizeof(int));
+  s[0] = n;
+  for (int64_t r = 0; r < N; ++r) {
+    const double f = prodfact(m, s) / pin;
+    const double re = c[2 * r], im = c[2 * r + 1];
+    if (probs) probs[r] = (re * re + im * im) * f;
+    if (amps) {
+      amps[2 * r] = re * sqrt(f);
+      amps[2 * r + 1] = im * sqrt(f);
+    }
+    if (!fock_next(m, s)) break;
+  }
+  free(s);
+  free(c);
+  return 0;
+}
+
+/* dL/dU (torch convention dL/dRe + i dL/dIm) of L = sum_r w[r] p[r] by a reverse
+ * sweep over stored layers */
+int oracle_slos_grad(int m, const int* in, const double* U_, const double* w, double* grad_) {
+  const cplx* U = (const cplx*)U_;
+  cplx* grad = (cplx*)grad_;
+  int n = 0;
+  for (int i = 0; i < m; ++i) n += in[i];
+  int* order = (int*)malloc(sizeof(int) * (n + 1));
+  oracle_slos_order(m, in, order);
+  cplx** L = (cplx**)malloc(sizeof(cplx*) * (n + 1));
+  for (int k = 0; k <= n; ++k) L[k] = (cplx*)malloc(sizeof(cplx) * fock_count(m, k));
+  L[0][0] = 1;
+  for (int k = 1; k <= n; ++k) slos_layer(m, k, U, order[k - 1], L[k - 1], L[k]);
+  for (int i = 0; i < m * m; ++i) grad[i] = 0;
+  const double pin = prodfact(m, in);
+  const int64_t N = (int64_t)fock_count(m, n);
+  cplx* adj = (cplx*)malloc(sizeof(cplx) * N);
+  int* s = (int*)calloc(m, sizeof(int));
+  s[0] = n;
+  for (int64_t r = 0; r < N; ++r) {
+    adj[r] = 2.0 * w[r] * (prodfact(m, s) / pin) * L[n][r];
+    if (!fock_next(m, s)) break;
+  }
+  for (int k = n; k >= 1; --k) {
+    const int mk = order[k - 1];
+    const int64_t np = (int64_t)fock_count(m, k - 1);
+    cplx* pa = (cplx*)malloc(sizeof(cplx) * (np > 0 ? np : 1));
+    for (int64_t p = 0; p < np; ++p) {
+      oracle_fock_unrank(m, k - 1, (uint64_t)p, s);
+      cplx acc = 0;
+      for (int j = 0; j < m; ++j) {
+        s[j]++;
+        const cplx x = adj[oracle_fock_rank(m, s)];
+        s[j]--;
+        acc += conj(U[j * m + mk]) * x;
+        grad[j * m + mk] += conj(L[k - 1][p]) * x;
+      }
+      pa[p] = acc;
+    }
+    free(adj);
+    adj = pa;
+  }
+  free(adj);
+  free(s);
+  for (int k = 0; k <= n; ++k) free(L[k]);
+  free(L);
+  free(order);
+  return 0;
+}
+
+/* ---------------------------------------------------------------- Philox4x32-10 */
+typedef struct {
+  uint32_t x, y, z, w;
+} u4;
+
+static u4 philox(u4 c, uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c.x;
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c.z;
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    u4 d = {hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    c = d;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+void oracle_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1, uint32_t* out) {
+  u4 r = philox((u4){c0, c1, c2, c3}, k0, k1);
+  out[0] = r.x;
+  out[1] = r.y;
+  out[2] = r.z;
+  out[3] = r.w;
+}
+
+/* permanent of the (rows x cols) selection of U, by Glynn */
+static cplx sub_perm(int d, const cplx* U, int m, const int* rows, const int* cols) {
+  if (d == 0) return 1;
+  double* a = (double*)malloc(sizeof(double) * 2 * d * d);
+  for (int r = 0; r < d; ++r)
+    for (int c = 0; c < d; ++c) {
+      const cplx v = U[rows[r] * m + cols[c]];
+      a[2 * (r * d + c)] = creal(v);
+      a[2 * (r * d + c) + 1] = cimag(v);
+    }
+  double o[2];
+  oracle_perm_glynn(d, a, o);
+  free(a);
+  return o[0] + I * o[1];
+}
+
+/* Clifford & Clifford algorithm B; out: count x m counts */
+void oracle_cc2017(const double* U_, int m, const int* in, int64_t count, uint64_t seed, uint64_t first, int32_t* out) {
+  const cplx* U = (const cplx*)U_;
+  int n = 0;
+  for (int i = 0; i < m; ++i) n += in[i];
+  int* cols0 = (int*)malloc(sizeof(int) * (n + 1));
+  for (int i = 0, q = 0; i < m; ++i)
+    for (int v = 0; v < in[i]; ++v) cols0[q++] = i;
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (int64_t s = 0; s < count; ++s) {
+    const uint64_t sid = first + (uint64_t)s;
+    const uint32_t slo = (uint32_t)sid, shi = (uint32_t)(sid >> 32);
+    int cols[64], rows[64], subc[64];
+    for (int l = 0; l < n; ++l) cols[l] = cols0[l];
+    for (int q = n - 1; q >= 1; --q) {
+      const u4 r = philox((u4){slo, shi, 0xffffffffu, (uint32_t)q}, k0, k1);
+      const int j = (int)(((uint64_t)r.x * (uint64_t)(q + 1)) >> 32);
+      const int t = cols[q];
+      cols[q] = cols[j];
+      cols[j] = t;
+    }
+    double* w = (double*)malloc(sizeof(double) * m);
+    cplx sub[64];
+    for (int k = 1; k <= n; ++k) {
+      for (int l = 0; l < k; ++l) {
+        int q = 0;
+        for (int c = 0; c < k; ++c)
+          if (c != l) subc[q++] = cols[c];
+        sub[l] = sub_perm(k - 1, U, m, rows, subc);
+      }
+      double W = 0;
+      for (int i = 0; i < m; ++i) {
+        cplx z = 0;
+        for (int l = 0; l < k; ++l) z += U[i * m + cols[l]] * sub[l];
+        w[i] = creal(z) * creal(z) + cimag(z) * cimag(z);
+        W += w[i];
+      }
+      const u4 r = philox((u4){slo, shi, (uint32_t)k, 0u}, k0, k1);
+      const uint64_t v = ((uint64_t)(r.x >> 5) << 26) | (uint64_t)(r.y >> 6);
+      const double target = (double)v * (1.0 / 9007199254740992.0) * W;
+      double run = 0;
+      int pick = -1, last_pos = 0;
+      for (int i = 0; i < m; ++i) {
+        if (w[i] > 0) last_pos = i;
+        run += w[i];
+        if (run > target) {
+          pick = i;
+          break;
+        }
+      }
+      rows[k - 1] = pick >= 0 ? pick : last_pos;
+    }
+    free(w);
+    int32_t* o = out + s * m;
+    for (int i = 0; i < m; ++i) o[i] = 0;
+    for (int k = 0; k < n; ++k) o[rows[k]]++;
+  }
+  free(cols0);
+}
+
+int oracle_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+void oracle_set_threads(int t) {
+#ifdef _OPENMP
+  if (t > 0) omp_set_num_threads(t);
+#else
+  (void)t;
+#endif
+}

@@ -1,0 +1,194 @@
+"""ctypes binding of ``libpcvl_gb300.so``: the only way the package reaches the GPU.
+
+There is no CPU fallback: when the library is missing or CUDA is unavailable every
+entry point raises ``RuntimeError``.  Tensors passed in must be CUDA tensors on the
+current device, contiguous, of the documented dtype; outputs are written in place.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+import torch
+
+_LIB_PATH = Path(__file__).resolve().parent / "lib" / "libpcvl_gb300.so"
+_lib = None
+
+SYMBOLS = {
+    "pcvl_version": (ctypes.c_char_p, []),
+    "pcvl_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
+    "pcvl_release_workspace": (ctypes.c_int, []),
+    "pcvl_permanent_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                            ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
+    "pcvl_slos_plan_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.c_void_p,
+                                             ctypes.c_int32, ctypes.c_int32]),
+    "pcvl_slos_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "pcvl_slos_output_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
+    "pcvl_slos_plan_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
+    "pcvl_slos_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "pcvl_slos_probabilities": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "pcvl_slos_amplitudes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "pcvl_slos_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "pcvl_cc2017_sample": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64,
+                                          ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p,
+                                          ctypes.c_void_p]),
+}
+
+
+def library_path() -> Path:
+    return Path(os.environ.get("PCVL_GB300_LIB", _LIB_PATH))
+
+
+def load(require_cuda: bool = True):
+    """Load the library (once).  Raises RuntimeError if it or CUDA is unavailable."""
+    global _lib
+    if require_cuda and not torch.cuda.is_available():
+        raise RuntimeError("perceval_gb300 needs a CUDA GPU: torch.cuda.is_available() is False")
+    if _lib is None:
+        path = library_path()
+        if not path.exists():
+            raise RuntimeError(f"{path} is missing: build it with perceval_gb300._build.build()")
+        lib = ctypes.CDLL(str(path))
+        for name, (res, args) in SYMBOLS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def last_error() -> str:
+    buf = ctypes.create_string_buffer(1024)
+    load(require_cuda=False).pcvl_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(status: int, what: str):
+    if status != 0:
+        raise RuntimeError(f"{what} failed (status {status}): {last_error()}")
+
+
+def _stream_ptr(stream) -> int:
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return int(stream.cuda_stream)
+
+
+def _dev_tensor(t: torch.Tensor, dtype, name: str) -> torch.Tensor:
+    if not (isinstance(t, torch.Tensor) and t.is_cuda):
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype}, got {t.dtype}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    return t
+
+
+# ------------------------------------------------------------------ permanents
+def permanent_batch(mats: torch.Tensor, offsets: np.ndarray, sizes: np.ndarray, out: torch.Tensor,
+                    method: int = 0, stream=None) -> torch.Tensor:
+    """Permanents of packed square complex128 matrices (see pcvl_permanent_batch)."""
+    lib = load()
+    _dev_tensor(mats, torch.complex128, "mats")
+    _dev_tensor(out, torch.complex128, "out")
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+    count = int(sizes.shape[0])
+    if offsets.shape[0] != count or out.numel() < count:
+        raise ValueError("offsets, sizes and out must describe the same number of matrices")
+    if count and int((offsets + sizes.astype(np.int64) ** 2).max()) > mats.numel():
+        raise ValueError("a matrix extends beyond the end of mats")
+    check(lib.pcvl_permanent_batch(mats.data_ptr(), offsets.ctypes.data, sizes.ctypes.data, count,
+                                   out.data_ptr(), int(method), _stream_ptr(stream)), "pcvl_permanent_batch")
+    return out
+
+
+# ------------------------------------------------------------------ SLOS
+class SlosPlan:
+    """Owner of a ``pcvl_slos_plan``: fixed (m, input state, batch)."""
+
+    def __init__(self, m: int, input_state, batch: int = 1, keep_layers: bool = False):
+        self._lib = load()
+        inp = np.ascontiguousarray(input_state, dtype=np.int32)
+        if inp.shape != (m,):
+            raise ValueError("input_state must have m entries")
+        h = ctypes.c_void_p()
+        check(self._lib.pcvl_slos_plan_create(ctypes.byref(h), int(m), inp.ctypes.data, int(batch),
+                                              1 if keep_layers else 0), "pcvl_slos_plan_create")
+        self._h = h
+        self.m, self.batch, self.keep_layers = m, batch, keep_layers
+        self.input_state = tuple(int(v) for v in inp)
+        c = ctypes.c_int64()
+        check(self._lib.pcvl_slos_output_count(h, ctypes.byref(c)), "pcvl_slos_output_count")
+        self.count = int(c.value)
+
+    @property
+    def device_bytes(self) -> int:
+        b = ctypes.c_int64()
+        check(self._lib.pcvl_slos_plan_bytes(self._h, ctypes.byref(b)), "pcvl_slos_plan_bytes")
+        return int(b.value)
+
+    def forward(self, u: torch.Tensor, stream=None):
+        _dev_tensor(u, torch.complex128, "u")
+        if u.numel() != self.batch * self.m * self.m:
+            raise ValueError("u must hold batch x m x m elements")
+        check(self._lib.pcvl_slos_forward(self._h, u.data_ptr(), _stream_ptr(stream)), "pcvl_slos_forward")
+
+    def probabilities(self, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        if out is None:
+            out = torch.empty(self.count * self.batch, dtype=torch.float64, device="cuda")
+        _dev_tensor(out, torch.float64, "out")
+        check(self._lib.pcvl_slos_probabilities(self._h, out.data_ptr(), _stream_ptr(stream)),
+              "pcvl_slos_probabilities")
+        return out
+
+    def amplitudes(self, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        if out is None:
+            out = torch.empty(self.count * self.batch, dtype=torch.complex128, device="cuda")
+        _dev_tensor(out, torch.complex128, "out")
+        check(self._lib.pcvl_slos_amplitudes(self._h, out.data_ptr(), _stream_ptr(stream)),
+              "pcvl_slos_amplitudes")
+        return out
+
+    def backward(self, weights: torch.Tensor, grad_u: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        _dev_tensor(weights, torch.float64, "weights")
+        if weights.numel() != self.count * self.batch:
+            raise ValueError("weights must hold count x batch elements (state-major)")
+        if grad_u is None:
+            grad_u = torch.empty(self.batch * self.m * self.m, dtype=torch.complex128, device="cuda")
+        _dev_tensor(grad_u, torch.complex128, "grad_u")
+        check(self._lib.pcvl_slos_backward(self._h, weights.data_ptr(), grad_u.data_ptr(), _stream_ptr(stream)),
+              "pcvl_slos_backward")
+        return grad_u
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.pcvl_slos_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------------ sampling
+def cc2017_sample(u: torch.Tensor, input_state, count: int, seed: int, first_sample: int = 0,
+                  precision: int = 0, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+    """Exact boson samples (Clifford & Clifford 2018); returns int32 counts (count, m)."""
+    lib = load()
+    _dev_tensor(u, torch.complex128, "u")
+    m = u.shape[-1]
+    inp = np.ascontiguousarray(input_state, dtype=np.int32)
+    if inp.shape != (m,):
+        raise ValueError("input_state must have m entries")
+    if out is None:
+        out = torch.empty((count, m), dtype=torch.int32, device="cuda")
+    _dev_tensor(out, torch.int32, "out")
+    check(lib.pcvl_cc2017_sample(u.data_ptr(), int(m), inp.ctypes.data, int(count), int(seed) & (2**64 - 1),
+                                 int(first_sample), int(precision), out.data_ptr(), _stream_ptr(stream)),
+          "pcvl_cc2017_sample")
+    return out

@@ -1,0 +1,55 @@
+"""Exact boson sampling on the GPU (restating perceval/backends/_clifford2017.py:36-61).
+
+``samples(count)`` draws all samples in one ``pcvl_cc2017_sample`` launch (one CTA
+per sample, Clifford & Clifford 2018 algorithm B).  Randomness comes from
+Philox4x32-10 keyed by the seed of ``perceval_gb300.utils.random_seed``; every
+sample has its own counter, so a fixed seed gives the same samples however the
+launch is scheduled, and successive calls continue the stream.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .. import _native
+from ..utils import _random
+from ..utils.states import BSSamples, FockState
+from ._abstract_backends import ASamplingBackend
+
+
+class Clifford2017Backend(ASamplingBackend):
+    def __init__(self, precision: str = "double"):
+        super().__init__()
+        if precision not in ("double", "single"):
+            raise ValueError("precision must be 'double' (float-float) or 'single' (FP32)")
+        self._precision = 0 if precision == "double" else 1
+        self._u_dev = None
+
+    @property
+    def name(self) -> str:
+        return "CliffordClifford2017"
+
+    def set_circuit(self, circuit):
+        super().set_circuit(circuit)
+        self._u_dev = None
+
+    def _unitary_device(self) -> torch.Tensor:
+        if self._u_dev is None:
+            _native.load()
+            self._u_dev = torch.from_numpy(self._umat).to("cuda")
+        return self._u_dev
+
+    def samples_tensor(self, count: int) -> torch.Tensor:
+        """``count`` samples as an int32 CUDA tensor of shape (count, m)."""
+        assert self._input_state is not None, "Input state must be set before sampling"
+        seed, first = _random.take_samples(count)
+        return _native.cc2017_sample(self._unitary_device(), list(self._input_state), count, seed, first,
+                                     self._precision)
+
+    def samples(self, count: int) -> BSSamples:
+        """Request ``count`` samples; one GPU launch draws them all."""
+        arr = self.samples_tensor(count).cpu().numpy()
+        return BSSamples(FockState(row) for row in arr)
+
+    def sample(self) -> FockState:
+        return self.samples(1)[0]

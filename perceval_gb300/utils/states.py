@@ -1,0 +1,362 @@
+"""Fock-state containers used at the backend boundary.
+
+The reference aliases these to closed native types (perceval/utils/states.py:42-49:
+``FockState``, ``BasicState``, ``BSDistribution``, ``BSSamples``, ``BSCount``,
+``StateVector``).  They are restated here as small pure-Python containers with the
+same observable behaviour that the backend API relies on:
+
+* ``FockState`` is an immutable, hashable occupation vector with ``m``, ``n``,
+  ``prodnfact()``, indexing, iteration and the ``|a,b,c>`` text form.
+* ``StateVector`` maps ``FockState`` to complex amplitudes, supports ``+``, ``-``
+  and scalar ``*`` and ``normalize()``.
+* ``BSDistribution`` maps ``FockState`` to probabilities (``add`` accumulates).
+* ``BSSamples`` is a list of ``FockState``; ``BSCount`` counts them.
+
+Enumeration order follows the reference: descending lexicographic order of the
+occupation vector within a fixed photon number
+(tests/utils/test_statevector.py:430-438, perceval/utils/states.py:268-298).
+"""
+from __future__ import annotations
+
+import math
+import re
+from typing import Iterable, Iterator, Sequence
+
+import numpy as np
+
+from .globals import global_params
+
+_MIN_P = global_params["min_p"]
+
+class FockState(tuple):
+    """Occupation numbers of m optical modes (photon counts per mode)."""
+
+    __slots__ = ()
+
+    def __new__(cls, state: "Sequence[int] | str | int" = ()):
+        if isinstance(state, FockState):
+            return state
+        if isinstance(state, str):
+            state = _parse_state(state)
+        elif isinstance(state, (int, np.integer)):
+            state = [0] * int(state)
+        vals = tuple(int(v) for v in state)
+        if any(v < 0 for v in vals):
+            raise ValueError("photon counts must be non-negative")
+        return super().__new__(cls, vals)
+
+    @property
+    def m(self) -> int:
+        return len(self)
+
+    @property
+    def n(self) -> int:
+        return sum(self)
+
+    def prodnfact(self) -> int:
+        """Product of the factorials of the per-mode photon counts."""
+        p = 1
+        for v in self:
+            p *= math.factorial(v)
+        return p
+
+    def photon2mode(self, k: int) -> int:
+        """Mode index of the k-th photon (photons ordered by mode)."""
+        acc = 0
+        for i, v in enumerate(self):
+            acc += v
+            if k < acc:
+                return i
+        raise IndexError(k)
+
+    def __str__(self) -> str:
+        return "|" + ",".join(str(v) for v in self) + ">"
+
+    def __repr__(self) -> str:
+        return str(self)
+
+    def __mul__(self, other):
+        if isinstance(other, FockState):
+            # tensor product of two Fock states
+            return FockState(tuple(self) + tuple(other))
+        if isinstance(other, (int, float, complex, np.number)):
+            return StateVector({self: complex(other)})
+        return NotImplemented
+
+    def __rmul__(self, other):
+        if isinstance(other, (int, float, complex, np.number)):
+            return StateVector({self: complex(other)})
+        return NotImplemented
+
+    def __add__(self, other):
+        return StateVector(self) + other
+
+    def __getitem__(self, item):
+        res = tuple.__getitem__(self, item)
+        if isinstance(item, slice):
+            return FockState(res)
+        return res
+
+
+BasicState = FockState
+
+
+def _parse_state(s: str) -> list[int]:
+    s = s.strip()
+    m = re.fullmatch(r"\|([0-9,\s]*)>", s)
+    if not m:
+        raise ValueError(f"cannot parse Fock state {s!r}")
+    body = m.group(1).strip()
+    if not body:
+        return []
+    return [int(x) for x in body.split(",")]
+
+
+class StateVector(dict):
+    """Superposition of Fock states: ``FockState -> complex`` amplitude."""
+
+    def __init__(self, init=None):
+        super().__init__()
+        if init is None:
+            return
+        if isinstance(init, dict):
+            for k, v in init.items():
+                self[FockState(k)] = complex(v)
+        else:
+            self[FockState(init)] = 1.0 + 0j
+
+    @property
+    def m(self) -> int:
+        return next(iter(self)).m if self else 0
+
+    def __add__(self, other):
+        res = StateVector(dict(self))
+        if isinstance(other, FockState):
+            other = StateVector(other)
+        for k, v in other.items():
+            res[k] = res.get(k, 0j) + v
+        return res
+
+    __iadd__ = __add__
+
+    def __sub__(self, other):
+        return self + (-1) * (StateVector(other) if isinstance(other, FockState) else other)
+
+    def __mul__(self, scalar):
+        if not isinstance(scalar, (int, float, complex, np.number)):
+            return NotImplemented
+        return StateVector({k: v * scalar for k, v in self.items()})
+
+    __rmul__ = __mul__
+
+    def __neg__(self):
+        return self * -1
+
+    def normalize(self):
+        """Drop numerically-zero amplitudes (|a|^2 < min_p) and rescale to unit norm."""
+        for k in [k for k, v in self.items() if abs(v) ** 2 < _MIN_P]:
+            del self[k]
+        norm = math.sqrt(sum(abs(v) ** 2 for v in self.values()))
+        if norm > 0:
+            for k in self:
+                self[k] /= norm
+        return self
+
+
+class BSDistribution(dict):
+    """Probability distribution over Fock states.
+
+    ``add`` ignores probabilities below ``global_params["min_p"]`` (1e-16): the
+    reference's distributions leave numerically-zero outputs out (a masked CNOT
+    distribution has exactly its two non-zero outputs,
+    tests/backends/test_backends.py:203-218).
+    """
+
+    def add(self, state: FockState, p: float):
+        p = float(p)
+        if p < _MIN_P:
+            return
+        state = FockState(state)
+        self[state] = self.get(state, 0.0) + p
+
+    def normalize(self):
+        tot = sum(self.values())
+        if tot > 0:
+            for k in self:
+                self[k] /= tot
+        return self
+
+
+class BSCount(dict):
+    """Occurrence counts of Fock states (missing keys count 0)."""
+
+    def __missing__(self, key):
+        return 0
+
+    def __getitem__(self, key):
+        return dict.get(self, FockState(key), 0)
+
+    def __setitem__(self, key, value):
+        dict.__setitem__(self, FockState(key), value)
+
+
+class BSSamples(list):
+    """List of sampled Fock states."""
+
+
+# ----------------------------------------------------------------------------------
+# Fock-space enumeration (the FSArray equivalent), descending lexicographic order.
+# ----------------------------------------------------------------------------------
+
+def fock_space_size(m: int, n: int) -> int:
+    """Number of n-photon states on m modes: C(m+n-1, n)."""
+    if m <= 0:
+        return 1 if n == 0 else 0
+    return math.comb(m + n - 1, n)
+
+
+def fock_space_array(m: int, n: int) -> np.ndarray:
+    """All n-photon occupation vectors on m modes, descending-lex order, as an int array.
+
+    Row r is the state of rank r (the index used by ``all_prob``).  Built by the
+    block recursion of descending-lex order: states with first-mode count a form a
+    contiguous block, blocks ordered from a = n down to 0.
+    """
+    if m == 0:
+        return np.zeros((1 if n == 0 else 0, 0), dtype=np.int32)
+    if m == 1:
+        return np.array([[n]], dtype=np.int32)
+    blocks = []
+    for a in range(n, -1, -1):
+        tail = fock_space_array(m - 1, n - a)
+        blk = np.empty((tail.shape[0], m), dtype=np.int32)
+        blk[:, 0] = a
+        blk[:, 1:] = tail
+        blocks.append(blk)
+    return np.concatenate(blocks, axis=0)
+
+
+def fock_rank(state: Sequence[int]) -> int:
+    """Rank of a state in descending-lex order of its (m, n) Fock space.
+
+    rank(s) = sum_i count(m - i, r_{i+1} - 1) where r_{i+1} is the number of photons
+    in modes after i: every state with a larger count in mode i (and equal counts
+    before) precedes s, and those form count(m - i, r_{i+1} - 1) states.
+    """
+    m = len(state)
+    rest = sum(state)
+    rank = 0
+    for i, v in enumerate(state):
+        rest -= v
+        if rest > 0:
+            rank += fock_space_size(m - i, rest - 1)
+    return rank
+
+
+def fock_unrank(m: int, n: int, rank: int) -> FockState:
+    """Inverse of ``fock_rank``."""
+    out = []
+    rest = n
+    for i in range(m - 1):
+        # choose the count v in mode i: blocks for v = rest, rest-1, ..., 0
+        v = rest
+        while True:
+            blk = fock_space_size(m - i - 1, rest - v)
+            if rank < blk:
+                break
+            rank -= blk
+            v -= 1
+        out.append(v)
+        rest -= v
+    out.append(rest)
+    return FockState(out)
+
+
+def allstate_iterator(input_state, mask=None) -> Iterator[FockState]:
+    """Iterate all output states with the input's photon number(s), respecting a mask.
+
+    Follows perceval/utils/states.py:268-290 (order of ``FSArray`` iteration).
+    """
+    m = input_state.m
+    if isinstance(input_state, StateVector):
+        ns = sorted({s.n for s in input_state})
+    else:
+        ns = [input_state.n]
+    for n in ns:
+        arr = fock_space_array(m, n)
+        if mask is not None:
+            arr = arr[mask.match_array(arr)]
+        for row in arr:
+            yield FockState(row)
+
+
+def max_photon_state_iterator(m: int, n_max: int) -> Iterator[FockState]:
+    """All states on m modes with 0..n_max photons (perceval/utils/states.py:292-298)."""
+    for n in range(n_max + 1):
+        for row in fock_space_array(m, n):
+            yield FockState(row)
+
+
+class FSMask:
+    """Restriction of a Fock space by per-mode conditions.
+
+    Restates the mask semantics used by ``AStrongSimulationBackend.set_mask``
+    (perceval/backends/_abstract_backends.py:103-137; tests/utils/test_mask.py:32-45):
+    each mask string has one character per mode; a digit fixes the photon count of
+    that mode, a space or ``*`` accepts any count.  A state is accepted when it
+    matches at least one mask string.  Modes listed in ``at_least_modes`` accept any
+    count greater than or equal to their digit.  ``match(state, partial=True)``
+    accepts states with fewer photons that can still be completed to a match with
+    the ``n`` photons the mask was built for.
+    """
+
+    def __init__(self, m: int, n: int, masks: Iterable[str], at_least_modes=None):
+        self.m = m
+        self.n = n
+        self._conds = []
+        at_least = set(at_least_modes or [])
+        for s in masks:
+            s = s.replace("*", " ")
+            assert len(s) == m, "Mask and state lengths have to be the same"
+            cond = []
+            for i, ch in enumerate(s):
+                if ch == " ":
+                    continue
+                cond.append((i, int(ch), i in at_least))
+            self._conds.append(cond)
+
+    def match(self, state, partial: bool = False) -> bool:
+        state = FockState(state)
+        for cond in self._conds:
+            if self._match_one(cond, state, partial):
+                return True
+        return False
+
+    def _match_one(self, cond, state, partial) -> bool:
+        missing = 0
+        for i, d, at_least in cond:
+            v = state[i]
+            if at_least:
+                if v < d:
+                    if not partial:
+                        return False
+                    missing += d - v
+            elif partial:
+                if v > d:
+                    return False
+                missing += d - v
+            elif v != d:
+                return False
+        if partial:
+            return missing <= self.n - state.n
+        return True
+
+    def match_array(self, arr: np.ndarray) -> np.ndarray:
+        """Vectorised ``match`` over rows of an occupation array (full match only)."""
+        ok = np.zeros(arr.shape[0], dtype=bool)
+        for cond in self._conds:
+            cur = np.ones(arr.shape[0], dtype=bool)
+            for i, d, at_least in cond:
+                cur &= (arr[:, i] >= d) if at_least else (arr[:, i] == d)
+            ok |= cur
+        return ok

@@ -1,0 +1,144 @@
+"""The reference's backend tests (tests/backends/test_backends.py) as known-answer
+data, run through BackendFactory on the GPU backends."""
+import math
+
+import numpy as np
+import pytest
+
+from _circuits import build
+from perceval_gb300 import BackendFactory, BasicState, BSCount, Circuit
+from perceval_gb300.components import BS, catalog
+from perceval_gb300.utils.matrix import random_unitary
+
+pytestmark = pytest.mark.gpu
+STRONG = ["SLOS", "Naive"]
+
+
+def check_output_distribution(backend, input_state, expected):
+    # mirrors tests/backends/test_backends.py:70-81
+    backend.set_input_state(input_state)
+    probs = []
+    for out, p in backend.prob_distribution().items():
+        assert p == pytest.approx(expected.get(str(out), 0.0), abs=1e-12), str(out)
+        probs.append(p)
+    assert sum(probs) == pytest.approx(1)
+
+
+@pytest.mark.parametrize("name", STRONG)
+def test_kat_distributions(native, kats, name):
+    for case in kats["distributions"]:
+        b = BackendFactory.get_backend(name)
+        b.set_circuit(build(case["m"], case["ops"]))
+        check_output_distribution(b, BasicState(case["input"]), case["expected"])
+
+
+@pytest.mark.parametrize("name", STRONG)
+def test_kat_cnot(native, kats, name):
+    for group in kats["probabilities"]:
+        b = BackendFactory.get_backend(name)
+        b.set_circuit(build(group["m"], group["ops"]))
+        for inp, out, p in group["cases"]:
+            b.set_input_state(BasicState(inp))
+            assert b.probability(BasicState(out)) == pytest.approx(p, abs=1e-12)
+    case = kats["heralded_mass"][0]
+    b = BackendFactory.get_backend(name)
+    b.set_circuit(build(case["m"], case["ops"]))
+    b.set_input_state(BasicState(case["input"]))
+    mass = sum(p for s, p in b.prob_distribution().items() if any(s[k] for k in case["modes"]))
+    assert mass == pytest.approx(case["expected"])
+
+
+@pytest.mark.parametrize("name", STRONG)
+def test_kat_masks(native, kats, name):
+    case = kats["masked"][0]
+    b = BackendFactory.get_backend(name)
+    b.set_mask(case["mask"])
+    b.set_circuit(build(case["m"], case["ops"]))
+    b.set_input_state(BasicState(case["input"]))
+    bsd = b.prob_distribution()
+    assert len(bsd) == 2
+    for s, p in case["expected"].items():
+        assert bsd[BasicState(s)] == pytest.approx(p)
+    case = kats["masked"][1]
+    b = BackendFactory.get_backend(name)
+    b.set_mask([case["mask"]])
+    b.set_circuit(build(case["m"], case["ops"]))
+    b.set_input_state(BasicState(case["input"]))
+    mass = sum(p for s, p in b.prob_distribution().items() if any(s[k] for k in case["heralded_modes"]))
+    assert mass == pytest.approx(case["heralded_expected"])
+
+
+@pytest.mark.parametrize("name", STRONG)
+def test_kat_amplitudes_and_evolve(native, kats, name):
+    for case in kats["amplitudes"]:
+        b = BackendFactory.get_backend(name)
+        b.set_circuit(build(case["m"], case["ops"]))
+        b.set_input_state(BasicState(case["input"]))
+        assert b.prob_amplitude(BasicState(case["output"])) == pytest.approx(complex(*case["expected"]))
+    for case in kats["evolve"]:
+        b = BackendFactory.get_backend(name)
+        b.set_circuit(build(case["m"], case["ops"]))
+        b.set_input_state(BasicState(case["input"]))
+        sv = b.evolve()
+        sv.normalize()
+        assert {str(k) for k in sv} == set(case["expected"])
+        for s, v in case["expected"].items():
+            assert sv[BasicState(s)] == pytest.approx(complex(*v))
+
+
+def test_slos_refresh_coefs(native):
+    # tests/backends/test_backends.py:252-277
+    slos = BackendFactory.get_backend("SLOS")
+    slos.set_circuit(BS())
+    slos.set_input_state(BasicState("|1,1>"))
+    slos.set_input_state(BasicState("|8,5>"))
+    check_output_distribution(slos, BasicState("|1,1>"), {"|0,2>": 0.5, "|2,0>": 0.5})
+    slos.set_circuit(Circuit(2))
+    check_output_distribution(slos, BasicState("|1,1>"), {"|1,1>": 1.0})
+
+
+def test_slos_equals_naive_on_random_circuit(native):
+    U = random_unitary(7, seed=11)
+    inp = BasicState([1, 0, 2, 0, 1, 0, 1])
+    s, n = BackendFactory.get_backend("SLOS"), BackendFactory.get_backend("Naive")
+    for b in (s, n):
+        b.set_circuit(U)
+        b.set_input_state(inp)
+    ps, pn = np.array(s.all_prob()), np.array(n.all_prob())
+    assert np.abs(ps - pn).max() <= 1e-10 * ps.max()
+    out = BasicState([0, 2, 0, 1, 1, 1, 0])
+    assert abs(s.prob_amplitude(out) - n.prob_amplitude(out)) <= 1e-10 * abs(n.prob_amplitude(out))
+    assert s.prob_amplitude(BasicState([1] * 7)) == 0
+
+
+def test_naive_batched_collision_free_outputs(native, oracle):
+    # the small-configuration second half: Naive amplitudes of collision-free outputs
+    U = random_unitary(12, seed=0)
+    inp = BasicState([1] * 6 + [0] * 6)
+    rng = np.random.default_rng(0)
+    outs = []
+    for _ in range(50):
+        o = np.zeros(12, dtype=int)
+        o[rng.choice(12, 6, replace=False)] = 1
+        outs.append(BasicState(o))
+    b = BackendFactory.get_backend("Naive")
+    b.set_circuit(U)
+    b.set_input_state(inp)
+    got = b.prob_amplitudes(outs)
+    _, ref = oracle.slos(U, list(inp))
+    from perceval_gb300.utils import fock_rank
+    want = np.array([ref[fock_rank(o)] for o in outs])
+    assert np.abs(got - want).max() <= 1e-10 * np.abs(want).max()
+
+
+def test_clifford_bs_kat(native, kats):
+    case = kats["sampling"][0]
+    b = BackendFactory.get_backend("CliffordClifford2017")
+    b.set_circuit(build(case["m"], case["ops"]))
+    b.set_input_state(BasicState(case["input"]))
+    counts = BSCount()
+    for s in b.samples(case["samples"]):
+        counts[s] += 1
+    for o in case["outcomes"]:
+        assert case["band"][0] * case["samples"] < counts[BasicState(o)] < case["band"][1] * case["samples"]
+    assert isinstance(b.sample(), BasicState)

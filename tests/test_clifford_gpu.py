@@ -1,0 +1,67 @@
+"""GPU Clifford & Clifford sampler: sample-by-sample agreement with the CPU oracle
+(same Philox stream and draw procedure) and chi-square agreement with the exact
+SLOS distribution (p > 0.01)."""
+import numpy as np
+import pytest
+import torch
+
+from _stats import chi2_pvalue
+from perceval_gb300.utils import fock_rank
+from perceval_gb300.utils.matrix import random_unitary
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("m,inp,precision", [
+    (5, (1, 1, 1, 0, 0), 0), (6, (2, 0, 1, 0, 1, 0), 0), (8, (1, 1, 1, 1, 1, 1, 0, 0), 0),
+    (10, (1,) * 10, 0), (12, (2, 2, 0, 0, 1, 1, 1, 1, 0, 0, 0, 1), 0), (6, (2, 0, 1, 0, 1, 0), 1)])
+def test_samples_equal_oracle(native, oracle, m, inp, precision):
+    U = random_unitary(m, seed=m)
+    N = 300
+    got = native.cc2017_sample(torch.from_numpy(U).cuda(), inp, N, seed=42, first_sample=7,
+                               precision=precision).cpu().numpy()
+    ref = oracle.cc2017(U, inp, N, seed=42, first=7)
+    assert got.shape == ref.shape
+    agree = np.all(got == ref, axis=1).mean()
+    # a different draw needs u within ~1e-13 (float-float) / ~1e-5 (FP32) of a CDF boundary
+    assert agree >= (1.0 if precision == 0 else 0.98), agree
+    assert np.all(got.sum(axis=1) == sum(inp))
+
+
+@pytest.mark.parametrize("inp", [(1, 1, 1, 0, 0, 0), (2, 1, 0, 0, 0, 1)])
+def test_chi_square_vs_exact(native, oracle, inp):
+    m = len(inp)
+    U = random_unitary(m, seed=21)
+    probs, _ = oracle.slos(U, inp)
+    N = 200000
+    got = native.cc2017_sample(torch.from_numpy(U).cuda(), inp, N, seed=9).cpu().numpy()
+    idx = np.array([fock_rank(r) for r in got])
+    counts = np.bincount(idx, minlength=len(probs))
+    assert chi2_pvalue(counts, probs) > 0.01
+
+
+def test_reproducible_and_streams_disjoint(native):
+    U = torch.from_numpy(random_unitary(16, seed=3)).cuda()
+    inp = (1,) * 8 + (0,) * 8
+    a = native.cc2017_sample(U, inp, 64, seed=5).cpu().numpy()
+    b = native.cc2017_sample(U, inp, 64, seed=5).cpu().numpy()
+    c = native.cc2017_sample(U, inp, 32, seed=5, first_sample=32).cpu().numpy()
+    assert np.array_equal(a, b) and np.array_equal(a[32:], c)
+    d = native.cc2017_sample(U, inp, 64, seed=6).cpu().numpy()
+    assert not np.array_equal(a, d)
+
+
+def test_larger_n_marginals(native):
+    # n = 20 on m = 400 (the sampling workload's size): one-mode marginals match the
+    # exact mean occupations E[n_i] = sum_j |U_ij|^2 over occupied inputs
+    m, n = 400, 20
+    U = random_unitary(m, seed=0)
+    inp = (1,) * n + (0,) * (m - n)
+    N = 4000
+    got = native.cc2017_sample(torch.from_numpy(U).cuda(), inp, N, seed=1).cpu().numpy()
+    assert np.all(got.sum(axis=1) == n)
+    mean = got.mean(axis=0)
+    exact = (np.abs(U[:, :n]) ** 2).sum(axis=1)
+    z = (mean - exact) / np.sqrt(exact / N + 1e-12)
+    assert np.abs(z).max() < 6
+    assert abs(mean.sum() - n) < 1e-9

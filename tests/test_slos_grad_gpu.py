@@ -1,0 +1,106 @@
+"""SLOS adjoint: GPU dL/dU against the oracle's reverse sweep, central finite
+differences (h = 1e-6) and float64 torch autograd through dense permanents; and the
+chain rule to the phases of a Clements mesh of MZIs."""
+import itertools
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from perceval_gb300.components.mesh import clements_mesh_phase_count, clements_mesh_unitary
+from perceval_gb300.utils import fock_space_array
+from perceval_gb300.utils.matrix import random_unitary
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_grad(native, Us, inp, w):
+    B, m = Us.shape[0], Us.shape[1]
+    plan = native.SlosPlan(m, inp, batch=B, keep_layers=True)
+    plan.forward(torch.from_numpy(np.ascontiguousarray(Us)).cuda())
+    p = plan.probabilities().cpu().numpy().reshape(-1, B)
+    g = plan.backward(torch.from_numpy(np.ascontiguousarray(w.reshape(-1))).cuda()).cpu().numpy()
+    return p, g.reshape(B, m, m)
+
+
+@pytest.mark.parametrize("B", [1, 3, 40])
+def test_grad_vs_oracle(native, oracle, B):
+    m, inp = 6, (1, 0, 2, 1, 0, 0)
+    Us = np.stack([random_unitary(m, seed=50 + b) for b in range(B)])
+    count = math.comb(m + 4 - 1, 4)
+    w = np.random.default_rng(1).normal(size=(count, B))
+    p, g = gpu_grad(native, Us, inp, w)
+    for b in {0, B // 2, B - 1}:
+        ref = oracle.slos_grad(Us[b], inp, w[:, b])
+        assert np.abs(g[b] - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
+def perm_torch(a):
+    n = a.shape[0]
+    tot = torch.zeros((), dtype=a.dtype)
+    for S in range(1, 1 << n):
+        cols = [j for j in range(n) if S >> j & 1]
+        tot = tot + (-1) ** len(cols) * torch.prod(a[:, cols].sum(dim=1))
+    return (-1) ** n * tot
+
+
+def test_grad_vs_torch_dense_permanent(native):
+    m, inp = 4, (1, 1, 0, 1)
+    U = random_unitary(m, seed=8)
+    states = fock_space_array(m, 3)
+    w = np.random.default_rng(2).normal(size=len(states))
+    Ut = torch.tensor(U, dtype=torch.complex128, requires_grad=True)
+    cols = [i for i, v in enumerate(inp) for _ in range(v)]
+    L = torch.zeros((), dtype=torch.float64)
+    for s, ws in zip(states, w):
+        rows = [j for j, v in enumerate(s) for _ in range(v)]
+        f = math.prod(math.factorial(int(v)) for v in s)
+        L = L + ws * perm_torch(Ut[rows][:, cols]).abs() ** 2 / f
+    L.backward()
+    _, g = gpu_grad(native, U[None], inp, w[:, None])
+    assert np.abs(g[0] - Ut.grad.numpy()).max() <= 1e-10 * np.abs(Ut.grad.numpy()).max()
+
+
+def test_mesh_phase_gradient_vs_finite_differences(native):
+    m, n = 6, 3
+    inp = [1] * n + [0] * (m - n)
+    K = clements_mesh_phase_count(m)
+    B = 2
+    phases = torch.tensor(np.random.default_rng(3).uniform(0, 2 * math.pi, (B, K)), requires_grad=True)
+    count = math.comb(m + n - 1, n)
+    w = np.random.default_rng(4).normal(size=(count, B))
+    U = clements_mesh_unitary(phases, m)
+    _, g = gpu_grad(native, U.detach().numpy(), inp, w)
+    U.backward(torch.from_numpy(g))
+    dphi = phases.grad.numpy()
+    plan = native.SlosPlan(m, inp, batch=B)
+    wd = torch.from_numpy(w.reshape(-1)).cuda()
+
+    def loss(ph):
+        Ux = clements_mesh_unitary(torch.from_numpy(ph), m).contiguous()
+        plan.forward(Ux.cuda())
+        return (plan.probabilities() * wd).reshape(count, B).sum(dim=0).cpu().numpy()
+
+    h = 1e-6
+    base = phases.detach().numpy()
+    for k in (0, 7, K - 1):
+        up, dn = base.copy(), base.copy()
+        up[:, k] += h
+        dn[:, k] -= h
+        fd = (loss(up) - loss(dn)) / (2 * h)
+        assert np.allclose(dphi[:, k], fd, rtol=1e-6, atol=1e-8)
+
+
+def test_config_clements_m16_n8_batch(native, oracle):
+    # the gradient workload's shape on 8 circuits: m = 16, n = 8, 490,314 outputs
+    m, n, B = 16, 8, 8
+    K = clements_mesh_phase_count(m)
+    phases = torch.tensor(np.random.default_rng(0).uniform(0, 2 * math.pi, (B, K)))
+    U = clements_mesh_unitary(phases, m).numpy()
+    count = math.comb(m + n - 1, n)
+    w = np.random.default_rng(0).normal(size=(count, B))
+    p, g = gpu_grad(native, U, [1] * n + [0] * (m - n), w)
+    assert np.abs(p.sum(axis=0) - 1).max() < 1e-11
+    ref = oracle.slos_grad(U[3], [1] * n + [0] * (m - n), w[:, 3])
+    assert np.abs(g[3] - ref).max() <= 1e-10 * np.abs(ref).max()
