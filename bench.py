@@ -1,0 +1,448 @@
+#!/usr/bin/env python3
+"""Benchmark of the linear-optics hot path on GB300.
+
+Headline workload (one step = one pass over one batch): exact permanents of 8192
+complex128 Haar submatrices, n uniform in 8..24, rows/columns drawn without
+replacement from a 1024x1024 Haar unitary (seed 0), all in one
+pcvl_permanent_batch call (size bins launched back to back).  `value` is perms/s
+with the matrices resident in HBM; `e2e` is the same through the C ABI from pinned
+host buffers with both copies inside the timed region.
+
+Secondary lines in the same JSON: SLOS full distribution m=24/n=12 (amplitudes/s,
+HBM roofline), batched SLOS forward+adjoint on 256 Clements meshes m=16/n=8,
+Clifford & Clifford sampling n=20/m=400, and the small m=12/n=6 SLOS + 1000 Naive
+amplitudes case.
+
+`--impl reference` times the CPU restatement of the reference path (the C oracle,
+OpenMP on every host core) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Haar perms/s & SLOS amps/s (frac. of roofline); ESS/s MCMC vs exact sampler"
+WORKLOAD = ("8192 Haar-submatrix permanents, n~U{8..24}, rows/cols without replacement from a "
+            "1024x1024 Haar unitary (numpy legacy seed 0; sizes/rows/cols from default_rng(seed))")
+N_MATS, BIG = 8192, 1024
+
+
+def make_batch(seed: int):
+    from perceval_gb300.utils.matrix import random_unitary
+    U = random_unitary(BIG, seed=0)
+    rng = np.random.default_rng(seed)
+    mats = []
+    for _ in range(N_MATS):
+        n = int(rng.integers(8, 25))
+        mats.append(np.ascontiguousarray(U[np.ix_(rng.choice(BIG, n, False), rng.choice(BIG, n, False))]))
+    sizes = np.array([a.shape[0] for a in mats], dtype=np.int32)
+    offs = np.zeros(N_MATS, dtype=np.int64)
+    offs[1:] = np.cumsum([a.size for a in mats])[:-1]
+    flat = np.concatenate([a.reshape(-1) for a in mats])
+    return mats, flat, offs, sizes
+
+
+def glynn_flops(n) -> float:
+    """Algorithmic FP64 flops of one n x n Glynn permanent: 2^(n-1) (8n - 4)."""
+    return (2.0 ** (n - 1)) * (8 * n - 4)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, out: Path):
+        self.out = out
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.out, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self) -> dict:
+        try:
+            rows = [r.split(",") for r in self.out.read_text().strip().splitlines() if r.strip()]
+        except OSError:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = max(float(r[2]) for r in rows)
+        power = [float(r[3]) for r in rows if r[3].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
+        loaded = [s for s, p in zip(sm, power) if p > 0.5 * max(power)] if power else sm
+        return {"sm_mhz": statistics.median(loaded or sm), "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(power) if power else None}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def measured_fp64_peak(torch) -> float:
+    """cuBLAS DGEMM 4096^3, best of 5, TFLOP/s (the FP64 roofline denominator)."""
+    a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(5):
+        s, e = torch.cuda.Event(True), torch.cuda.Event(True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e))
+    return 2 * 4096 ** 3 / (best * 1e-3) / 1e12
+
+
+def traffic_from_profile(name: str):
+    p = ROOT / "profiles" / f"{name}.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()).get("dram_bytes_per_launch")
+        except (OSError, ValueError):
+            return None
+    return None
+
+
+# ----------------------------------------------------------------------------- CPU
+def cpu_perm_baseline(budget_s: float = 15.0) -> dict:
+    """Oracle (C, OpenMP, all host threads) on a stratified sample: per size n,
+    timed matrices of that size; the full batch time is extrapolated by the counts."""
+    from oracle import oracle
+    _, flat, offs, sizes = make_batch(seed=0)
+    counts = np.bincount(sizes, minlength=25)
+    per_n, used = {}, {}
+    spent = 0.0
+    for n in range(8, 25):
+        idx = np.nonzero(sizes == n)[0]
+        t0 = time.perf_counter()
+        k = 0
+        # each size gets an equal share of the budget (at least one matrix)
+        while k < len(idx) and (k == 0 or time.perf_counter() - t0 < budget_s / 17):
+            i = idx[k]
+            oracle.perm(flat[offs[i]:offs[i] + n * n].reshape(n, n))
+            k += 1
+        dt = time.perf_counter() - t0
+        per_n[n] = dt / k
+        used[n] = k
+        spent += dt
+    total = sum(counts[n] * per_n[n] for n in range(8, 25))
+    return {"value": N_MATS / total, "unit": "perms/s", "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"{sum(used.values())} matrices of the batch, every size n=8..24 "
+                      f"({used[24]} of n=24), {spent:.1f} s of CPU work; full-batch time extrapolated "
+                      f"from the per-size times and the size counts"}
+
+
+def run_reference(args):
+    ws, rank = dist_setup()
+    if rank != 0:
+        return
+    from oracle import oracle
+    oracle.build()
+    vals = []
+    for _ in range(args.warmup):
+        cpu_perm_baseline(budget_s=1.0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_perm_baseline(budget_s=8.0))
+    wall = time.perf_counter() - t0
+    v = statistics.median(x["value"] for x in vals)
+    cb = dict(vals[0])
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "perms/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "complex128 (FP64)",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "implementation": "CPU oracle restating the "
+                                            "reference path (exqalibur is closed and absent)"},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "perms/s", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU
+def run_ours(args):
+    import torch
+    ws, rank = dist_setup()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    from perceval_gb300 import _native
+    from perceval_gb300.utils.matrix import random_unitary
+    _native.load()
+    dev = torch.device("cuda")
+    out_dir = ROOT / "gpurun_out"
+    out_dir.mkdir(exist_ok=True)
+
+    mats, flat, offs, sizes = make_batch(seed=rank)
+    flops_total = float(sum(glynn_flops(int(n)) for n in sizes))
+    flat_d = torch.from_numpy(flat).to(dev)
+    out_d = torch.empty(N_MATS, dtype=torch.complex128, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    bins = len(set(int(n) for n in sizes))
+    launches_per_step = bins + 2  # prepare + one per size bin + reduce
+
+    def step():
+        _native.permanent_batch(flat_d, offs, sizes, out_d)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    ev = [(torch.cuda.Event(True), torch.cuda.Event(True)) for _ in range(args.steps)]
+    clocks = Clocks(out_dir / "bench_clocks.csv")
+    with clocks:
+        barrier()
+        for s, e in ev:
+            flush.zero_()  # L2 flush between timed steps, outside the events
+            s.record()
+            step()
+            e.record()
+        barrier()
+    ms = sum(s.elapsed_time(e) for s, e in ev)
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t)
+    value = ws * N_MATS * args.steps / (ms * 1e-3)
+
+    # e2e through the C ABI from pinned host buffers (copies inside the timed region)
+    host_in = torch.from_numpy(flat).pin_memory()
+    host_out = torch.empty(N_MATS, dtype=torch.complex128).pin_memory()
+    dev_in = torch.empty_like(flat_d)
+
+    def e2e_step():
+        dev_in.copy_(host_in, non_blocking=True)
+        _native.permanent_batch(dev_in, offs, sizes, out_d)
+        host_out.copy_(out_d, non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if ws > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t)
+    e2e = {"value": ws * N_MATS * args.steps / e2e_s, "unit": "perms/s", "h2d_bytes_per_step": int(flat.nbytes),
+           "d2h_bytes_per_step": int(N_MATS * 16)}
+
+    # dominant kernel alone: the n = 24 bin (its CTAs' share of the step is largest)
+    sel = [i for i in range(N_MATS) if sizes[i] == 24]
+    sub = np.concatenate([mats[i].reshape(-1) for i in sel])
+    sub_d = torch.from_numpy(sub).to(dev)
+    sub_out = torch.empty(len(sel), dtype=torch.complex128, device=dev)
+    sub_offs = np.arange(len(sel), dtype=np.int64) * 576
+    sub_sizes = np.full(len(sel), 24, dtype=np.int32)
+    _native.permanent_batch(sub_d, sub_offs, sub_sizes, sub_out)
+    torch.cuda.synchronize()
+    kt = []
+    for _ in range(3):
+        flush.zero_()
+        s, e = torch.cuda.Event(True), torch.cuda.Event(True)
+        s.record()
+        _native.permanent_batch(sub_d, sub_offs, sub_sizes, sub_out)
+        e.record()
+        e.synchronize()
+        kt.append(s.elapsed_time(e))
+    k_ms = statistics.median(kt)
+    fp64_peak = measured_fp64_peak(torch)
+    achieved = len(sel) * glynn_flops(24) / (k_ms * 1e-3) / 1e12
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak, "traffic": traffic_from_profile("perm_bin_n24"),
+                "kernel": "perm_bin_kernel<24> (the n=24 bin of the batch)",
+                "peak_source": "measured cuBLAS DGEMM 4096^3 on this GPU (no FP64 entry in the measured peaks)",
+                "note": "float-float on the FP32 pipe: frac > 1 means faster than native FP64 peak",
+                "step_tflops_fp64_equiv": flops_total / (ms / args.steps * 1e-3) / 1e12}
+
+    line = {"metric": METRIC, "value": value, "unit": "perms/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "complex128 I/O, float-float (f32x2) arithmetic", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "l2": "flushed between timed steps (256 MiB write)",
+                       "parallelism": f"replicas x{ws}", "launch": "one pcvl_permanent_batch per step"},
+            "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "roofline": roofline,
+            "clocks": clocks.summary()}
+
+    if rank == 0 and not args.skip_secondary:
+        line["secondary"] = secondary(torch, _native, random_unitary, dev, flush)
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        line["cpu_baseline"] = cpu_perm_baseline()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def secondary(torch, _native, random_unitary, dev, flush):
+    res = {}
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            flush.zero_()
+            s, e = torch.cuda.Event(True), torch.cuda.Event(True)
+            s.record()
+            fn()
+            e.record()
+            e.synchronize()
+            ts.append(s.elapsed_time(e))
+        return statistics.median(ts)
+
+    hbm = None
+    try:
+        hbm = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]
+    except (OSError, ValueError, KeyError):
+        hbm = 6800.0
+    # SLOS m=24, n=12
+    m, n = 24, 12
+    plan = _native.SlosPlan(m, [1] * n + [0] * (m - n))
+    Ud = torch.from_numpy(random_unitary(m, seed=0)).to(dev)
+    t_fwd = timed(lambda: plan.forward(Ud), reps=2)
+    probs = plan.probabilities()
+    t_prob = timed(lambda: plan.probabilities(probs), reps=2)
+    Ls = [math.comb(m + k - 1, k) for k in range(n + 1)]
+    alg_bytes = 16 * sum(Ls[k - 1] + Ls[k] for k in range(1, n + 1))
+    res["slos_m24_n12"] = {"amps_per_s": Ls[n] / (t_fwd * 1e-3), "forward_ms": t_fwd, "probabilities_ms": t_prob,
+                           "algorithmic_gb": alg_bytes / 1e9,
+                           "hbm_frac": alg_bytes / (t_fwd * 1e-3) / 1e9 / hbm, "hbm_peak_gbs": hbm,
+                           "sum_p": float(probs.sum())}
+    del plan, probs
+    torch.cuda.empty_cache()
+    # batched forward + adjoint, 256 Clements meshes m=16, n=8
+    from perceval_gb300.components.mesh import clements_mesh_unitary
+    ph = torch.from_numpy(np.random.default_rng(0).uniform(0, 2 * math.pi, (256, 240)))
+    Um = clements_mesh_unitary(ph, 16).contiguous().to(dev)
+    plan = _native.SlosPlan(16, [1] * 8 + [0] * 8, batch=256, keep_layers=True)
+    w = torch.from_numpy(np.random.default_rng(1).normal(size=plan.count * 256)).to(dev)
+    t_f = timed(lambda: plan.forward(Um), reps=2)
+    t_b = timed(lambda: plan.backward(w), reps=2)
+    Ls = [math.comb(16 + k - 1, k) for k in range(9)]
+    fb = 16 * 256 * sum(Ls[k - 1] + Ls[k] for k in range(1, 9))
+    res["slos_grad_m16_n8_b256"] = {"forward_ms": t_f, "backward_ms": t_b, "circuits_per_s": 256 / ((t_f + t_b) * 1e-3),
+                                    "forward_hbm_frac": fb / (t_f * 1e-3) / 1e9 / hbm}
+    del plan
+    torch.cuda.empty_cache()
+    # Clifford & Clifford, n=20, m=400
+    U4 = torch.from_numpy(random_unitary(400, seed=0)).to(dev)
+    cnt = 20000
+    t_cc = timed(lambda: _native.cc2017_sample(U4, [1] * 20 + [0] * 380, cnt, seed=1), reps=1)
+    res["cc2017_n20_m400"] = {"samples_per_s": cnt / (t_cc * 1e-3), "samples": cnt, "precision": "float-float"}
+    # small case: SLOS m=12, n=6 and 1000 Naive amplitudes (latency-bound)
+    from perceval_gb300 import BackendFactory, BasicState
+    U12 = random_unitary(12, seed=0)
+    t0 = time.perf_counter()
+    b = BackendFactory.get_backend("SLOS")
+    b.set_circuit(U12)
+    b.set_input_state(BasicState([1] * 6 + [0] * 6))
+    p = b.all_prob()
+    t_slos = time.perf_counter() - t0
+    rng = np.random.default_rng(0)
+    outs = []
+    for _ in range(1000):
+        o = np.zeros(12, dtype=int)
+        o[rng.choice(12, 6, replace=False)] = 1
+        outs.append(BasicState(o))
+    nb = BackendFactory.get_backend("Naive")
+    nb.set_circuit(U12)
+    nb.set_input_state(BasicState([1] * 6 + [0] * 6))
+    t0 = time.perf_counter()
+    nb.prob_amplitudes(outs)
+    t_naive = time.perf_counter() - t0
+    res["small_m12_n6"] = {"slos_all_prob_ms": t_slos * 1e3, "outputs": len(p), "naive_1000_amplitudes_ms": t_naive * 1e3}
+    return res
+
+
+def profile_case(name: str):
+    """One untimed run of a single hot kernel on a small case, for ncu captures."""
+    import torch
+    from perceval_gb300 import _native
+    from perceval_gb300.utils.matrix import random_unitary
+    _native.load()
+    dev = torch.device("cuda")
+    if name == "perm24":
+        # 64 matrices of the n = 24 bin (one perm_bin_kernel<24> launch)
+        mats, flat, offs, sizes = make_batch(seed=0)
+        sel = [i for i in range(N_MATS) if sizes[i] == 24][:64]
+        sub = torch.from_numpy(np.concatenate([mats[i].reshape(-1) for i in sel])).to(dev)
+        out = torch.empty(len(sel), dtype=torch.complex128, device=dev)
+        _native.permanent_batch(sub, np.arange(len(sel), dtype=np.int64) * 576, np.full(len(sel), 24, np.int32), out)
+    elif name == "slos20":
+        # SLOS m = 20, n = 10: last layer 20,030,010 states (320 MB, above L2)
+        plan = _native.SlosPlan(20, [1] * 10 + [0] * 10)
+        plan.forward(torch.from_numpy(random_unitary(20, seed=0)).to(dev))
+        plan.probabilities()
+    elif name == "slos16b256":
+        from perceval_gb300.components.mesh import clements_mesh_unitary
+        ph = torch.from_numpy(np.random.default_rng(0).uniform(0, 2 * math.pi, (256, 240)))
+        plan = _native.SlosPlan(16, [1] * 8 + [0] * 8, batch=256, keep_layers=True)
+        plan.forward(clements_mesh_unitary(ph, 16).contiguous().to(dev))
+        plan.backward(torch.ones(plan.count * 256, dtype=torch.float64, device=dev))
+    elif name == "cc2017":
+        U4 = torch.from_numpy(random_unitary(400, seed=0)).to(dev)
+        _native.cc2017_sample(U4, [1] * 20 + [0] * 380, 608, seed=1)
+    else:
+        raise SystemExit(f"unknown profile case {name}")
+    torch.cuda.synchronize()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--skip-secondary", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--profile-case", choices=["perm24", "slos20", "slos16b256", "cc2017"],
+                    help="run one small untimed case of a single kernel (for ncu) and exit")
+    args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args.profile_case)
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()
