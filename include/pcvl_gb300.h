@@ -49,6 +49,25 @@ int pcvl_release_workspace(void);
 int pcvl_permanent_batch(const double* mats_d, const int64_t* offsets_h, const int32_t* sizes_h,
                          int32_t count, double* out_d, int32_t method, void* stream);
 
+/* Allocation-free variant of pcvl_permanent_batch.  It has no counterpart in the
+ * reference.  Some callers cannot call cudaMalloc: a plugin inside a host program
+ * whose memory pool already holds the whole GPU, a latency-critical loop that must not
+ * take the implicit synchronisation of an allocation, or a process whose device
+ * allocations are frozen after start-up.  This entry point computes the same
+ * permanents as pcvl_permanent_batch (same arguments, same results) without allocating
+ * anything: its scratch is a fixed array of about 53 MB held on every GPU that loads
+ * the library until the process exits.  Limits per call: at most 16384 matrices, at
+ * most 3 * 2^20 complex elements spanned by offsets_h[i] + sizes_h[i]^2, at most 2^17
+ * CTA partial sums (ample for batches within the first two limits); larger requests
+ * are refused with PCVL_ERR_ARG and a message naming the limit.  The first call on a
+ * device looks up the scratch's device address (cudaGetSymbolAddress); make that
+ * first call before any stream capture.  Every call reuses the same scratch and
+ * rewrites every part of it that it reads, so nothing needs clearing; but calls whose
+ * GPU work overlaps (different streams, or different host threads without ordering)
+ * race on it and must be serialised by the caller. */
+int pcvl_permanent_batch_noalloc(const double* mats_d, const int64_t* offsets_h, const int32_t* sizes_h,
+                                 int32_t count, double* out_d, int32_t method, void* stream);
+
 /* ------------------------------------------------------------------ SLOS
  * Replaces the numeric SLOS path of perceval/backends/_slos.py:
  *   _Path._decompose / compute   (:61-102)  -> photon-addition order

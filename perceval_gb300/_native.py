@@ -22,6 +22,9 @@ SYMBOLS = {
     "pcvl_release_workspace": (ctypes.c_int, []),
     "pcvl_permanent_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                             ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
+    "pcvl_permanent_batch_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                    ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
+                                                    ctypes.c_void_p]),
     "pcvl_slos_plan_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.c_void_p,
                                              ctypes.c_int32, ctypes.c_int32]),
     "pcvl_slos_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
@@ -102,6 +105,26 @@ def permanent_batch(mats: torch.Tensor, offsets: np.ndarray, sizes: np.ndarray, 
         raise ValueError("a matrix extends beyond the end of mats")
     check(lib.pcvl_permanent_batch(mats.data_ptr(), offsets.ctypes.data, sizes.ctypes.data, count,
                                    out.data_ptr(), int(method), _stream_ptr(stream)), "pcvl_permanent_batch")
+    return out
+
+
+def permanent_batch_noalloc(mats: torch.Tensor, offsets: np.ndarray, sizes: np.ndarray, out: torch.Tensor,
+                            method: int = 0, stream=None) -> torch.Tensor:
+    """Same as ``permanent_batch`` through the allocation-free entry point: the library
+    allocates no device memory for the call (fixed per-call limits, see the header)."""
+    lib = load()
+    _dev_tensor(mats, torch.complex128, "mats")
+    _dev_tensor(out, torch.complex128, "out")
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+    count = int(sizes.shape[0])
+    if offsets.shape[0] != count or out.numel() < count:
+        raise ValueError("offsets, sizes and out must describe the same number of matrices")
+    if count and int((offsets + sizes.astype(np.int64) ** 2).max()) > mats.numel():
+        raise ValueError("a matrix extends beyond the end of mats")
+    check(lib.pcvl_permanent_batch_noalloc(mats.data_ptr(), offsets.ctypes.data, sizes.ctypes.data, count,
+                                           out.data_ptr(), int(method), _stream_ptr(stream)),
+          "pcvl_permanent_batch_noalloc")
     return out
 
 
