@@ -113,6 +113,36 @@ PCVL_HD cdd cdd_mul(cdd x, cdd y) {
   return {re, im};
 }
 
+// Lazy variants for chains of operations.  The result pair (hi, lo) is exact up to the
+// FP32 roundings of the low-order terms but not renormalised: |lo| stays below about
+// 2^-20 of the operands' magnitude, so feeding it to cdd_mul_lazy (whose cross terms
+// multiply lo by hi in FP32) costs at most ~2^-46 of the product's magnitude.
+PCVL_HD cdd cdd_add_lazy(cdd a, cdd b) {
+  const dd r = two_sum(a.re.hi, b.re.hi);
+  const dd i = two_sum(a.im.hi, b.im.hi);
+  return {{r.hi, r.lo + (a.re.lo + b.re.lo)}, {i.hi, i.lo + (a.im.lo + b.im.lo)}};
+}
+PCVL_HD cdd cdd_mul_lazy(cdd x, cdd y) {
+  const dd p1 = two_prod(x.re.hi, y.re.hi);
+  const dd p2 = two_prod(x.im.hi, y.im.hi);
+  const dd s = two_sum(p1.hi, -p2.hi);
+  float t = s.lo + (p1.lo - p2.lo);
+  t = fmaf(x.re.hi, y.re.lo, t);
+  t = fmaf(x.re.lo, y.re.hi, t);
+  t = fmaf(-x.im.hi, y.im.lo, t);
+  t = fmaf(-x.im.lo, y.im.hi, t);
+  const dd q1 = two_prod(x.re.hi, y.im.hi);
+  const dd q2 = two_prod(x.im.hi, y.re.hi);
+  const dd u = two_sum(q1.hi, q2.hi);
+  float v = u.lo + (q1.lo + q2.lo);
+  v = fmaf(x.re.hi, y.im.lo, v);
+  v = fmaf(x.re.lo, y.im.hi, v);
+  v = fmaf(x.im.hi, y.re.lo, v);
+  v = fmaf(x.im.lo, y.re.hi, v);
+  return {{s.hi, t}, {u.hi, v}};
+}
+PCVL_HD cdd cdd_norm(cdd a) { return {two_sum(a.re.hi, a.re.lo), two_sum(a.im.hi, a.im.lo)}; }
+
 // Lazy complex accumulator for sums of products: the high parts accumulate through
 // two_sum (exact), everything of lower order goes to a plain float accumulator.
 // One finish() renormalises.

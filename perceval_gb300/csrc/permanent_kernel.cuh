@@ -40,17 +40,38 @@ struct PermBinArgs {
 
 constexpr int kPermThreads = 128;
 
-template <int LO, int HI>
+// prod_i (H_i + T_i) over rows [LO, HI) as a balanced tree.  Glynn uses the lazy
+// float-float operations; Ryser, whose alternating subset sum cancels far more, keeps
+// every intermediate normalised.
+template <int LO, int HI, bool LAZY>
 struct RowProd {
   static __device__ __forceinline__ cdd run(const cdd* H, const cdd* Tb) {
     if constexpr (HI - LO == 1) {
-      return cdd_add(H[LO], Tb[LO]);
+      return LAZY ? cdd_add_lazy(H[LO], Tb[LO]) : cdd_add(H[LO], Tb[LO]);
     } else {
       constexpr int MID = (LO + HI) / 2;
-      return cdd_mul(RowProd<LO, MID>::run(H, Tb), RowProd<MID, HI>::run(H, Tb));
+      const cdd a = RowProd<LO, MID, LAZY>::run(H, Tb);
+      const cdd b = RowProd<MID, HI, LAZY>::run(H, Tb);
+      return LAZY ? cdd_mul_lazy(a, b) : cdd_mul(a, b);
     }
   }
 };
+
+// signed sum over the lo patterns of one hi pattern
+template <int N, bool LAZY>
+__device__ __forceinline__ void lo_sweep(const cdd* H, const cdd* T, int nsteps, int hsign, float& arh, float& arl,
+                                         float& aih, float& ail) {
+  for (int b = 0; b < nsteps; ++b) {
+    cdd prod = RowProd<0, N, LAZY>::run(H, T + b * N);
+    if ((__popc(b) & 1) ^ hsign) prod = cdd_neg(prod);
+    const dd r = two_sum(arh, prod.re.hi);
+    const dd i = two_sum(aih, prod.im.hi);
+    arh = r.hi;
+    arl += r.lo + prod.re.lo;
+    aih = i.hi;
+    ail += i.lo + prod.im.lo;
+  }
+}
 
 __device__ __forceinline__ cdd shfl_down_cdd(cdd v, int d) {
   cdd r;
@@ -104,7 +125,8 @@ __global__ void __launch_bounds__(kPermThreads) perm_bin_kernel(PermBinArgs a) {
   const uint64_t h0 = (uint64_t)chunk * (uint64_t)(kPermThreads * a.P) + (uint64_t)tid * a.P;
   const int hi_col0 = ryser ? L : 1 + L;
   const int nsteps = 1 << L;
-  cdd acc = cdd_zero();
+  // signed sum of the products: high parts through two_sum, the rest in float
+  float arh = 0.f, arl = 0.f, aih = 0.f, ail = 0.f;
 
   for (int64_t p = 0; p < a.P; ++p) {
     const uint64_t h = h0 + p;
@@ -125,12 +147,19 @@ __global__ void __launch_bounds__(kPermThreads) perm_bin_kernel(PermBinArgs a) {
       H[i] = v;
     }
     const int hsign = __popcll(h) & 1;
-    for (int b = 0; b < nsteps; ++b) {
-      cdd prod = RowProd<0, N>::run(H, T + b * N);
-      if ((__popc(b) & 1) ^ hsign) prod = cdd_neg(prod);
-      acc = cdd_add(acc, prod);
-    }
+    if (ryser)
+      lo_sweep<N, false>(H, T, nsteps, hsign, arh, arl, aih, ail);
+    else
+      lo_sweep<N, true>(H, T, nsteps, hsign, arh, arl, aih, ail);
+    // fold the low parts in every hi pattern so they stay small
+    const dd r = two_sum(arh, arl);
+    const dd i = two_sum(aih, ail);
+    arh = r.hi;
+    arl = r.lo;
+    aih = i.hi;
+    ail = i.lo;
   }
+  cdd acc = {{arh, arl}, {aih, ail}};
 
   // block reduction (df64), one FP64 partial per CTA
 #pragma unroll

@@ -154,6 +154,241 @@ __device__ __forceinline__ double state_prodfact(uint32_t r, int m, int k, const
   return pf;
 }
 
+// ------------------------------------------------------------------ tiled single-circuit path
+// The modes split into a prefix (the first p = m - t) and a tail (the last t <= 8).
+// A tile is the set of states sharing one prefix pi; its r = k - |pi| tail photons
+// range over the count(t, r) tail states tau, contiguous in rank order:
+//     rank(pi, tau) = A(pi, r) + rank_t(tau),  A = sum_{i<p} Cn(m - i, R_{i+1} - 1).
+// Tiles themselves are ordered like the states of the (p + 1)-mode space whose last
+// mode holds r, so tile index -> pi is one unranking.  Parents of (pi, tau):
+//   prefix mode j:  A - Pfx_j + rank_t(tau)          (contiguous over tau)
+//   tail mode j:    A - Pfx_p + rank_t(tau - e_j)    (rank_t from a small table)
+// with Pfx_j = sum_{i<j} Cn(m - i - 1, R_{i+1} - 1).  Descriptors are computed once per
+// tile (one thread each) for a chunk of tiles; the CTA's threads then sweep the
+// chunk's children, finding their tile by binary search over the chunk's offsets.
+constexpr int kTileChunk = 128;
+
+struct SlosTiledArgs {
+  int m, k, p, t;
+  uint32_t ntiles;
+  const cdd* in;
+  cdd* out;
+  const cdd* ucol;          // u_j = U[j, mk]
+  const uint32_t* cn;
+  int cn_stride;
+  const uint32_t* tail;     // tail tables: parent ranks (forward) or child ranks (backward)
+  uint32_t tail_off[kSlosMaxN + 2];  // entry offset of the block of r tail photons
+  uint32_t tstate_off[kSlosMaxN + 2];  // state offset of the block of r tail photons
+  uint32_t tsize[kSlosMaxN + 2];     // count(t, r)
+};
+
+struct TileDesc {
+  uint32_t start, tbase, mask;
+  int r;
+};
+
+// Descriptor of tile `tile` of layer k; pre[i] receives A - Pfx_i for occupied
+// prefix modes (bit i of mask).
+template <int MMAX>
+__device__ __forceinline__ TileDesc tile_desc(uint32_t tile, int m, int k, int p, const uint32_t* cn, int st,
+                                             uint32_t* pre) {
+  uint32_t rho = tile, A = 0, Pfx = 0, mask = 0;
+  int R = k;
+#pragma unroll
+  for (int i = 0; i < MMAX; ++i) {
+    if (i < p) {
+      const int M1 = p + 1 - i;
+      int x = R;
+      while (x > 0) {
+        const uint32_t c = cn_at(cn, st, M1, x - 1);
+        if (rho >= c) {
+          rho -= c;
+          break;
+        }
+        --x;
+      }
+      const int v = R - x;
+      if (v > 0) {
+        mask |= 1u << i;
+        pre[i] = Pfx;
+      }
+      const int Rn = R - v;
+      A += cn_at(cn, st, m - i, Rn - 1);
+      Pfx += cn_at(cn, st, m - i - 1, Rn - 1);
+      R = Rn;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < MMAX; ++i)
+    if (i < p && ((mask >> i) & 1u)) pre[i] = A - pre[i];
+  return {A, A - Pfx, mask, R};
+}
+
+// exclusive scan of kTileChunk sizes held one per thread (threads >= kTileChunk pass 0)
+__device__ __forceinline__ void chunk_scan(uint32_t v, uint32_t* off, uint32_t* warp_tot) {
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  if (tid < kTileChunk && lane == 31) warp_tot[w] = x;
+  __syncthreads();
+  if (tid < kTileChunk) {
+    uint32_t base = 0;
+    for (int q = 0; q < w; ++q) base += warp_tot[q];
+    off[tid + 1] = base + x;
+    if (tid == 0) off[0] = 0;
+  }
+  __syncthreads();
+}
+
+// mode 0: forward layer (gather from parents); mode 1: adjoint layer (gather from
+// children, plus per-CTA partials of dL/du); the parent/child roles swap through the
+// tail table and the prefix offsets.
+template <int MMAX>
+__global__ void __launch_bounds__(256) slos_forward_tiled(SlosTiledArgs a) {
+  extern __shared__ uint32_t cn_s[];
+  __shared__ uint32_t s_off[kTileChunk + 1], s_start[kTileChunk], s_tbase[kTileChunk], s_mask[kTileChunk];
+  __shared__ int s_r[kTileChunk];
+  __shared__ uint32_t s_pre[kTileChunk][MMAX];
+  __shared__ uint32_t s_wtot[kTileChunk / 32];
+  __shared__ cdd u[MMAX];
+  const int ncn = (a.m + 1) * a.cn_stride;
+  for (int i = threadIdx.x; i < ncn; i += blockDim.x) cn_s[i] = a.cn[i];
+  const int m = a.m, p = a.p, t = a.t, tid = threadIdx.x;
+  if (tid < MMAX) u[tid] = tid < m ? a.ucol[tid] : cdd_zero();
+  __syncthreads();
+  const uint32_t nchunks = (a.ntiles + kTileChunk - 1) / kTileChunk;
+  for (uint32_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+    // largest tiles (small prefixes) come last in rank order: take chunks from the end
+    const uint32_t first = (nchunks - 1 - ch) * kTileChunk;
+    uint32_t size = 0;
+    if (tid < kTileChunk && first + tid < a.ntiles) {
+      const TileDesc d = tile_desc<MMAX>(first + tid, m, a.k, p, cn_s, a.cn_stride, s_pre[tid]);
+      s_start[tid] = d.start;
+      s_tbase[tid] = d.tbase;
+      s_mask[tid] = d.mask;
+      s_r[tid] = d.r;
+      size = a.tsize[d.r];
+    }
+    chunk_scan(size, s_off, s_wtot);
+    const uint32_t total = s_off[kTileChunk];
+    for (uint32_t idx = tid; idx < total; idx += blockDim.x) {
+      int lo = 0, hi = kTileChunk;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (s_off[mid] <= idx) lo = mid; else hi = mid;
+      }
+      const uint32_t tau = idx - s_off[lo];
+      const uint32_t mask = s_mask[lo];
+      const int r = s_r[lo];
+      const uint32_t tbase = s_tbase[lo];
+      const uint32_t* row = a.tail + a.tail_off[r] + (size_t)tau * t;
+      cacc acc = cacc_zero();
+#pragma unroll
+      for (int j = 0; j < MMAX; ++j) {
+        if (j < p) {
+          if ((mask >> j) & 1u) cacc_fma(acc, ld_cdd(&a.in[s_pre[lo][j] + tau]), u[j]);
+        } else if (j < m && r > 0) {
+          const uint32_t e = __ldg(&row[j - p]);
+          if (e != kNone) cacc_fma(acc, ld_cdd(&a.in[tbase + e]), u[j]);
+        }
+      }
+      a.out[s_start[lo] + tau] = cacc_finish(acc);
+    }
+    __syncthreads();
+  }
+}
+
+// double from a float by exponent re-bias (integer pipe); zero and subnormals take the
+// conversion instruction
+__device__ __forceinline__ double f2d_int(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)f;
+  const uint64_t bits = ((uint64_t)(u & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
+                        ((uint64_t)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+__device__ __forceinline__ double dd_to_double_fast(dd a) { return f2d_int(a.hi) + f2d_int(a.lo); }
+
+// Probabilities (mode 0), amplitudes (mode 1) or adjoint seed (mode 2) of the last
+// layer over tiles: F = prod(out!) / prod(in!) = fpre (per tile, float-float) x ftail[tau].
+template <int MMAX>
+__global__ void __launch_bounds__(256) slos_finalize_tiled(SlosTiledArgs a, const dd* __restrict__ ftail,
+                                                          dd inv_in, int mode, const double* __restrict__ w,
+                                                          double* __restrict__ out_real, double2* __restrict__ out_c,
+                                                          cdd* __restrict__ seed) {
+  extern __shared__ uint32_t cn_s[];
+  __shared__ uint32_t s_off[kTileChunk + 1], s_start[kTileChunk];
+  __shared__ int s_r[kTileChunk];
+  __shared__ dd s_f[kTileChunk];
+  __shared__ uint32_t s_wtot[kTileChunk / 32];
+  const int ncn = (a.m + 1) * a.cn_stride;
+  for (int i = threadIdx.x; i < ncn; i += blockDim.x) cn_s[i] = a.cn[i];
+  __syncthreads();
+  const int m = a.m, p = a.p, tid = threadIdx.x;
+  const uint32_t nchunks = (a.ntiles + kTileChunk - 1) / kTileChunk;
+  for (uint32_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+    const uint32_t first = (nchunks - 1 - ch) * kTileChunk;
+    uint32_t size = 0;
+    if (tid < kTileChunk && first + tid < a.ntiles) {
+      // prefix occupation: unrank the tile again, multiplying the factorials
+      uint32_t rho = first + tid;
+      int R = a.k;
+      dd f = inv_in;
+      uint32_t A = 0;
+      for (int i = 0; i < p; ++i) {
+        const int M1 = p + 1 - i;
+        int x = R;
+        while (x > 0) {
+          const uint32_t c = cn_at(cn_s, a.cn_stride, M1, x - 1);
+          if (rho >= c) {
+            rho -= c;
+            break;
+          }
+          --x;
+        }
+        const int v = R - x;
+        for (int q = 2; q <= v; ++q) f = dd_mul_f(f, (float)q);
+        const int Rn = R - v;
+        A += cn_at(cn_s, a.cn_stride, m - i, Rn - 1);
+        R = Rn;
+      }
+      s_start[tid] = A;
+      s_r[tid] = R;
+      s_f[tid] = f;
+      size = a.tsize[R];
+    }
+    chunk_scan(size, s_off, s_wtot);
+    const uint32_t total = s_off[kTileChunk];
+    for (uint32_t idx = tid; idx < total; idx += blockDim.x) {
+      int lo = 0, hi = kTileChunk;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (s_off[mid] <= idx) lo = mid; else hi = mid;
+      }
+      const uint32_t tau = idx - s_off[lo];
+      const uint32_t r_idx = s_start[lo] + tau;
+      const dd F = dd_mul(s_f[lo], ftail[a.tstate_off[s_r[lo]] + tau]);
+      const cdd c = ld_cdd(&a.in[r_idx]);
+      if (mode == 0) {
+        const dd c2 = dd_add(dd_mul(c.re, c.re), dd_mul(c.im, c.im));
+        out_real[r_idx] = dd_to_double_fast(dd_mul(c2, F));
+      } else if (mode == 1) {
+        const double sF = sqrt(dd_to_double_fast(F));
+        out_c[r_idx] = make_double2(dd_to_double_fast(c.re) * sF, dd_to_double_fast(c.im) * sF);
+      } else {
+        const dd f2 = dd_mul(dd_from_double(2.0 * w[r_idx]), F);
+        seed[r_idx] = {dd_mul(c.re, f2), dd_mul(c.im, f2)};
+      }
+    }
+    __syncthreads();
+  }
+}
+
 template <int MMAX, bool BATCHED>
 __global__ void __launch_bounds__(256) slos_forward_layer(SlosLayerArgs a) {
   extern __shared__ uint32_t cn_s[];
@@ -401,6 +636,11 @@ struct pcvl_slos_plan {
   int gpart_blocks = 0;
   int64_t bytes = 0;
   bool forwarded = false;
+  // tiled single-circuit path (batch == 1)
+  int tail_t = 0, tail_p = 0;
+  uint32_t* tail_parent_d = nullptr;   // rank_t(tau - e_j) per tail state and tail mode
+  dd* ftail_d = nullptr;               // prod tau_j! per tail state
+  std::vector<uint32_t> tail_off, tstate_off, tsize;
   cdd* final_layer() const { return keep ? layers[n] : layers[n % 2]; }
 };
 
@@ -414,7 +654,65 @@ void free_plan(pcvl_slos_plan* p) {
   cudaFree(p->adj_d[0]);
   cudaFree(p->adj_d[1]);
   cudaFree(p->gpart_d);
+  cudaFree(p->tail_parent_d);
+  cudaFree(p->ftail_d);
   delete p;
+}
+
+// Tail tables for t tail modes and up to n tail photons (descending-lex order within
+// each photon number): parent ranks rank_t(tau - e_j) (kNone where tau_j = 0) and the
+// factorial products prod_j tau_j!.
+void tail_tables(int t, int n, std::vector<uint32_t>& parent, std::vector<dd>& ftail, std::vector<uint32_t>& tail_off,
+                 std::vector<uint32_t>& tstate_off, std::vector<uint32_t>& tsize) {
+  tail_off.assign(n + 2, 0);
+  tstate_off.assign(n + 2, 0);
+  tsize.assign(n + 2, 0);
+  parent.clear();
+  ftail.clear();
+  auto rank = [t](const std::vector<int>& s) {
+    int rest = 0;
+    for (int v : s) rest += v;
+    uint64_t r = 0;
+    for (int i = 0; i < t; ++i) {
+      rest -= s[i];
+      if (rest > 0) r += fock_count(t - i, rest - 1);
+    }
+    return (uint32_t)r;
+  };
+  for (int r = 0; r <= n; ++r) {
+    tail_off[r] = (uint32_t)parent.size();
+    tstate_off[r] = (uint32_t)ftail.size();
+    tsize[r] = (uint32_t)fock_count(t, r);
+    std::vector<int> s(t, 0);
+    s[0] = r;
+    for (uint32_t q = 0; q < tsize[r]; ++q) {
+      double f = 1.0;
+      for (int j = 0; j < t; ++j) {
+        for (int v = 2; v <= s[j]; ++v) f *= v;
+        if (s[j] == 0) {
+          parent.push_back(kNone);
+        } else {
+          s[j] -= 1;
+          parent.push_back(rank(s));
+          s[j] += 1;
+        }
+      }
+      ftail.push_back(dd_from_double(f));
+      // next state in descending-lex order
+      int tail = 0;
+      for (int i = t - 2; i >= 0; --i) {
+        tail += s[i + 1];
+        if (s[i] > 0) {
+          s[i] -= 1;
+          s[i + 1] = tail + 1;
+          for (int j = i + 2; j < t; ++j) s[j] = 0;
+          break;
+        }
+      }
+    }
+  }
+  tail_off[n + 1] = (uint32_t)parent.size();
+  tstate_off[n + 1] = (uint32_t)ftail.size();
 }
 
 // Photon-addition order of perceval/backends/_slos.py:61-86 for one input state:
@@ -537,11 +835,74 @@ extern "C" int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int
     if ((rc = alloc((void**)&p->layers[1], std::max<size_t>(s1, 1) * B * sizeof(cdd), p->bytes)) != PCVL_OK)
       goto fail;
   }
+  if (batch == 1) {
+    // largest tail (<= 8 modes, < m so the prefix is non-empty unless m == 1) whose
+    // tables stay small: count(t + 1, n) tail states over all photon numbers
+    int t = std::min(m, 8);
+    while (t > 1 && fock_count(t + 1, n) > 1000000ull) --t;
+    p->tail_t = t;
+    p->tail_p = m - t;
+    std::vector<uint32_t> parent;
+    std::vector<dd> ftail;
+    tail_tables(t, n, parent, ftail, p->tail_off, p->tstate_off, p->tsize);
+    if ((rc = alloc((void**)&p->tail_parent_d, parent.size() * 4, p->bytes)) != PCVL_OK) goto fail;
+    if ((rc = alloc((void**)&p->ftail_d, ftail.size() * sizeof(dd), p->bytes)) != PCVL_OK) goto fail;
+    if (cudaMemcpy(p->tail_parent_d, parent.data(), parent.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(p->ftail_d, ftail.data(), ftail.size() * sizeof(dd), cudaMemcpyHostToDevice) != cudaSuccess) {
+      set_error("SLOS plan: tail table upload failed");
+      rc = PCVL_ERR_CUDA;
+      goto fail;
+    }
+  }
   *plan = p;
   return PCVL_OK;
 fail:
   free_plan(p);
   return rc;
+}
+
+static SlosTiledArgs tiled_args(const pcvl_slos_plan* p, int k) {
+  SlosTiledArgs a{};
+  a.m = p->m;
+  a.k = k;
+  a.p = p->tail_p;
+  a.t = p->tail_t;
+  a.ntiles = (uint32_t)fock_count(p->tail_p + 1, k);
+  a.cn = p->cn_d;
+  a.cn_stride = p->cn_stride;
+  a.tail = p->tail_parent_d;
+  for (int r = 0; r <= p->n + 1 && r < kSlosMaxN + 2; ++r) {
+    a.tail_off[r] = p->tail_off[r];
+    a.tstate_off[r] = p->tstate_off[r];
+    a.tsize[r] = p->tsize[r];
+  }
+  return a;
+}
+
+template <int MMAX>
+static int launch_tiled(const SlosTiledArgs& a, cudaStream_t s) {
+  const size_t smem = (size_t)(a.m + 1) * a.cn_stride * sizeof(uint32_t);
+  const uint32_t chunks = (a.ntiles + kTileChunk - 1) / kTileChunk;
+  const int grid = (int)std::max<uint32_t>(1, std::min<uint32_t>(chunks, (uint32_t)num_sms() * 8));
+  slos_forward_tiled<MMAX><<<grid, 256, smem, s>>>(a);
+  return (int)cudaGetLastError();
+}
+
+static int dispatch_tiled(const SlosTiledArgs& a, cudaStream_t s) {
+  if (a.m <= 8) return launch_tiled<8>(a, s);
+  if (a.m <= 16) return launch_tiled<16>(a, s);
+  if (a.m <= 24) return launch_tiled<24>(a, s);
+  return launch_tiled<32>(a, s);
+}
+
+template <int MMAX>
+static int launch_fin_tiled(const SlosTiledArgs& a, const dd* ftail, dd inv_in, int mode, const double* w,
+                            double* out_real, double2* out_c, cdd* seed, cudaStream_t s) {
+  const size_t smem = (size_t)(a.m + 1) * a.cn_stride * sizeof(uint32_t);
+  const uint32_t chunks = (a.ntiles + kTileChunk - 1) / kTileChunk;
+  const int grid = (int)std::max<uint32_t>(1, std::min<uint32_t>(chunks, (uint32_t)num_sms() * 8));
+  slos_finalize_tiled<MMAX><<<grid, 256, smem, s>>>(a, ftail, inv_in, mode, w, out_real, out_c, seed);
+  return (int)cudaGetLastError();
 }
 
 extern "C" int pcvl_slos_plan_destroy(pcvl_slos_plan* plan) {
@@ -581,8 +942,16 @@ extern "C" int pcvl_slos_forward(pcvl_slos_plan* p, const double* u_d, void* str
     a.ucol = p->ucols_d + (size_t)p->order[k - 1] * m * B;
     a.cn = p->cn_d;
     a.cn_stride = p->cn_stride;
-    const int grid = B > 1 ? grid_for(a.nstates, 8) : grid_for(a.nstates, 256);
-    const int rc = dispatch_layer(false, a, grid, s);
+    int rc;
+    if (B == 1) {
+      SlosTiledArgs ta = tiled_args(p, k);
+      ta.in = a.in;
+      ta.out = a.out;
+      ta.ucol = a.ucol;
+      rc = dispatch_tiled(ta, s);
+    } else {
+      rc = dispatch_layer(false, a, grid_for(a.nstates, 8), s);
+    }
     if (rc != 0) {
       set_error("SLOS layer %d launch failed: %s", k, cudaGetErrorString((cudaError_t)rc));
       return PCVL_ERR_CUDA;
@@ -595,6 +964,25 @@ extern "C" int pcvl_slos_forward(pcvl_slos_plan* p, const double* u_d, void* str
 static int finalize(pcvl_slos_plan* p, int mode, const double* w, double* out_real, double2* out_c, cdd* seed,
                     cudaStream_t s) {
   PCVL_CHECK(p->forwarded, "pcvl_slos_forward has not run on this plan");
+  if (p->B == 1) {
+    SlosTiledArgs ta = tiled_args(p, p->n);
+    ta.in = p->final_layer();
+    const dd inv_in = dd_from_double(1.0 / p->prodfact_in);
+    int rc;
+    if (p->m <= 8)
+      rc = launch_fin_tiled<8>(ta, p->ftail_d, inv_in, mode, w, out_real, out_c, seed, s);
+    else if (p->m <= 16)
+      rc = launch_fin_tiled<16>(ta, p->ftail_d, inv_in, mode, w, out_real, out_c, seed, s);
+    else if (p->m <= 24)
+      rc = launch_fin_tiled<24>(ta, p->ftail_d, inv_in, mode, w, out_real, out_c, seed, s);
+    else
+      rc = launch_fin_tiled<32>(ta, p->ftail_d, inv_in, mode, w, out_real, out_c, seed, s);
+    if (rc != 0) {
+      set_error("SLOS finalize launch failed: %s", cudaGetErrorString((cudaError_t)rc));
+      return PCVL_ERR_CUDA;
+    }
+    return PCVL_OK;
+  }
   const size_t smem = (size_t)(p->m + 1) * p->cn_stride * sizeof(uint32_t);
   const uint64_t tot = p->sizes[p->n] * (uint64_t)p->B;
   slos_finalize<<<grid_for(tot, 256), 256, smem, s>>>(p->final_layer(), (uint32_t)p->sizes[p->n], p->m, p->n,
