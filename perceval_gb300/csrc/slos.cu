@@ -10,20 +10,32 @@
 // twin at :93-97 spells out).  Amplitude = c_n[s] sqrt(prod s! / prod t!) (:192),
 // probability = |c_n[s]|^2 prod s! / prod t! (:198-199, all_prob_normalize_output).
 //
-// Indexing.  Layer k is the k-photon space in descending lexicographic order.  With
+// Ranks.  Layer k is the k-photon space in descending lexicographic order.  With
 // Cn(M, x) = C(M + x - 1, x) (states of x photons on M modes) and R_{i+1} the photons
 // in modes after i:
-//     rank(s)          = sum_{i <= m-2} Cn(m - i, R_{i+1} - 1)
-//     rank(s - e_j)    = rank(s) - sum_{i < j} Cn(m - i - 1, R_{i+1}(s) - 1)
-//     rank(p + e_j)    = rank(p) + sum_{i < j} Cn(m - i - 1, R_{i+1}(p))
-// so every parent (child) index comes from one walk over the modes while the state
-// is unranked; no parent tables are stored.
+//     rank(s)       = sum_{i <= m-2} Cn(m - i, R_{i+1} - 1)
+//     rank(s - e_j) = rank(s) - sum_{i < j} Cn(m - i - 1, R_{i+1}(s) - 1)
+//     rank(p + e_j) = rank(p) + sum_{i < j} Cn(m - i - 1, R_{i+1}(p))
+//
+// Tiles.  The modes split into a prefix (the first p = m - t) and a tail (the last
+// t <= 8).  A tile is the set of states sharing one prefix pi; its r = k - |pi| tail
+// photons range over the count(t, r) tail states tau, contiguous in rank order:
+//     rank(pi, tau) = A(pi, r) + rank_t(tau),   A = sum_{i<p} Cn(m - i, R_{i+1} - 1),
+// and tiles are ordered like the states of the (p + 1)-mode space whose last mode
+// holds r, so tile index -> pi is one unranking.  From the formulas above:
+//   parent through prefix mode j:  A - Pfx_j + tau           Pfx_j = sum_{i<j} Cn(m-i-1, R_{i+1}-1)
+//   parent through tail mode j:    A - Pfx_p + TP[r][tau][j] TP = rank_t(tau - e_j)
+//   child through prefix mode j:   A + Q_j + tau             Q_j = sum_{i<j} Cn(m-i-1, R_{i+1})
+//   child through tail mode j:     A + Q_p + TC[r][tau][j]   TC = rank_t(tau + e_j)
+// so a parent or child index costs one add (prefix modes, contiguous over tau) or one
+// small-table read (tail modes).  Each lane of a warp computes the descriptor of one
+// tile of a group of 32; the warp then sweeps the group's states.
 //
 // Layout.  Coefficients are float-float complex (16 bytes, FP64-class precision),
-// state-major with the circuit index b innermost: element (r, b) at r * B + b.  For
-// B >= 2 one warp handles one state and its lanes 32 circuits (blockIdx.y selects
-// the 32-circuit chunk), so the index walk is warp-uniform and loads are coalesced
-// across circuits; for B == 1 each thread handles one state.
+// state-major with the circuit index b innermost: element (r, b) at r * B + b.  With
+// B == 1 the lanes take consecutive states; with B >= 2 the lanes take 32 circuits
+// of one state (blockIdx.y selects the 32-circuit chunk), so loads are coalesced
+// across circuits and the index work is shared by the 32 lanes.
 #include <algorithm>
 #include <cstring>
 #include <new>
@@ -37,266 +49,308 @@ namespace pcvl {
 constexpr int kSlosMaxM = 32;
 constexpr int kSlosMaxN = 32;
 constexpr uint32_t kNone = 0xffffffffu;
+constexpr int kWarps = 8;  // warps per CTA (256 threads)
 
-struct SlosLayerArgs {
-  int m, k, B;
-  uint32_t nstates;        // states of the layer written (children fwd, parents bwd)
-  const cdd* in;           // layer read
-  cdd* out;                // layer written
-  const cdd* ucol;         // column mk of every circuit: [j][b]
-  const uint32_t* cn;      // Cn table, (m + 1) x (nmax + 1), row M = Cn(M, .)
-  int cn_stride;           // nmax + 1
-  const cdd* cpar;         // backward: forward coefficients of the parent layer
-  cdd* gpart;              // backward: per-CTA partial dL/du_j, [blockIdx.x][j][b]
+struct SlosArgs {
+  int m, k, p, t, B;      // k: photons of the layer whose states are the tiles
+  uint32_t ntiles;
+  const cdd* in;          // forward: parent layer; adjoint: child-layer adjoint
+  cdd* out;               // forward: child layer; adjoint: parent-layer adjoint
+  const cdd* ucol;        // u_j (b) = U_b[j, mk] at ucol[j * B + b]
+  const cdd* cpar;        // adjoint: forward coefficients of the parent layer
+  cdd* gpart;             // adjoint: per-CTA partials of dL/du_j, [blockIdx.x][j][b]
+  const uint32_t* cn;
+  int cn_stride;
+  const uint32_t* tail;   // TP (forward) or TC (adjoint)
+  const dd* ftail;        // prod tau_j! per tail state
+  uint32_t tail_off[kSlosMaxN + 2];    // entry offset of the block of r tail photons
+  uint32_t tstate_off[kSlosMaxN + 2];  // state offset of that block
+  uint32_t tsize[kSlosMaxN + 2];       // count(t, r)
+  // work units of the layer, by tail photon count r (class r: count(p, k - r) tiles
+  // of tsize[r] states): unit offsets, tiles, and chunks per tile (0: the class is
+  // swept flat, 32 states per unit, one lane per state)
+  uint32_t uoff[kSlosMaxN + 2];
+  uint32_t npf[kSlosMaxN + 1];
+  uint32_t cpt[kSlosMaxN + 1];
 };
+
+constexpr uint32_t kChunk = 256;   // states per unit of a large tile (single circuit)
+constexpr uint32_t kChunkB = 8;    // states per unit (batched)
 
 __device__ __forceinline__ uint32_t cn_at(const uint32_t* cn, int stride, int M, int x) {
   return x < 0 ? 0u : cn[M * stride + x];
 }
 
-// Unranks child `c` (k photons) and returns the rank of every parent c - e_j
-// (kNone where s_j == 0).
+// Prefix descriptor of one tile, in registers.
 template <int MMAX>
-__device__ __forceinline__ void parent_ranks(uint32_t c, int m, int k, const uint32_t* cn, int st,
-                                             uint32_t (&pr)[MMAX]) {
-  uint32_t rho = c, pfx = 0;
-  int R = k;
-#pragma unroll
-  for (int j = 0; j < MMAX; ++j) {
-    if (j < m) {
-      int v;
-      if (j == m - 1) {
-        v = R;
-      } else {
-        const int M1 = m - j;
-        int x = R;
-        while (x > 0) {
-          const uint32_t t = cn_at(cn, st, M1, x - 1);
-          if (rho >= t) {
-            rho -= t;
-            break;
-          }
-          --x;
-        }
-        v = R - x;
-      }
-      pr[j] = v > 0 ? c - pfx : kNone;
-      const int Rn = R - v;
-      if (j < m - 1) pfx += cn_at(cn, st, m - j - 1, Rn - 1);
-      R = Rn;
-    } else {
-      pr[j] = kNone;
-    }
-  }
-}
-
-// Unranks parent `p` (k photons) and returns the rank of every child p + e_j.
-template <int MMAX>
-__device__ __forceinline__ void child_ranks(uint32_t p, int m, int k, const uint32_t* cn, int st,
-                                            uint32_t (&ch)[MMAX]) {
-  uint32_t rho = p, q = 0;
-  int R = k;
-#pragma unroll
-  for (int j = 0; j < MMAX; ++j) {
-    if (j < m) {
-      ch[j] = p + q;
-      int v;
-      if (j == m - 1) {
-        v = R;
-      } else {
-        const int M1 = m - j;
-        int x = R;
-        while (x > 0) {
-          const uint32_t t = cn_at(cn, st, M1, x - 1);
-          if (rho >= t) {
-            rho -= t;
-            break;
-          }
-          --x;
-        }
-        v = R - x;
-      }
-      const int Rn = R - v;
-      if (j < m - 1) q += cn_at(cn, st, m - j - 1, Rn);
-      R = Rn;
-    } else {
-      ch[j] = kNone;
-    }
-  }
-}
-
-// Unranks state r and returns prod_j s_j! (as a double).
-__device__ __forceinline__ double state_prodfact(uint32_t r, int m, int k, const uint32_t* cn, int st,
-                                                 const double* fact) {
-  uint32_t rho = r;
-  int R = k;
-  double pf = 1.0;
-  for (int j = 0; j < m && R > 0; ++j) {
-    int v;
-    if (j == m - 1) {
-      v = R;
-    } else {
-      const int M1 = m - j;
-      int x = R;
-      while (x > 0) {
-        const uint32_t t = cn_at(cn, st, M1, x - 1);
-        if (rho >= t) {
-          rho -= t;
-          break;
-        }
-        --x;
-      }
-      v = R - x;
-    }
-    pf *= fact[v];
-    R -= v;
-  }
-  return pf;
-}
-
-// ------------------------------------------------------------------ tiled single-circuit path
-// The modes split into a prefix (the first p = m - t) and a tail (the last t <= 8).
-// A tile is the set of states sharing one prefix pi; its r = k - |pi| tail photons
-// range over the count(t, r) tail states tau, contiguous in rank order:
-//     rank(pi, tau) = A(pi, r) + rank_t(tau),  A = sum_{i<p} Cn(m - i, R_{i+1} - 1).
-// Tiles themselves are ordered like the states of the (p + 1)-mode space whose last
-// mode holds r, so tile index -> pi is one unranking.  Parents of (pi, tau):
-//   prefix mode j:  A - Pfx_j + rank_t(tau)          (contiguous over tau)
-//   tail mode j:    A - Pfx_p + rank_t(tau - e_j)    (rank_t from a small table)
-// with Pfx_j = sum_{i<j} Cn(m - i - 1, R_{i+1} - 1).  Descriptors are computed once per
-// tile (one thread each) for a chunk of tiles; the CTA's threads then sweep the
-// chunk's children, finding their tile by binary search over the chunk's offsets.
-constexpr int kTileChunk = 128;
-
-struct SlosTiledArgs {
-  int m, k, p, t;
-  uint32_t ntiles;
-  const cdd* in;
-  cdd* out;
-  const cdd* ucol;          // u_j = U[j, mk]
-  const uint32_t* cn;
-  int cn_stride;
-  const uint32_t* tail;     // tail tables: parent ranks (forward) or child ranks (backward)
-  uint32_t tail_off[kSlosMaxN + 2];  // entry offset of the block of r tail photons
-  uint32_t tstate_off[kSlosMaxN + 2];  // state offset of the block of r tail photons
-  uint32_t tsize[kSlosMaxN + 2];     // count(t, r)
+struct Desc {
+  uint32_t A;             // rank of the tile's first state
+  uint32_t tb;            // forward: A - Pfx_p; adjoint: A + Q_p
+  uint32_t mask;          // occupied prefix modes
+  uint32_t base[MMAX];    // forward: A - Pfx_j (occupied j); adjoint: A + Q_j
+  dd f;                   // prod pi_i! / prod(in!)  (normalisation only)
 };
 
-struct TileDesc {
-  uint32_t start, tbase, mask;
-  int r;
-};
-
-// Descriptor of tile `tile` of layer k; pre[i] receives A - Pfx_i for occupied
-// prefix modes (bit i of mask).
-template <int MMAX>
-__device__ __forceinline__ TileDesc tile_desc(uint32_t tile, int m, int k, int p, const uint32_t* cn, int st,
-                                             uint32_t* pre) {
-  uint32_t rho = tile, A = 0, Pfx = 0, mask = 0;
-  int R = k;
+// Unranks prefix pi_idx of the q-photon prefix space (p modes) for a tile with r
+// tail photons and walks the modes once for the tile's offsets.
+template <int MMAX, bool ADJ, bool FACT>
+__device__ __forceinline__ void describe(uint32_t pi_idx, int q, int r, const SlosArgs& a, const uint32_t* cn,
+                                         Desc<MMAX>& d, dd inv_in) {
+  const int m = a.m, p = a.p, st = a.cn_stride;
+  uint32_t rho = pi_idx, A = 0, acc = 0, mask = 0;
+  int Rp = q, R = q + r;
+  dd f = inv_in;
 #pragma unroll
   for (int i = 0; i < MMAX; ++i) {
     if (i < p) {
-      const int M1 = p + 1 - i;
-      int x = R;
-      while (x > 0) {
-        const uint32_t c = cn_at(cn, st, M1, x - 1);
-        if (rho >= c) {
-          rho -= c;
-          break;
+      int v = Rp;
+      if (i < p - 1) {
+        int x = Rp;
+        while (x > 0) {
+          const uint32_t c = cn_at(cn, st, p - i, x - 1);
+          if (rho >= c) {
+            rho -= c;
+            break;
+          }
+          --x;
         }
-        --x;
+        v = Rp - x;
       }
-      const int v = R - x;
-      if (v > 0) {
-        mask |= 1u << i;
-        pre[i] = Pfx;
-      }
+      if (FACT)
+        for (int s2 = 2; s2 <= v; ++s2) f = dd_mul_f(f, (float)s2);
+      Rp -= v;
       const int Rn = R - v;
+      if (ADJ) {
+        d.base[i] = acc;  // Q_i
+        acc += cn_at(cn, st, m - i - 1, Rn);
+      } else {
+        if (v > 0) {
+          mask |= 1u << i;
+          d.base[i] = acc;  // Pfx_i
+        }
+        acc += cn_at(cn, st, m - i - 1, Rn - 1);
+      }
       A += cn_at(cn, st, m - i, Rn - 1);
-      Pfx += cn_at(cn, st, m - i - 1, Rn - 1);
       R = Rn;
     }
   }
 #pragma unroll
-  for (int i = 0; i < MMAX; ++i)
-    if (i < p && ((mask >> i) & 1u)) pre[i] = A - pre[i];
-  return {A, A - Pfx, mask, R};
-}
-
-// exclusive scan of kTileChunk sizes held one per thread (threads >= kTileChunk pass 0)
-__device__ __forceinline__ void chunk_scan(uint32_t v, uint32_t* off, uint32_t* warp_tot) {
-  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  uint32_t x = v;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
-    if (lane >= d) x += y;
-  }
-  if (tid < kTileChunk && lane == 31) warp_tot[w] = x;
-  __syncthreads();
-  if (tid < kTileChunk) {
-    uint32_t base = 0;
-    for (int q = 0; q < w; ++q) base += warp_tot[q];
-    off[tid + 1] = base + x;
-    if (tid == 0) off[0] = 0;
-  }
-  __syncthreads();
-}
-
-// mode 0: forward layer (gather from parents); mode 1: adjoint layer (gather from
-// children, plus per-CTA partials of dL/du); the parent/child roles swap through the
-// tail table and the prefix offsets.
-template <int MMAX>
-__global__ void __launch_bounds__(256) slos_forward_tiled(SlosTiledArgs a) {
-  extern __shared__ uint32_t cn_s[];
-  __shared__ uint32_t s_off[kTileChunk + 1], s_start[kTileChunk], s_tbase[kTileChunk], s_mask[kTileChunk];
-  __shared__ int s_r[kTileChunk];
-  __shared__ uint32_t s_pre[kTileChunk][MMAX];
-  __shared__ uint32_t s_wtot[kTileChunk / 32];
-  __shared__ cdd u[MMAX];
-  const int ncn = (a.m + 1) * a.cn_stride;
-  for (int i = threadIdx.x; i < ncn; i += blockDim.x) cn_s[i] = a.cn[i];
-  const int m = a.m, p = a.p, t = a.t, tid = threadIdx.x;
-  if (tid < MMAX) u[tid] = tid < m ? a.ucol[tid] : cdd_zero();
-  __syncthreads();
-  const uint32_t nchunks = (a.ntiles + kTileChunk - 1) / kTileChunk;
-  for (uint32_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
-    // largest tiles (small prefixes) come last in rank order: take chunks from the end
-    const uint32_t first = (nchunks - 1 - ch) * kTileChunk;
-    uint32_t size = 0;
-    if (tid < kTileChunk && first + tid < a.ntiles) {
-      const TileDesc d = tile_desc<MMAX>(first + tid, m, a.k, p, cn_s, a.cn_stride, s_pre[tid]);
-      s_start[tid] = d.start;
-      s_tbase[tid] = d.tbase;
-      s_mask[tid] = d.mask;
-      s_r[tid] = d.r;
-      size = a.tsize[d.r];
+  for (int i = 0; i < MMAX; ++i) {
+    if (i < p) {
+      if (ADJ)
+        d.base[i] = A + d.base[i];
+      else if ((mask >> i) & 1u)
+        d.base[i] = A - d.base[i];
     }
-    chunk_scan(size, s_off, s_wtot);
-    const uint32_t total = s_off[kTileChunk];
-    for (uint32_t idx = tid; idx < total; idx += blockDim.x) {
-      int lo = 0, hi = kTileChunk;
-      while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (s_off[mid] <= idx) lo = mid; else hi = mid;
-      }
-      const uint32_t tau = idx - s_off[lo];
-      const uint32_t mask = s_mask[lo];
-      const int r = s_r[lo];
-      const uint32_t tbase = s_tbase[lo];
-      const uint32_t* row = a.tail + a.tail_off[r] + (size_t)tau * t;
-      cacc acc = cacc_zero();
+  }
+  d.A = A;
+  d.tb = ADJ ? A + acc : A - acc;
+  d.mask = ADJ ? (p >= 32 ? 0xffffffffu : ((1u << p) - 1u)) : mask;
+  if (FACT) d.f = f;
+}
+
+// class (tail photon count) of unit u: uniform across the warp
+__device__ __forceinline__ int unit_class(const SlosArgs& a, uint32_t u) {
+  int r = 0;
+  while (r < a.k && a.uoff[r + 1] <= u) ++r;
+  return r;
+}
+
+// Dynamic shared memory of the layer kernels: [rank table][u].  u holds u_j
+// (single circuit, broadcast) or u_j of the CTA's 32 circuits ([j][lane]).
+__host__ __device__ inline size_t smem_cn_bytes(int m, int stride) {
+  return ((size_t)(m + 1) * stride * sizeof(uint32_t) + 15) / 16 * 16;
+}
+template <int MMAX>
+__host__ __device__ inline size_t smem_bytes(int m, int stride) {
+  return smem_cn_bytes(m, stride) + (size_t)MMAX * 32 * sizeof(cdd);
+}
+// rank table and u (conjugated for the adjoint) into shared memory
+template <int MMAX, bool BATCHED, bool CONJ>
+__device__ __forceinline__ cdd* load_shared(const SlosArgs& a, unsigned char* raw, uint32_t*& cn) {
+  cn = reinterpret_cast<uint32_t*>(raw);
+  cdd* u = reinterpret_cast<cdd*>(raw + smem_cn_bytes(a.m, a.cn_stride));
+  const int ncn = (a.m + 1) * a.cn_stride;
+  for (int i = threadIdx.x; i < ncn; i += blockDim.x) cn[i] = a.cn[i];
+  if (BATCHED) {
+    for (int i = threadIdx.x; i < MMAX * 32; i += blockDim.x) {
+      const int j = i >> 5, b = blockIdx.y * 32 + (i & 31);
+      cdd v = (j < a.m && b < a.B) ? a.ucol[(size_t)j * a.B + b] : cdd_zero();
+      u[i] = CONJ ? cdd_conj(v) : v;
+    }
+  } else if (threadIdx.x < MMAX) {
+    cdd v = (int)threadIdx.x < a.m ? a.ucol[threadIdx.x] : cdd_zero();
+    u[threadIdx.x] = CONJ ? cdd_conj(v) : v;
+  }
+  __syncthreads();
+  return u;
+}
+
+// Forward value of state (d, tau) with r tail photons: sum over its occupied modes of
+// u_j x[parent_j].  Prefix modes follow the tile mask (uniform over a tile); tail
+// modes loop over the set bits of the state's own tail occupation.
+template <int MMAX, bool BATCHED>
+__device__ __forceinline__ cdd fwd_value(const SlosArgs& a, const Desc<MMAX>& d, int r, uint32_t tau,
+                                         const cdd* __restrict__ x, const cdd* u, int us, int b) {
+  const int p = a.p;
+  cacc acc = cacc_zero();
 #pragma unroll
-      for (int j = 0; j < MMAX; ++j) {
-        if (j < p) {
-          if ((mask >> j) & 1u) cacc_fma(acc, ld_cdd(&a.in[s_pre[lo][j] + tau]), u[j]);
-        } else if (j < m && r > 0) {
-          const uint32_t e = __ldg(&row[j - p]);
-          if (e != kNone) cacc_fma(acc, ld_cdd(&a.in[tbase + e]), u[j]);
-        }
+  for (int j = 0; j < MMAX; ++j) {
+    if (j < p && ((d.mask >> j) & 1u)) {
+      const uint32_t ad = d.base[j] + tau;
+      cacc_fma(acc, ld_cdd(&x[BATCHED ? (size_t)ad * a.B + b : (size_t)ad]), u[j * us]);
+    }
+  }
+  if (r > 0) {
+    const uint32_t* row = a.tail + a.tail_off[r] + (size_t)tau * a.t;
+    uint32_t occ = 0;
+    for (int jl = 0; jl < a.t; ++jl)
+      if (__ldg(&row[jl]) != kNone) occ |= 1u << jl;
+    while (occ) {
+      const int jl = __ffs(occ) - 1;
+      occ &= occ - 1;
+      const uint32_t ad = d.tb + __ldg(&row[jl]);
+      cacc_fma(acc, ld_cdd(&x[BATCHED ? (size_t)ad * a.B + b : (size_t)ad]), u[(p + jl) * us]);
+    }
+  }
+  return cacc_finish(acc);
+}
+
+template <int MMAX, bool BATCHED>
+__global__ void __launch_bounds__(256) slos_fwd(SlosArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t* cn;
+  const cdd* us_base = load_shared<MMAX, BATCHED, false>(a, smem_raw, cn);
+  const int lane = threadIdx.x & 31;
+  const int b = BATCHED ? blockIdx.y * 32 + lane : 0;
+  const cdd* u = BATCHED ? us_base + lane : us_base;
+  const int us = BATCHED ? 32 : 1;
+  const uint32_t total = a.uoff[a.k + 1];
+  const uint32_t nw = gridDim.x * kWarps;
+  for (uint32_t unit = blockIdx.x * kWarps + (threadIdx.x >> 5); unit < total; unit += nw) {
+    const int r = unit_class(a, unit);
+    const int q = a.k - r;
+    const uint32_t S = a.tsize[r], lu = unit - a.uoff[r], cpt = a.cpt[r];
+    Desc<MMAX> d;
+    if (cpt > 0) {
+      // one tile (uniform prefix), a chunk of its states
+      const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
+      describe<MMAX, false, false>(pi, q, r, a, cn, d, dd{0.f, 0.f});
+      const uint32_t chunk = BATCHED ? kChunkB : kChunk;
+      const uint32_t t0 = ch * chunk, t1 = min(S, t0 + chunk);
+      if (BATCHED) {
+        if (b < a.B)
+          for (uint32_t tau = t0; tau < t1; ++tau)
+            a.out[(size_t)(d.A + tau) * a.B + b] = fwd_value<MMAX, true>(a, d, r, tau, a.in, u, us, b);
+      } else {
+        for (uint32_t tau = t0 + lane; tau < t1; tau += 32)
+          a.out[d.A + tau] = fwd_value<MMAX, false>(a, d, r, tau, a.in, u, us, 0);
       }
-      a.out[s_start[lo] + tau] = cacc_finish(acc);
+    } else {
+      // small tiles swept flat: one state per lane
+      const uint32_t flat = lu * 32 + lane;
+      if (flat < a.npf[r] * S) {
+        const uint32_t pi = flat / S, tau = flat - pi * S;
+        describe<MMAX, false, false>(pi, q, r, a, cn, d, dd{0.f, 0.f});
+        a.out[d.A + tau] = fwd_value<MMAX, false>(a, d, r, tau, a.in, u, us, 0);
+      }
+    }
+  }
+}
+
+// Adjoint value of parent state (d, tau): a_{k-1} = sum_j conj(u_j) a_k[child_j], and
+// g_j += conj(c_{k-1}) a_k[child_j] (every child exists).
+template <int MMAX, bool BATCHED>
+__device__ __forceinline__ void bwd_state(const SlosArgs& a, const Desc<MMAX>& d, int r, uint32_t tau,
+                                          const cdd* uc, int us, int b, cacc (&g)[MMAX]) {
+  const int p = a.p, m = a.m;
+  const size_t pidx = BATCHED ? (size_t)(d.A + tau) * a.B + b : (size_t)(d.A + tau);
+  const cdd cp = cdd_conj(ld_cdd(&a.cpar[pidx]));
+  const uint32_t* row = a.tail + a.tail_off[r] + (size_t)tau * a.t;
+  cacc acc = cacc_zero();
+#pragma unroll
+  for (int j = 0; j < MMAX; ++j) {
+    if (j < m) {
+      const uint32_t ad = j < p ? d.base[j] + tau : d.tb + __ldg(&row[j - p]);
+      const cdd v = ld_cdd(&a.in[BATCHED ? (size_t)ad * a.B + b : (size_t)ad]);
+      cacc_fma(acc, v, uc[j * us]);
+      cacc_fma(g[j], v, cp);
+    }
+  }
+  a.out[pidx] = cacc_finish(acc);
+}
+
+// Adjoint step over the parent layer (its states are the units' states); per-CTA
+// partials of dL/du_j go to gpart.
+template <int MMAX, bool BATCHED>
+__global__ void __launch_bounds__(256) slos_bwd(SlosArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ cdd red[kWarps][32];
+  uint32_t* cn;
+  const cdd* us_base = load_shared<MMAX, BATCHED, true>(a, smem_raw, cn);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int b = BATCHED ? blockIdx.y * 32 + lane : 0;
+  const int m = a.m;
+  const cdd* uc = BATCHED ? us_base + lane : us_base;
+  const int us = BATCHED ? 32 : 1;
+  cacc g[MMAX];
+#pragma unroll
+  for (int j = 0; j < MMAX; ++j) g[j] = cacc_zero();
+  const uint32_t total = a.uoff[a.k + 1];
+  const uint32_t nw = gridDim.x * kWarps;
+  for (uint32_t unit = blockIdx.x * kWarps + wid; unit < total; unit += nw) {
+    const int r = unit_class(a, unit);
+    const int q = a.k - r;
+    const uint32_t S = a.tsize[r], lu = unit - a.uoff[r], cpt = a.cpt[r];
+    Desc<MMAX> d;
+    if (cpt > 0) {
+      const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
+      describe<MMAX, true, false>(pi, q, r, a, cn, d, dd{0.f, 0.f});
+      const uint32_t chunk = BATCHED ? kChunkB : kChunk;
+      const uint32_t t0 = ch * chunk, t1 = min(S, t0 + chunk);
+      if (BATCHED) {
+        if (b < a.B)
+          for (uint32_t tau = t0; tau < t1; ++tau) bwd_state<MMAX, true>(a, d, r, tau, uc, us, b, g);
+      } else {
+        for (uint32_t tau = t0 + lane; tau < t1; tau += 32) bwd_state<MMAX, false>(a, d, r, tau, uc, us, 0, g);
+      }
+    } else {
+      const uint32_t flat = lu * 32 + lane;
+      if (flat < a.npf[r] * S) {
+        const uint32_t pi = flat / S, tau = flat - pi * S;
+        describe<MMAX, true, false>(pi, q, r, a, cn, d, dd{0.f, 0.f});
+        bwd_state<MMAX, false>(a, d, r, tau, uc, us, 0, g);
+      }
+    }
+  }
+  // reduce g over the CTA: over all threads (one circuit) or over warps per lane
+#pragma unroll
+  for (int j = 0; j < MMAX; ++j) {
+    if (j >= m) break;
+    cdd v = cacc_finish(g[j]);
+    if (!BATCHED) {
+#pragma unroll
+      for (int dlt = 16; dlt > 0; dlt >>= 1) {
+        cdd o;
+        o.re.hi = __shfl_down_sync(0xffffffffu, v.re.hi, dlt);
+        o.re.lo = __shfl_down_sync(0xffffffffu, v.re.lo, dlt);
+        o.im.hi = __shfl_down_sync(0xffffffffu, v.im.hi, dlt);
+        o.im.lo = __shfl_down_sync(0xffffffffu, v.im.lo, dlt);
+        v = cdd_add(v, o);
+      }
+    }
+    red[wid][lane] = v;
+    __syncthreads();
+    if (wid == 0) {
+      if (BATCHED) {
+        cdd s2 = red[0][lane];
+        for (int w = 1; w < kWarps; ++w) s2 = cdd_add(s2, red[w][lane]);
+        if (b < a.B) a.gpart[((size_t)blockIdx.x * m + j) * a.B + b] = s2;
+      } else if (lane == 0) {
+        cdd s2 = red[0][0];
+        for (int w = 1; w < kWarps; ++w) s2 = cdd_add(s2, red[w][0]);
+        a.gpart[(size_t)blockIdx.x * m + j] = s2;
+      }
     }
     __syncthreads();
   }
@@ -314,213 +368,64 @@ __device__ __forceinline__ double f2d_int(float f) {
 }
 __device__ __forceinline__ double dd_to_double_fast(dd a) { return f2d_int(a.hi) + f2d_int(a.lo); }
 
-// Probabilities (mode 0), amplitudes (mode 1) or adjoint seed (mode 2) of the last
-// layer over tiles: F = prod(out!) / prod(in!) = fpre (per tile, float-float) x ftail[tau].
+// Last layer -> probabilities (mode 0), amplitudes (mode 1) or the adjoint seed
+// a_n = 2 w F c_n (mode 2), with F = prod(out!) / prod(in!) = f(tile) x ftail[tau].
+__device__ __forceinline__ void fin_state(const SlosArgs& a, dd f, int r, size_t idx, int mode,
+                                          const double* __restrict__ w_in, double* __restrict__ out_real,
+                                          double2* __restrict__ out_c, cdd* __restrict__ seed, uint32_t tau) {
+  const dd F = dd_mul(f, a.ftail[a.tstate_off[r] + tau]);
+  const cdd c = ld_cdd(&a.in[idx]);
+  if (mode == 0) {
+    const dd c2 = dd_add(dd_mul(c.re, c.re), dd_mul(c.im, c.im));
+    out_real[idx] = dd_to_double_fast(dd_mul(c2, F));
+  } else if (mode == 1) {
+    const double sF = sqrt(dd_to_double_fast(F));
+    out_c[idx] = make_double2(dd_to_double_fast(c.re) * sF, dd_to_double_fast(c.im) * sF);
+  } else {
+    const dd f2 = dd_mul(dd_from_double(2.0 * w_in[idx]), F);
+    seed[idx] = {dd_mul(c.re, f2), dd_mul(c.im, f2)};
+  }
+}
+
 template <int MMAX>
-__global__ void __launch_bounds__(256) slos_finalize_tiled(SlosTiledArgs a, const dd* __restrict__ ftail,
-                                                          dd inv_in, int mode, const double* __restrict__ w,
-                                                          double* __restrict__ out_real, double2* __restrict__ out_c,
-                                                          cdd* __restrict__ seed) {
-  extern __shared__ uint32_t cn_s[];
-  __shared__ uint32_t s_off[kTileChunk + 1], s_start[kTileChunk];
-  __shared__ int s_r[kTileChunk];
-  __shared__ dd s_f[kTileChunk];
-  __shared__ uint32_t s_wtot[kTileChunk / 32];
+__global__ void __launch_bounds__(256) slos_fin(SlosArgs a, dd inv_in, int mode, const double* __restrict__ w_in,
+                                               double* __restrict__ out_real, double2* __restrict__ out_c,
+                                               cdd* __restrict__ seed) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t* cn = reinterpret_cast<uint32_t*>(smem_raw);
   const int ncn = (a.m + 1) * a.cn_stride;
-  for (int i = threadIdx.x; i < ncn; i += blockDim.x) cn_s[i] = a.cn[i];
+  for (int i = threadIdx.x; i < ncn; i += blockDim.x) cn[i] = a.cn[i];
   __syncthreads();
-  const int m = a.m, p = a.p, tid = threadIdx.x;
-  const uint32_t nchunks = (a.ntiles + kTileChunk - 1) / kTileChunk;
-  for (uint32_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
-    const uint32_t first = (nchunks - 1 - ch) * kTileChunk;
-    uint32_t size = 0;
-    if (tid < kTileChunk && first + tid < a.ntiles) {
-      // prefix occupation: unrank the tile again, multiplying the factorials
-      uint32_t rho = first + tid;
-      int R = a.k;
-      dd f = inv_in;
-      uint32_t A = 0;
-      for (int i = 0; i < p; ++i) {
-        const int M1 = p + 1 - i;
-        int x = R;
-        while (x > 0) {
-          const uint32_t c = cn_at(cn_s, a.cn_stride, M1, x - 1);
-          if (rho >= c) {
-            rho -= c;
-            break;
-          }
-          --x;
-        }
-        const int v = R - x;
-        for (int q = 2; q <= v; ++q) f = dd_mul_f(f, (float)q);
-        const int Rn = R - v;
-        A += cn_at(cn_s, a.cn_stride, m - i, Rn - 1);
-        R = Rn;
-      }
-      s_start[tid] = A;
-      s_r[tid] = R;
-      s_f[tid] = f;
-      size = a.tsize[R];
-    }
-    chunk_scan(size, s_off, s_wtot);
-    const uint32_t total = s_off[kTileChunk];
-    for (uint32_t idx = tid; idx < total; idx += blockDim.x) {
-      int lo = 0, hi = kTileChunk;
-      while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (s_off[mid] <= idx) lo = mid; else hi = mid;
-      }
-      const uint32_t tau = idx - s_off[lo];
-      const uint32_t r_idx = s_start[lo] + tau;
-      const dd F = dd_mul(s_f[lo], ftail[a.tstate_off[s_r[lo]] + tau]);
-      const cdd c = ld_cdd(&a.in[r_idx]);
-      if (mode == 0) {
-        const dd c2 = dd_add(dd_mul(c.re, c.re), dd_mul(c.im, c.im));
-        out_real[r_idx] = dd_to_double_fast(dd_mul(c2, F));
-      } else if (mode == 1) {
-        const double sF = sqrt(dd_to_double_fast(F));
-        out_c[r_idx] = make_double2(dd_to_double_fast(c.re) * sF, dd_to_double_fast(c.im) * sF);
+  const int lane = threadIdx.x & 31;
+  const bool batched = a.B > 1;
+  const int b = batched ? blockIdx.y * 32 + lane : 0;
+  const uint32_t total = a.uoff[a.k + 1];
+  const uint32_t nw = gridDim.x * kWarps;
+  for (uint32_t unit = blockIdx.x * kWarps + (threadIdx.x >> 5); unit < total; unit += nw) {
+    const int r = unit_class(a, unit);
+    const int q = a.k - r;
+    const uint32_t S = a.tsize[r], lu = unit - a.uoff[r], cpt = a.cpt[r];
+    Desc<MMAX> d;
+    if (cpt > 0) {
+      const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
+      describe<MMAX, false, true>(pi, q, r, a, cn, d, inv_in);
+      const uint32_t chunk = batched ? kChunkB : kChunk;
+      const uint32_t t0 = ch * chunk, t1 = min(S, t0 + chunk);
+      if (batched) {
+        if (b < a.B)
+          for (uint32_t tau = t0; tau < t1; ++tau)
+            fin_state(a, d.f, r, (size_t)(d.A + tau) * a.B + b, mode, w_in, out_real, out_c, seed, tau);
       } else {
-        const dd f2 = dd_mul(dd_from_double(2.0 * w[r_idx]), F);
-        seed[r_idx] = {dd_mul(c.re, f2), dd_mul(c.im, f2)};
+        for (uint32_t tau = t0 + lane; tau < t1; tau += 32)
+          fin_state(a, d.f, r, d.A + tau, mode, w_in, out_real, out_c, seed, tau);
       }
-    }
-    __syncthreads();
-  }
-}
-
-template <int MMAX, bool BATCHED>
-__global__ void __launch_bounds__(256) slos_forward_layer(SlosLayerArgs a) {
-  extern __shared__ uint32_t cn_s[];
-  const int ncn = (a.m + 1) * a.cn_stride;
-  for (int i = threadIdx.x; i < ncn; i += blockDim.x) cn_s[i] = a.cn[i];
-  __syncthreads();
-  const int m = a.m, B = a.B;
-  if (!BATCHED) {
-    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < a.nstates; c += gridDim.x * blockDim.x) {
-      uint32_t pr[MMAX];
-      parent_ranks<MMAX>(c, m, a.k, cn_s, a.cn_stride, pr);
-      cacc acc = cacc_zero();
-#pragma unroll
-      for (int j = 0; j < MMAX; ++j)
-        if (pr[j] != kNone) cacc_fma(acc, ld_cdd(&a.in[pr[j]]), ld_cdd(&a.ucol[j]));
-      a.out[c] = cacc_finish(acc);
-    }
-  } else {
-    const int lane = threadIdx.x & 31;
-    const int b = blockIdx.y * 32 + lane;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    cdd u[MMAX];
-#pragma unroll
-    for (int j = 0; j < MMAX; ++j) u[j] = (j < m && b < B) ? a.ucol[(size_t)j * B + b] : cdd_zero();
-    for (uint32_t c = warp; c < a.nstates; c += nwarps) {
-      uint32_t pr[MMAX];
-      parent_ranks<MMAX>(c, m, a.k, cn_s, a.cn_stride, pr);
-      if (b < B) {
-        cacc acc = cacc_zero();
-#pragma unroll
-        for (int j = 0; j < MMAX; ++j)
-          if (pr[j] != kNone) cacc_fma(acc, ld_cdd(&a.in[(size_t)pr[j] * B + b]), u[j]);
-        a.out[(size_t)c * B + b] = cacc_finish(acc);
+    } else {
+      const uint32_t flat = lu * 32 + lane;
+      if (flat < a.npf[r] * S) {
+        const uint32_t pi = flat / S, tau = flat - pi * S;
+        describe<MMAX, false, true>(pi, q, r, a, cn, d, inv_in);
+        fin_state(a, d.f, r, d.A + tau, mode, w_in, out_real, out_c, seed, tau);
       }
-    }
-  }
-}
-
-// One adjoint step: parent adjoint a_{k-1}[p] = sum_j conj(u_j) a_k[p + e_j] and the
-// per-CTA partial of dL/du_j = sum_p conj(c_{k-1}[p]) a_k[p + e_j].
-template <int MMAX, bool BATCHED>
-__global__ void __launch_bounds__(256) slos_backward_layer(SlosLayerArgs a) {
-  extern __shared__ uint32_t cn_s[];
-  __shared__ cdd red[8][32];
-  const int ncn = (a.m + 1) * a.cn_stride;
-  for (int i = threadIdx.x; i < ncn; i += blockDim.x) cn_s[i] = a.cn[i];
-  __syncthreads();
-  const int m = a.m, B = a.B;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  cacc g[MMAX];
-#pragma unroll
-  for (int j = 0; j < MMAX; ++j) g[j] = cacc_zero();
-
-  if (!BATCHED) {
-    cdd uc[MMAX];
-#pragma unroll
-    for (int j = 0; j < MMAX; ++j) uc[j] = j < m ? cdd_conj(a.ucol[j]) : cdd_zero();
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < a.nstates; p += gridDim.x * blockDim.x) {
-      uint32_t ch[MMAX];
-      child_ranks<MMAX>(p, m, a.k, cn_s, a.cn_stride, ch);
-      const cdd cp = cdd_conj(a.cpar[p]);
-      cacc acc = cacc_zero();
-#pragma unroll
-      for (int j = 0; j < MMAX; ++j) {
-        if (j < m) {
-          const cdd x = ld_cdd(&a.in[ch[j]]);
-          cacc_fma(acc, x, uc[j]);
-          cacc_fma(g[j], x, cp);
-        }
-      }
-      a.out[p] = cacc_finish(acc);
-    }
-    // block reduction of g[j] over all threads; thread 0 of the block writes
-#pragma unroll
-    for (int j = 0; j < MMAX; ++j) {
-      if (j >= m) break;
-      cdd v = cacc_finish(g[j]);
-#pragma unroll
-      for (int d = 16; d > 0; d >>= 1) {
-        cdd o;
-        o.re.hi = __shfl_down_sync(0xffffffffu, v.re.hi, d);
-        o.re.lo = __shfl_down_sync(0xffffffffu, v.re.lo, d);
-        o.im.hi = __shfl_down_sync(0xffffffffu, v.im.hi, d);
-        o.im.lo = __shfl_down_sync(0xffffffffu, v.im.lo, d);
-        v = cdd_add(v, o);
-      }
-      if (lane == 0) red[wid][0] = v;
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        cdd s = red[0][0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) s = cdd_add(s, red[w][0]);
-        a.gpart[(size_t)blockIdx.x * m + j] = s;
-      }
-      __syncthreads();
-    }
-  } else {
-    const int b = blockIdx.y * 32 + lane;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    cdd uc[MMAX];
-#pragma unroll
-    for (int j = 0; j < MMAX; ++j) uc[j] = (j < m && b < B) ? cdd_conj(a.ucol[(size_t)j * B + b]) : cdd_zero();
-    for (uint32_t p = warp; p < a.nstates; p += nwarps) {
-      uint32_t ch[MMAX];
-      child_ranks<MMAX>(p, m, a.k, cn_s, a.cn_stride, ch);
-      if (b < B) {
-        const cdd cp = cdd_conj(a.cpar[(size_t)p * B + b]);
-        cacc acc = cacc_zero();
-#pragma unroll
-        for (int j = 0; j < MMAX; ++j) {
-          if (j < m) {
-            const cdd x = ld_cdd(&a.in[(size_t)ch[j] * B + b]);
-            cacc_fma(acc, x, uc[j]);
-            cacc_fma(g[j], x, cp);
-          }
-        }
-        a.out[(size_t)p * B + b] = cacc_finish(acc);
-      }
-    }
-    // reduce g[j] over the warps of the block, per lane (= circuit)
-#pragma unroll
-    for (int j = 0; j < MMAX; ++j) {
-      if (j >= m) break;
-      red[wid][lane] = cacc_finish(g[j]);
-      __syncthreads();
-      if (wid == 0) {
-        cdd s = red[0][lane];
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) s = cdd_add(s, red[w][lane]);
-        if (b < B) a.gpart[((size_t)blockIdx.x * m + j) * B + b] = s;
-      }
-      __syncthreads();
     }
   }
 }
@@ -555,65 +460,47 @@ __global__ void slos_fill_vacuum(cdd* layer0, int B) {
   if (b < B) layer0[b] = cdd_one();
 }
 
-// mode 0: probabilities (double), 1: amplitudes (complex128), 2: adjoint seed
-// a_n = 2 w F c (needs w), where F = prod(out!) / prod(in!).
-__global__ void slos_finalize(const cdd* __restrict__ cfin, uint32_t nstates, int m, int n, int B,
-                              const uint32_t* __restrict__ cn, int cn_stride, double inv_prodfact_in,
-                              int mode, const double* __restrict__ w, double* __restrict__ out_real,
-                              double2* __restrict__ out_cplx, cdd* __restrict__ seed) {
-  __shared__ double fact[kSlosMaxN + 1];
-  extern __shared__ uint32_t cn_s[];
-  if (threadIdx.x <= kSlosMaxN) {
-    double f = 1.0;
-    for (int i = 2; i <= (int)threadIdx.x; ++i) f *= i;
-    fact[threadIdx.x] = f;
-  }
-  const int ncn = (m + 1) * cn_stride;
-  for (int i = threadIdx.x; i < ncn; i += blockDim.x) cn_s[i] = cn[i];
-  __syncthreads();
-  const size_t tot = (size_t)nstates * B;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
-    const uint32_t r = (uint32_t)(i / B);
-    const double F = state_prodfact(r, m, n, cn_s, cn_stride, fact) * inv_prodfact_in;
-    const cdd c = cfin[i];
-    if (mode == 0) {
-      const dd c2 = dd_add(dd_mul(c.re, c.re), dd_mul(c.im, c.im));
-      out_real[i] = dd_to_double(c2) * F;
-    } else if (mode == 1) {
-      const double s = sqrt(F);
-      out_cplx[i] = make_double2(dd_to_double(c.re) * s, dd_to_double(c.im) * s);
-    } else {
-      const double f = 2.0 * w[i] * F;
-      const dd fd = dd_from_double(f);
-      seed[i] = {dd_mul(c.re, fd), dd_mul(c.im, fd)};
-    }
-  }
-}
+enum class Kern { Fwd, Bwd, Fin };
 
 template <int MMAX>
-static int launch_layer(bool backward, const SlosLayerArgs& a, int grid, cudaStream_t s) {
-  const size_t smem = (size_t)(a.m + 1) * a.cn_stride * sizeof(uint32_t);
+static int launch_kernel(Kern kind, const SlosArgs& a, int grid, dd inv_in, int mode, const double* w,
+                         double* out_real, double2* out_c, cdd* seed, cudaStream_t s) {
+  const size_t smem = smem_bytes<MMAX>(a.m, a.cn_stride);
   const bool batched = a.B > 1;
   dim3 g(grid, batched ? (a.B + 31) / 32 : 1);
-  if (!backward) {
-    if (batched)
-      slos_forward_layer<MMAX, true><<<g, 256, smem, s>>>(a);
-    else
-      slos_forward_layer<MMAX, false><<<g, 256, smem, s>>>(a);
-  } else {
-    if (batched)
-      slos_backward_layer<MMAX, true><<<g, 256, smem, s>>>(a);
-    else
-      slos_backward_layer<MMAX, false><<<g, 256, smem, s>>>(a);
+  // the descriptors of 8 warps, u and the rank table may pass 48 KB: allow it
+  cudaFuncSetAttribute(slos_fwd<MMAX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(slos_fwd<MMAX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(slos_bwd<MMAX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(slos_bwd<MMAX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(slos_fin<MMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  switch (kind) {
+    case Kern::Fwd:
+      if (batched)
+        slos_fwd<MMAX, true><<<g, 256, smem, s>>>(a);
+      else
+        slos_fwd<MMAX, false><<<g, 256, smem, s>>>(a);
+      break;
+    case Kern::Bwd:
+      if (batched)
+        slos_bwd<MMAX, true><<<g, 256, smem, s>>>(a);
+      else
+        slos_bwd<MMAX, false><<<g, 256, smem, s>>>(a);
+      break;
+    case Kern::Fin:
+      slos_fin<MMAX><<<g, 256, smem, s>>>(a, inv_in, mode, w, out_real, out_c, seed);
+      break;
   }
   return (int)cudaGetLastError();
 }
 
-static int dispatch_layer(bool backward, const SlosLayerArgs& a, int grid, cudaStream_t s) {
-  if (a.m <= 8) return launch_layer<8>(backward, a, grid, s);
-  if (a.m <= 16) return launch_layer<16>(backward, a, grid, s);
-  if (a.m <= 24) return launch_layer<24>(backward, a, grid, s);
-  return launch_layer<32>(backward, a, grid, s);
+static int dispatch(Kern kind, const SlosArgs& a, int grid, cudaStream_t s, dd inv_in = dd{0.f, 0.f},
+                    int mode = 0, const double* w = nullptr, double* out_real = nullptr, double2* out_c = nullptr,
+                    cdd* seed = nullptr) {
+  if (a.m <= 8) return launch_kernel<8>(kind, a, grid, inv_in, mode, w, out_real, out_c, seed, s);
+  if (a.m <= 16) return launch_kernel<16>(kind, a, grid, inv_in, mode, w, out_real, out_c, seed, s);
+  if (a.m <= 24) return launch_kernel<24>(kind, a, grid, inv_in, mode, w, out_real, out_c, seed, s);
+  return launch_kernel<32>(kind, a, grid, inv_in, mode, w, out_real, out_c, seed, s);
 }
 
 }  // namespace pcvl
@@ -636,10 +523,10 @@ struct pcvl_slos_plan {
   int gpart_blocks = 0;
   int64_t bytes = 0;
   bool forwarded = false;
-  // tiled single-circuit path (batch == 1)
   int tail_t = 0, tail_p = 0;
-  uint32_t* tail_parent_d = nullptr;   // rank_t(tau - e_j) per tail state and tail mode
-  dd* ftail_d = nullptr;               // prod tau_j! per tail state
+  uint32_t* tp_d = nullptr;       // rank_t(tau - e_j) per tail state and tail mode
+  uint32_t* tc_d = nullptr;       // rank_t(tau + e_j)
+  dd* ftail_d = nullptr;          // prod tau_j! per tail state
   std::vector<uint32_t> tail_off, tstate_off, tsize;
   cdd* final_layer() const { return keep ? layers[n] : layers[n % 2]; }
 };
@@ -654,65 +541,10 @@ void free_plan(pcvl_slos_plan* p) {
   cudaFree(p->adj_d[0]);
   cudaFree(p->adj_d[1]);
   cudaFree(p->gpart_d);
-  cudaFree(p->tail_parent_d);
+  cudaFree(p->tp_d);
+  cudaFree(p->tc_d);
   cudaFree(p->ftail_d);
   delete p;
-}
-
-// Tail tables for t tail modes and up to n tail photons (descending-lex order within
-// each photon number): parent ranks rank_t(tau - e_j) (kNone where tau_j = 0) and the
-// factorial products prod_j tau_j!.
-void tail_tables(int t, int n, std::vector<uint32_t>& parent, std::vector<dd>& ftail, std::vector<uint32_t>& tail_off,
-                 std::vector<uint32_t>& tstate_off, std::vector<uint32_t>& tsize) {
-  tail_off.assign(n + 2, 0);
-  tstate_off.assign(n + 2, 0);
-  tsize.assign(n + 2, 0);
-  parent.clear();
-  ftail.clear();
-  auto rank = [t](const std::vector<int>& s) {
-    int rest = 0;
-    for (int v : s) rest += v;
-    uint64_t r = 0;
-    for (int i = 0; i < t; ++i) {
-      rest -= s[i];
-      if (rest > 0) r += fock_count(t - i, rest - 1);
-    }
-    return (uint32_t)r;
-  };
-  for (int r = 0; r <= n; ++r) {
-    tail_off[r] = (uint32_t)parent.size();
-    tstate_off[r] = (uint32_t)ftail.size();
-    tsize[r] = (uint32_t)fock_count(t, r);
-    std::vector<int> s(t, 0);
-    s[0] = r;
-    for (uint32_t q = 0; q < tsize[r]; ++q) {
-      double f = 1.0;
-      for (int j = 0; j < t; ++j) {
-        for (int v = 2; v <= s[j]; ++v) f *= v;
-        if (s[j] == 0) {
-          parent.push_back(kNone);
-        } else {
-          s[j] -= 1;
-          parent.push_back(rank(s));
-          s[j] += 1;
-        }
-      }
-      ftail.push_back(dd_from_double(f));
-      // next state in descending-lex order
-      int tail = 0;
-      for (int i = t - 2; i >= 0; --i) {
-        tail += s[i + 1];
-        if (s[i] > 0) {
-          s[i] -= 1;
-          s[i + 1] = tail + 1;
-          for (int j = i + 2; j < t; ++j) s[j] = 0;
-          break;
-        }
-      }
-    }
-  }
-  tail_off[n + 1] = (uint32_t)parent.size();
-  tstate_off[n + 1] = (uint32_t)ftail.size();
 }
 
 // Photon-addition order of perceval/backends/_slos.py:61-86 for one input state:
@@ -733,6 +565,65 @@ std::vector<int> path_order(const std::vector<int>& input) {
   return order;
 }
 
+uint32_t tail_rank(int t, const std::vector<int>& s) {
+  int rest = 0;
+  for (int v : s) rest += v;
+  uint64_t r = 0;
+  for (int i = 0; i < t; ++i) {
+    rest -= s[i];
+    if (rest > 0) r += fock_count(t - i, rest - 1);
+  }
+  return (uint32_t)r;
+}
+
+// Tail tables for t tail modes and 0..n tail photons (descending-lex order within each
+// photon number): parent ranks rank_t(tau - e_j) (kNone where tau_j = 0), child ranks
+// rank_t(tau + e_j), and the factorial products prod_j tau_j!.
+void tail_tables(int t, int n, std::vector<uint32_t>& tp, std::vector<uint32_t>& tc, std::vector<dd>& ftail,
+                 std::vector<uint32_t>& tail_off, std::vector<uint32_t>& tstate_off, std::vector<uint32_t>& tsize) {
+  tail_off.assign(n + 2, 0);
+  tstate_off.assign(n + 2, 0);
+  tsize.assign(n + 2, 0);
+  tp.clear();
+  tc.clear();
+  ftail.clear();
+  for (int r = 0; r <= n + 1; ++r) {
+    tail_off[r] = (uint32_t)tp.size();
+    tstate_off[r] = (uint32_t)ftail.size();
+    tsize[r] = (uint32_t)fock_count(t, r);
+    if (r > n) break;
+    std::vector<int> s(t, 0);
+    s[0] = r;
+    for (uint32_t q = 0; q < tsize[r]; ++q) {
+      double f = 1.0;
+      for (int j = 0; j < t; ++j) {
+        for (int v = 2; v <= s[j]; ++v) f *= v;
+        if (s[j] == 0) {
+          tp.push_back(kNone);
+        } else {
+          s[j] -= 1;
+          tp.push_back(tail_rank(t, s));
+          s[j] += 1;
+        }
+        s[j] += 1;
+        tc.push_back(tail_rank(t, s));
+        s[j] -= 1;
+      }
+      ftail.push_back(dd_from_double(f));
+      int tail = 0;  // next state in descending-lex order
+      for (int i = t - 2; i >= 0; --i) {
+        tail += s[i + 1];
+        if (s[i] > 0) {
+          s[i] -= 1;
+          s[i + 1] = tail + 1;
+          for (int j = i + 2; j < t; ++j) s[j] = 0;
+          break;
+        }
+      }
+    }
+  }
+}
+
 int alloc(void** p, size_t bytes, int64_t& total) {
   cudaError_t e = cudaMalloc(p, bytes < 256 ? 256 : bytes);
   if (e != cudaSuccess) {
@@ -744,10 +635,57 @@ int alloc(void** p, size_t bytes, int64_t& total) {
   return PCVL_OK;
 }
 
-int grid_for(uint64_t work_units, int per_block) {
-  const int sms = pcvl::num_sms();
-  uint64_t g = (work_units + per_block - 1) / per_block;
-  g = std::min<uint64_t>(g, (uint64_t)sms * 16);
+int upload(void* dst, const void* src, size_t bytes) {
+  if (cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+    pcvl::set_error("SLOS plan: table upload failed");
+    return PCVL_ERR_CUDA;
+  }
+  return PCVL_OK;
+}
+
+SlosArgs make_args(const pcvl_slos_plan* p, int k) {
+  SlosArgs a{};
+  a.m = p->m;
+  a.k = k;
+  a.p = p->tail_p;
+  a.t = p->tail_t;
+  a.B = p->B;
+  a.ntiles = (uint32_t)fock_count(p->tail_p + 1, k);
+  a.cn = p->cn_d;
+  a.cn_stride = p->cn_stride;
+  a.ftail = p->ftail_d;
+  for (int r = 0; r <= p->n + 1; ++r) {
+    a.tail_off[r] = p->tail_off[r];
+    a.tstate_off[r] = p->tstate_off[r];
+    a.tsize[r] = p->tsize[r];
+  }
+  // work units by class r = tail photons: batched -> (tile, kChunkB states); single
+  // circuit -> (tile, kChunk states) for tiles of >= 32 states, flat 32-state units below
+  uint64_t u = 0;
+  for (int r = 0; r <= k; ++r) {
+    const uint64_t npf = fock_count(p->tail_p, k - r), S = p->tsize[r];
+    a.uoff[r] = (uint32_t)u;
+    a.npf[r] = (uint32_t)npf;
+    if (p->B > 1) {
+      a.cpt[r] = (uint32_t)((S + kChunkB - 1) / kChunkB);
+      u += npf * a.cpt[r];
+    } else if (S >= 32) {
+      a.cpt[r] = (uint32_t)((S + kChunk - 1) / kChunk);
+      u += npf * a.cpt[r];
+    } else {
+      a.cpt[r] = 0;
+      u += (npf * S + 31) / 32;
+    }
+  }
+  a.uoff[k + 1] = (uint32_t)u;
+  return a;
+}
+
+// CTAs for a layer: one warp per unit, capped at 16 CTAs per SM (grid-stride beyond)
+int grid_for_units(const SlosArgs& a) {
+  const uint64_t units = a.uoff[a.k + 1];
+  uint64_t g = (units + kWarps - 1) / kWarps;
+  g = std::min<uint64_t>(g, (uint64_t)pcvl::num_sms() * 16);
   return (int)std::max<uint64_t>(g, 1);
 }
 
@@ -781,8 +719,8 @@ extern "C" int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int
     p->sizes[k] = fock_count(m, k);
     if (p->sizes[k] >= 0xffffffffull) {
       delete p;
-      set_error("SLOS layer %d holds %llu states: more than 2^32 - 1 states per layer is not supported",
-                k, (unsigned long long)fock_count(m, k));
+      set_error("SLOS layer %d holds %llu states: more than 2^32 - 1 states per layer is not supported", k,
+                (unsigned long long)fock_count(m, k));
       return PCVL_ERR_ARG;
     }
   }
@@ -790,9 +728,11 @@ extern "C" int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int
   const size_t B = (size_t)batch;
   size_t need = 0;
   if (p->keep) {
-    for (int k = 0; k <= n; ++k) need += p->sizes[k] * B * sizeof(cdd);
     size_t mx = 0;
-    for (int k = 0; k <= n; ++k) mx = std::max<size_t>(mx, p->sizes[k]);
+    for (int k = 0; k <= n; ++k) {
+      need += p->sizes[k] * B * sizeof(cdd);
+      mx = std::max<size_t>(mx, p->sizes[k]);
+    }
     need += 2 * mx * B * sizeof(cdd);
   } else {
     need += (p->sizes[n] + (n > 0 ? p->sizes[n - 1] : 0)) * B * sizeof(cdd);
@@ -805,16 +745,29 @@ extern "C" int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int
   }
 
   int rc = PCVL_OK;
-  p->cn_stride = n + 1;
+  // the tail: at most 8 modes and a table of at most 10^6 tail states over 0..n+1 photons
+  int t = std::min(m, 8);
+  while (t > 1 && fock_count(t + 1, n + 1) > 1000000ull) --t;
+  p->tail_t = t;
+  p->tail_p = m - t;
+  std::vector<uint32_t> tp, tc;
+  std::vector<dd> ftail;
+  tail_tables(t, n, tp, tc, ftail, p->tail_off, p->tstate_off, p->tsize);
+  p->cn_stride = n + 2;
   std::vector<uint32_t> cn((size_t)(m + 1) * p->cn_stride);
   for (int M = 0; M <= m; ++M)
-    for (int x = 0; x <= n; ++x) cn[(size_t)M * p->cn_stride + x] = (uint32_t)fock_count(M, x);
+    for (int x = 0; x < p->cn_stride; ++x) {
+      const uint64_t v = fock_count(M, x);
+      cn[(size_t)M * p->cn_stride + x] = v > 0xffffffffull ? 0xffffffffu : (uint32_t)v;
+    }
   if ((rc = alloc((void**)&p->cn_d, cn.size() * 4, p->bytes)) != PCVL_OK) goto fail;
-  if (cudaMemcpy(p->cn_d, cn.data(), cn.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
-    set_error("SLOS plan: table upload failed");
-    rc = PCVL_ERR_CUDA;
-    goto fail;
-  }
+  if ((rc = upload(p->cn_d, cn.data(), cn.size() * 4)) != PCVL_OK) goto fail;
+  if ((rc = alloc((void**)&p->tp_d, tp.size() * 4, p->bytes)) != PCVL_OK) goto fail;
+  if ((rc = upload(p->tp_d, tp.data(), tp.size() * 4)) != PCVL_OK) goto fail;
+  if ((rc = alloc((void**)&p->tc_d, tc.size() * 4, p->bytes)) != PCVL_OK) goto fail;
+  if ((rc = upload(p->tc_d, tc.data(), tc.size() * 4)) != PCVL_OK) goto fail;
+  if ((rc = alloc((void**)&p->ftail_d, ftail.size() * sizeof(dd), p->bytes)) != PCVL_OK) goto fail;
+  if ((rc = upload(p->ftail_d, ftail.data(), ftail.size() * sizeof(dd))) != PCVL_OK) goto fail;
   if ((rc = alloc((void**)&p->ucols_d, (size_t)m * m * B * sizeof(cdd), p->bytes)) != PCVL_OK) goto fail;
   if (p->keep) {
     p->layers.assign(n + 1, nullptr);
@@ -824,7 +777,7 @@ extern "C" int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int
     for (int k = 0; k <= n; ++k) mx = std::max<size_t>(mx, p->sizes[k]);
     for (int i = 0; i < 2; ++i)
       if ((rc = alloc((void**)&p->adj_d[i], mx * B * sizeof(cdd), p->bytes)) != PCVL_OK) goto fail;
-    p->gpart_blocks = pcvl::num_sms() * 4;
+    p->gpart_blocks = pcvl::num_sms() * 16;
     if ((rc = alloc((void**)&p->gpart_d, (size_t)p->gpart_blocks * m * B * sizeof(cdd), p->bytes)) != PCVL_OK)
       goto fail;
   } else {
@@ -835,74 +788,11 @@ extern "C" int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int
     if ((rc = alloc((void**)&p->layers[1], std::max<size_t>(s1, 1) * B * sizeof(cdd), p->bytes)) != PCVL_OK)
       goto fail;
   }
-  if (batch == 1) {
-    // largest tail (<= 8 modes, < m so the prefix is non-empty unless m == 1) whose
-    // tables stay small: count(t + 1, n) tail states over all photon numbers
-    int t = std::min(m, 8);
-    while (t > 1 && fock_count(t + 1, n) > 1000000ull) --t;
-    p->tail_t = t;
-    p->tail_p = m - t;
-    std::vector<uint32_t> parent;
-    std::vector<dd> ftail;
-    tail_tables(t, n, parent, ftail, p->tail_off, p->tstate_off, p->tsize);
-    if ((rc = alloc((void**)&p->tail_parent_d, parent.size() * 4, p->bytes)) != PCVL_OK) goto fail;
-    if ((rc = alloc((void**)&p->ftail_d, ftail.size() * sizeof(dd), p->bytes)) != PCVL_OK) goto fail;
-    if (cudaMemcpy(p->tail_parent_d, parent.data(), parent.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(p->ftail_d, ftail.data(), ftail.size() * sizeof(dd), cudaMemcpyHostToDevice) != cudaSuccess) {
-      set_error("SLOS plan: tail table upload failed");
-      rc = PCVL_ERR_CUDA;
-      goto fail;
-    }
-  }
   *plan = p;
   return PCVL_OK;
 fail:
   free_plan(p);
   return rc;
-}
-
-static SlosTiledArgs tiled_args(const pcvl_slos_plan* p, int k) {
-  SlosTiledArgs a{};
-  a.m = p->m;
-  a.k = k;
-  a.p = p->tail_p;
-  a.t = p->tail_t;
-  a.ntiles = (uint32_t)fock_count(p->tail_p + 1, k);
-  a.cn = p->cn_d;
-  a.cn_stride = p->cn_stride;
-  a.tail = p->tail_parent_d;
-  for (int r = 0; r <= p->n + 1 && r < kSlosMaxN + 2; ++r) {
-    a.tail_off[r] = p->tail_off[r];
-    a.tstate_off[r] = p->tstate_off[r];
-    a.tsize[r] = p->tsize[r];
-  }
-  return a;
-}
-
-template <int MMAX>
-static int launch_tiled(const SlosTiledArgs& a, cudaStream_t s) {
-  const size_t smem = (size_t)(a.m + 1) * a.cn_stride * sizeof(uint32_t);
-  const uint32_t chunks = (a.ntiles + kTileChunk - 1) / kTileChunk;
-  const int grid = (int)std::max<uint32_t>(1, std::min<uint32_t>(chunks, (uint32_t)num_sms() * 8));
-  slos_forward_tiled<MMAX><<<grid, 256, smem, s>>>(a);
-  return (int)cudaGetLastError();
-}
-
-static int dispatch_tiled(const SlosTiledArgs& a, cudaStream_t s) {
-  if (a.m <= 8) return launch_tiled<8>(a, s);
-  if (a.m <= 16) return launch_tiled<16>(a, s);
-  if (a.m <= 24) return launch_tiled<24>(a, s);
-  return launch_tiled<32>(a, s);
-}
-
-template <int MMAX>
-static int launch_fin_tiled(const SlosTiledArgs& a, const dd* ftail, dd inv_in, int mode, const double* w,
-                            double* out_real, double2* out_c, cdd* seed, cudaStream_t s) {
-  const size_t smem = (size_t)(a.m + 1) * a.cn_stride * sizeof(uint32_t);
-  const uint32_t chunks = (a.ntiles + kTileChunk - 1) / kTileChunk;
-  const int grid = (int)std::max<uint32_t>(1, std::min<uint32_t>(chunks, (uint32_t)num_sms() * 8));
-  slos_finalize_tiled<MMAX><<<grid, 256, smem, s>>>(a, ftail, inv_in, mode, w, out_real, out_c, seed);
-  return (int)cudaGetLastError();
 }
 
 extern "C" int pcvl_slos_plan_destroy(pcvl_slos_plan* plan) {
@@ -926,32 +816,20 @@ extern "C" int pcvl_slos_forward(pcvl_slos_plan* p, const double* u_d, void* str
   PCVL_CHECK(p && u_d, "null pointer argument");
   cudaStream_t s = (cudaStream_t)stream_;
   const int m = p->m, B = p->B;
-  slos_convert_u<<<grid_for((uint64_t)B * m * m, 256), 256, 0, s>>>((const double2*)u_d, m, B, p->ucols_d);
+  {
+    const int g = (int)std::max<uint64_t>(1, std::min<uint64_t>(((uint64_t)B * m * m + 255) / 256, 4096));
+    slos_convert_u<<<g, 256, 0, s>>>((const double2*)u_d, m, B, p->ucols_d);
+  }
   PCVL_CUDA(cudaGetLastError());
-  cdd* l0 = p->layers[0];
-  slos_fill_vacuum<<<(B + 255) / 256, 256, 0, s>>>(l0, B);
+  slos_fill_vacuum<<<(B + 255) / 256, 256, 0, s>>>(p->layers[0], B);
   PCVL_CUDA(cudaGetLastError());
   for (int k = 1; k <= p->n; ++k) {
-    SlosLayerArgs a{};
-    a.m = m;
-    a.k = k;
-    a.B = B;
-    a.nstates = (uint32_t)p->sizes[k];
+    SlosArgs a = make_args(p, k);
     a.in = p->keep ? p->layers[k - 1] : p->layers[(k - 1) % 2];
     a.out = p->keep ? p->layers[k] : p->layers[k % 2];
     a.ucol = p->ucols_d + (size_t)p->order[k - 1] * m * B;
-    a.cn = p->cn_d;
-    a.cn_stride = p->cn_stride;
-    int rc;
-    if (B == 1) {
-      SlosTiledArgs ta = tiled_args(p, k);
-      ta.in = a.in;
-      ta.out = a.out;
-      ta.ucol = a.ucol;
-      rc = dispatch_tiled(ta, s);
-    } else {
-      rc = dispatch_layer(false, a, grid_for(a.nstates, 8), s);
-    }
+    a.tail = p->tp_d;
+    const int rc = dispatch(Kern::Fwd, a, grid_for_units(a), s);
     if (rc != 0) {
       set_error("SLOS layer %d launch failed: %s", k, cudaGetErrorString((cudaError_t)rc));
       return PCVL_ERR_CUDA;
@@ -964,31 +842,14 @@ extern "C" int pcvl_slos_forward(pcvl_slos_plan* p, const double* u_d, void* str
 static int finalize(pcvl_slos_plan* p, int mode, const double* w, double* out_real, double2* out_c, cdd* seed,
                     cudaStream_t s) {
   PCVL_CHECK(p->forwarded, "pcvl_slos_forward has not run on this plan");
-  if (p->B == 1) {
-    SlosTiledArgs ta = tiled_args(p, p->n);
-    ta.in = p->final_layer();
-    const dd inv_in = dd_from_double(1.0 / p->prodfact_in);
-    int rc;
-    if (p->m <= 8)
-      rc = launch_fin_tiled<8>(ta, p->ftail_d, inv_in, mode, w, out_real, out_c, seed, s);
-    else if (p->m <= 16)
-      rc = launch_fin_tiled<16>(ta, p->ftail_d, inv_in, mode, w, out_real, out_c, seed, s);
-    else if (p->m <= 24)
-      rc = launch_fin_tiled<24>(ta, p->ftail_d, inv_in, mode, w, out_real, out_c, seed, s);
-    else
-      rc = launch_fin_tiled<32>(ta, p->ftail_d, inv_in, mode, w, out_real, out_c, seed, s);
-    if (rc != 0) {
-      set_error("SLOS finalize launch failed: %s", cudaGetErrorString((cudaError_t)rc));
-      return PCVL_ERR_CUDA;
-    }
-    return PCVL_OK;
+  SlosArgs a = make_args(p, p->n);
+  a.in = p->final_layer();
+  const int rc = dispatch(Kern::Fin, a, grid_for_units(a), s, dd_from_double(1.0 / p->prodfact_in),
+                          mode, w, out_real, out_c, seed);
+  if (rc != 0) {
+    set_error("SLOS finalize launch failed: %s", cudaGetErrorString((cudaError_t)rc));
+    return PCVL_ERR_CUDA;
   }
-  const size_t smem = (size_t)(p->m + 1) * p->cn_stride * sizeof(uint32_t);
-  const uint64_t tot = p->sizes[p->n] * (uint64_t)p->B;
-  slos_finalize<<<grid_for(tot, 256), 256, smem, s>>>(p->final_layer(), (uint32_t)p->sizes[p->n], p->m, p->n,
-                                                      p->B, p->cn_d, p->cn_stride, 1.0 / p->prodfact_in, mode,
-                                                      w, out_real, out_c, seed);
-  PCVL_CUDA(cudaGetLastError());
   return PCVL_OK;
 }
 
@@ -1005,26 +866,22 @@ extern "C" int pcvl_slos_amplitudes(pcvl_slos_plan* p, double* amps_d, void* str
 extern "C" int pcvl_slos_backward(pcvl_slos_plan* p, const double* weights_d, double* grad_u_d, void* stream_) {
   PCVL_CHECK(p && weights_d && grad_u_d, "null pointer argument");
   PCVL_CHECK(p->keep, "pcvl_slos_backward needs a plan created with keep_layers != 0");
+  PCVL_CHECK(p->forwarded, "pcvl_slos_forward has not run on this plan");
   cudaStream_t s = (cudaStream_t)stream_;
   const int m = p->m, B = p->B, n = p->n;
   PCVL_CUDA(cudaMemsetAsync(grad_u_d, 0, (size_t)B * m * m * 2 * sizeof(double), s));
   PCVL_TRY(finalize(p, 2, weights_d, nullptr, nullptr, p->adj_d[n % 2], s));
   for (int k = n; k >= 1; --k) {
-    SlosLayerArgs a{};
-    a.m = m;
-    a.k = k - 1;  // photons of the parent layer
-    a.B = B;
-    a.nstates = (uint32_t)p->sizes[k - 1];
+    SlosArgs a = make_args(p, k - 1);  // tiles of the parent layer
     a.in = p->adj_d[k % 2];
     a.out = p->adj_d[(k - 1) % 2];
     const int mk = p->order[k - 1];
     a.ucol = p->ucols_d + (size_t)mk * m * B;
-    a.cn = p->cn_d;
-    a.cn_stride = p->cn_stride;
     a.cpar = p->layers[k - 1];
     a.gpart = p->gpart_d;
-    const int grid = std::min(p->gpart_blocks, B > 1 ? grid_for(a.nstates, 8) : grid_for(a.nstates, 256));
-    const int rc = dispatch_layer(true, a, grid, s);
+    a.tail = p->tc_d;
+    const int grid = std::min(p->gpart_blocks, grid_for_units(a));
+    const int rc = dispatch(Kern::Bwd, a, grid, s);
     if (rc != 0) {
       set_error("SLOS adjoint layer %d launch failed: %s", k, cudaGetErrorString((cudaError_t)rc));
       return PCVL_ERR_CUDA;
