@@ -63,12 +63,13 @@ struct SlosArgs {
   int cn_stride;
   const uint32_t* tail;   // TP (forward) or TC (adjoint)
   const dd* ftail;        // prod tau_j! per tail state
+  const uint8_t* tocc;    // occupied tail modes per tail state (bit j)
   uint32_t tail_off[kSlosMaxN + 2];    // entry offset of the block of r tail photons
   uint32_t tstate_off[kSlosMaxN + 2];  // state offset of that block
   uint32_t tsize[kSlosMaxN + 2];       // count(t, r)
   // work units of the layer, by tail photon count r (class r: count(p, k - r) tiles
-  // of tsize[r] states): unit offsets, tiles, and chunks per tile (0: the class is
-  // swept flat, 32 states per unit, one lane per state)
+  // of tsize[r] states): unit offsets, tiles, and chunks per tile (0: small tiles,
+  // 32 whole tiles per unit, one per lane)
   uint32_t uoff[kSlosMaxN + 2];
   uint32_t npf[kSlosMaxN + 1];
   uint32_t cpt[kSlosMaxN + 1];
@@ -95,7 +96,7 @@ struct Desc {
 // tail photons and walks the modes once for the tile's offsets.
 template <int MMAX, bool ADJ, bool FACT>
 __device__ __forceinline__ void describe(uint32_t pi_idx, int q, int r, const SlosArgs& a, const uint32_t* cn,
-                                         Desc<MMAX>& d, dd inv_in) {
+                                         Desc<MMAX>& d, dd inv_in, uint32_t* base) {
   const int m = a.m, p = a.p, st = a.cn_stride;
   uint32_t rho = pi_idx, A = 0, acc = 0, mask = 0;
   int Rp = q, R = q + r;
@@ -121,12 +122,12 @@ __device__ __forceinline__ void describe(uint32_t pi_idx, int q, int r, const Sl
       Rp -= v;
       const int Rn = R - v;
       if (ADJ) {
-        d.base[i] = acc;  // Q_i
+        base[i] = acc;  // Q_i
         acc += cn_at(cn, st, m - i - 1, Rn);
       } else {
         if (v > 0) {
           mask |= 1u << i;
-          d.base[i] = acc;  // Pfx_i
+          base[i] = acc;  // Pfx_i
         }
         acc += cn_at(cn, st, m - i - 1, Rn - 1);
       }
@@ -138,9 +139,9 @@ __device__ __forceinline__ void describe(uint32_t pi_idx, int q, int r, const Sl
   for (int i = 0; i < MMAX; ++i) {
     if (i < p) {
       if (ADJ)
-        d.base[i] = A + d.base[i];
+        base[i] = A + base[i];
       else if ((mask >> i) & 1u)
-        d.base[i] = A - d.base[i];
+        base[i] = A - base[i];
     }
   }
   d.A = A;
@@ -216,44 +217,78 @@ __device__ __forceinline__ cdd fwd_value(const SlosArgs& a, const Desc<MMAX>& d,
   return cacc_finish(acc);
 }
 
-template <int MMAX, bool BATCHED>
-__global__ void __launch_bounds__(256) slos_fwd(SlosArgs a) {
+// Batched forward layer: a warp takes a unit (one tile, up to kChunkB states) and its
+// lanes 32 circuits; the parent offsets are warp-uniform, the loads coalesced.
+template <int MMAX>
+__global__ void __launch_bounds__(256) slos_fwdb(SlosArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t* cn;
-  const cdd* us_base = load_shared<MMAX, BATCHED, false>(a, smem_raw, cn);
+  const cdd* us_base = load_shared<MMAX, true, false>(a, smem_raw, cn);
   const int lane = threadIdx.x & 31;
-  const int b = BATCHED ? blockIdx.y * 32 + lane : 0;
-  const cdd* u = BATCHED ? us_base + lane : us_base;
-  const int us = BATCHED ? 32 : 1;
+  const int b = blockIdx.y * 32 + lane;
+  const cdd* u = us_base + lane;
+  const uint32_t total = a.uoff[a.k + 1];
+  const uint32_t nw = gridDim.x * kWarps;
+  for (uint32_t unit = blockIdx.x * kWarps + (threadIdx.x >> 5); unit < total; unit += nw) {
+    const int r = unit_class(a, unit);
+    const uint32_t S = a.tsize[r], lu = unit - a.uoff[r], cpt = a.cpt[r];
+    const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
+    Desc<MMAX> d;
+    describe<MMAX, false, false>(pi, a.k - r, r, a, cn, d, dd{0.f, 0.f}, d.base);
+    const uint32_t t0 = ch * kChunkB, t1 = min(S, t0 + kChunkB);
+    if (b < a.B)
+      for (uint32_t tau = t0; tau < t1; ++tau)
+        a.out[(size_t)(d.A + tau) * a.B + b] = fwd_value<MMAX, true>(a, d, r, tau, a.in, u, 32, b);
+  }
+}
+
+// Single-circuit forward layer.  Every lane keeps its tile's parent offsets in its
+// own shared-memory slot and loops over the set bits of its state's occupation mask
+// (prefix bits from the tile, tail bits from a per-tail-state table), so a warp runs
+// as many multiply-adds as its busiest lane, not one per mode.
+template <int MMAX>
+__global__ void __launch_bounds__(256) slos_fwd1(SlosArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t* cn;
+  const cdd* u = load_shared<MMAX, false, false>(a, smem_raw, cn);
+  uint32_t* sbase = reinterpret_cast<uint32_t*>(smem_raw + smem_cn_bytes(a.m, a.cn_stride) +
+                                                (size_t)MMAX * 32 * sizeof(cdd)) +
+                    (size_t)threadIdx.x * MMAX;
+  const int lane = threadIdx.x & 31, p = a.p;
   const uint32_t total = a.uoff[a.k + 1];
   const uint32_t nw = gridDim.x * kWarps;
   for (uint32_t unit = blockIdx.x * kWarps + (threadIdx.x >> 5); unit < total; unit += nw) {
     const int r = unit_class(a, unit);
     const int q = a.k - r;
     const uint32_t S = a.tsize[r], lu = unit - a.uoff[r], cpt = a.cpt[r];
+    uint32_t pi, t0, t1, tstep;
+    if (cpt > 0) {  // one tile, a chunk of its states, one state per lane
+      pi = lu / cpt;
+      t0 = (lu - pi * cpt) * kChunk + lane;
+      t1 = min(S, (lu - pi * cpt) * kChunk + kChunk);
+      tstep = 32;
+    } else {        // small tiles: one tile per lane, all its states
+      pi = lu * 32 + lane;
+      t0 = 0;
+      t1 = pi < a.npf[r] ? S : 0;
+      tstep = 1;
+    }
+    if (t0 >= t1) continue;
     Desc<MMAX> d;
-    if (cpt > 0) {
-      // one tile (uniform prefix), a chunk of its states
-      const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
-      describe<MMAX, false, false>(pi, q, r, a, cn, d, dd{0.f, 0.f});
-      const uint32_t chunk = BATCHED ? kChunkB : kChunk;
-      const uint32_t t0 = ch * chunk, t1 = min(S, t0 + chunk);
-      if (BATCHED) {
-        if (b < a.B)
-          for (uint32_t tau = t0; tau < t1; ++tau)
-            a.out[(size_t)(d.A + tau) * a.B + b] = fwd_value<MMAX, true>(a, d, r, tau, a.in, u, us, b);
-      } else {
-        for (uint32_t tau = t0 + lane; tau < t1; tau += 32)
-          a.out[d.A + tau] = fwd_value<MMAX, false>(a, d, r, tau, a.in, u, us, 0);
+    describe<MMAX, false, false>(pi, q, r, a, cn, d, dd{0.f, 0.f}, sbase);
+    const uint8_t* occ_t = a.tocc + a.tstate_off[r];
+    const uint32_t* rows = a.tail + a.tail_off[r];
+    for (uint32_t tau = t0; tau < t1; tau += tstep) {
+      uint32_t occ = d.mask | ((uint32_t)__ldg(&occ_t[tau]) << p);
+      const uint32_t* row = rows + (size_t)tau * a.t - p;
+      cacc acc = cacc_zero();
+      while (occ) {
+        const int j = __ffs(occ) - 1;
+        occ &= occ - 1;
+        const uint32_t ad = j < p ? sbase[j] + tau : d.tb + __ldg(&row[j]);
+        cacc_fma(acc, ld_cdd(&a.in[ad]), u[j]);
       }
-    } else {
-      // small tiles swept flat: one state per lane
-      const uint32_t flat = lu * 32 + lane;
-      if (flat < a.npf[r] * S) {
-        const uint32_t pi = flat / S, tau = flat - pi * S;
-        describe<MMAX, false, false>(pi, q, r, a, cn, d, dd{0.f, 0.f});
-        a.out[d.A + tau] = fwd_value<MMAX, false>(a, d, r, tau, a.in, u, us, 0);
-      }
+      a.out[d.A + tau] = cacc_finish(acc);
     }
   }
 }
@@ -305,7 +340,7 @@ __global__ void __launch_bounds__(256) slos_bwd(SlosArgs a) {
     Desc<MMAX> d;
     if (cpt > 0) {
       const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
-      describe<MMAX, true, false>(pi, q, r, a, cn, d, dd{0.f, 0.f});
+      describe<MMAX, true, false>(pi, q, r, a, cn, d, dd{0.f, 0.f}, d.base);
       const uint32_t chunk = BATCHED ? kChunkB : kChunk;
       const uint32_t t0 = ch * chunk, t1 = min(S, t0 + chunk);
       if (BATCHED) {
@@ -315,11 +350,11 @@ __global__ void __launch_bounds__(256) slos_bwd(SlosArgs a) {
         for (uint32_t tau = t0 + lane; tau < t1; tau += 32) bwd_state<MMAX, false>(a, d, r, tau, uc, us, 0, g);
       }
     } else {
-      const uint32_t flat = lu * 32 + lane;
-      if (flat < a.npf[r] * S) {
-        const uint32_t pi = flat / S, tau = flat - pi * S;
-        describe<MMAX, true, false>(pi, q, r, a, cn, d, dd{0.f, 0.f});
-        bwd_state<MMAX, false>(a, d, r, tau, uc, us, 0, g);
+      // small tiles: one tile per lane
+      const uint32_t pi = lu * 32 + lane;
+      if (pi < a.npf[r]) {
+        describe<MMAX, true, false>(pi, q, r, a, cn, d, dd{0.f, 0.f}, d.base);
+        for (uint32_t tau = 0; tau < S; ++tau) bwd_state<MMAX, false>(a, d, r, tau, uc, us, 0, g);
       }
     }
   }
@@ -408,7 +443,7 @@ __global__ void __launch_bounds__(256) slos_fin(SlosArgs a, dd inv_in, int mode,
     Desc<MMAX> d;
     if (cpt > 0) {
       const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
-      describe<MMAX, false, true>(pi, q, r, a, cn, d, inv_in);
+      describe<MMAX, false, true>(pi, q, r, a, cn, d, inv_in, d.base);
       const uint32_t chunk = batched ? kChunkB : kChunk;
       const uint32_t t0 = ch * chunk, t1 = min(S, t0 + chunk);
       if (batched) {
@@ -420,11 +455,10 @@ __global__ void __launch_bounds__(256) slos_fin(SlosArgs a, dd inv_in, int mode,
           fin_state(a, d.f, r, d.A + tau, mode, w_in, out_real, out_c, seed, tau);
       }
     } else {
-      const uint32_t flat = lu * 32 + lane;
-      if (flat < a.npf[r] * S) {
-        const uint32_t pi = flat / S, tau = flat - pi * S;
-        describe<MMAX, false, true>(pi, q, r, a, cn, d, inv_in);
-        fin_state(a, d.f, r, d.A + tau, mode, w_in, out_real, out_c, seed, tau);
+      const uint32_t pi = lu * 32 + lane;
+      if (pi < a.npf[r]) {
+        describe<MMAX, false, true>(pi, q, r, a, cn, d, inv_in, d.base);
+        for (uint32_t tau = 0; tau < S; ++tau) fin_state(a, d.f, r, d.A + tau, mode, w_in, out_real, out_c, seed, tau);
       }
     }
   }
@@ -469,17 +503,19 @@ static int launch_kernel(Kern kind, const SlosArgs& a, int grid, dd inv_in, int 
   const bool batched = a.B > 1;
   dim3 g(grid, batched ? (a.B + 31) / 32 : 1);
   // the descriptors of 8 warps, u and the rank table may pass 48 KB: allow it
-  cudaFuncSetAttribute(slos_fwd<MMAX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaFuncSetAttribute(slos_fwd<MMAX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(slos_fwdb<MMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaFuncSetAttribute(slos_bwd<MMAX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaFuncSetAttribute(slos_bwd<MMAX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaFuncSetAttribute(slos_fin<MMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   switch (kind) {
     case Kern::Fwd:
-      if (batched)
-        slos_fwd<MMAX, true><<<g, 256, smem, s>>>(a);
-      else
-        slos_fwd<MMAX, false><<<g, 256, smem, s>>>(a);
+      if (batched) {
+        slos_fwdb<MMAX><<<g, 256, smem, s>>>(a);
+      } else {
+        const size_t smem1 = smem + (size_t)256 * MMAX * sizeof(uint32_t);
+        cudaFuncSetAttribute(slos_fwd1<MMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+        slos_fwd1<MMAX><<<g, 256, smem1, s>>>(a);
+      }
       break;
     case Kern::Bwd:
       if (batched)
@@ -526,6 +562,7 @@ struct pcvl_slos_plan {
   int tail_t = 0, tail_p = 0;
   uint32_t* tp_d = nullptr;       // rank_t(tau - e_j) per tail state and tail mode
   uint32_t* tc_d = nullptr;       // rank_t(tau + e_j)
+  uint8_t* tocc_d = nullptr;      // occupied tail modes per tail state
   dd* ftail_d = nullptr;          // prod tau_j! per tail state
   std::vector<uint32_t> tail_off, tstate_off, tsize;
   cdd* final_layer() const { return keep ? layers[n] : layers[n % 2]; }
@@ -543,6 +580,7 @@ void free_plan(pcvl_slos_plan* p) {
   cudaFree(p->gpart_d);
   cudaFree(p->tp_d);
   cudaFree(p->tc_d);
+  cudaFree(p->tocc_d);
   cudaFree(p->ftail_d);
   delete p;
 }
@@ -580,13 +618,15 @@ uint32_t tail_rank(int t, const std::vector<int>& s) {
 // photon number): parent ranks rank_t(tau - e_j) (kNone where tau_j = 0), child ranks
 // rank_t(tau + e_j), and the factorial products prod_j tau_j!.
 void tail_tables(int t, int n, std::vector<uint32_t>& tp, std::vector<uint32_t>& tc, std::vector<dd>& ftail,
-                 std::vector<uint32_t>& tail_off, std::vector<uint32_t>& tstate_off, std::vector<uint32_t>& tsize) {
+                 std::vector<uint8_t>& tocc, std::vector<uint32_t>& tail_off, std::vector<uint32_t>& tstate_off,
+                 std::vector<uint32_t>& tsize) {
   tail_off.assign(n + 2, 0);
   tstate_off.assign(n + 2, 0);
   tsize.assign(n + 2, 0);
   tp.clear();
   tc.clear();
   ftail.clear();
+  tocc.clear();
   for (int r = 0; r <= n + 1; ++r) {
     tail_off[r] = (uint32_t)tp.size();
     tstate_off[r] = (uint32_t)ftail.size();
@@ -596,7 +636,9 @@ void tail_tables(int t, int n, std::vector<uint32_t>& tp, std::vector<uint32_t>&
     s[0] = r;
     for (uint32_t q = 0; q < tsize[r]; ++q) {
       double f = 1.0;
+      uint8_t occ = 0;
       for (int j = 0; j < t; ++j) {
+        if (s[j] > 0) occ |= (uint8_t)(1u << j);
         for (int v = 2; v <= s[j]; ++v) f *= v;
         if (s[j] == 0) {
           tp.push_back(kNone);
@@ -610,6 +652,7 @@ void tail_tables(int t, int n, std::vector<uint32_t>& tp, std::vector<uint32_t>&
         s[j] -= 1;
       }
       ftail.push_back(dd_from_double(f));
+      tocc.push_back(occ);
       int tail = 0;  // next state in descending-lex order
       for (int i = t - 2; i >= 0; --i) {
         tail += s[i + 1];
@@ -654,13 +697,14 @@ SlosArgs make_args(const pcvl_slos_plan* p, int k) {
   a.cn = p->cn_d;
   a.cn_stride = p->cn_stride;
   a.ftail = p->ftail_d;
+  a.tocc = p->tocc_d;
   for (int r = 0; r <= p->n + 1; ++r) {
     a.tail_off[r] = p->tail_off[r];
     a.tstate_off[r] = p->tstate_off[r];
     a.tsize[r] = p->tsize[r];
   }
   // work units by class r = tail photons: batched -> (tile, kChunkB states); single
-  // circuit -> (tile, kChunk states) for tiles of >= 32 states, flat 32-state units below
+  // circuit -> (tile, kChunk states) for tiles of >= 32 states, 32 whole tiles below
   uint64_t u = 0;
   for (int r = 0; r <= k; ++r) {
     const uint64_t npf = fock_count(p->tail_p, k - r), S = p->tsize[r];
@@ -674,7 +718,7 @@ SlosArgs make_args(const pcvl_slos_plan* p, int k) {
       u += npf * a.cpt[r];
     } else {
       a.cpt[r] = 0;
-      u += (npf * S + 31) / 32;
+      u += (npf + 31) / 32;
     }
   }
   a.uoff[k + 1] = (uint32_t)u;
@@ -752,7 +796,8 @@ extern "C" int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int
   p->tail_p = m - t;
   std::vector<uint32_t> tp, tc;
   std::vector<dd> ftail;
-  tail_tables(t, n, tp, tc, ftail, p->tail_off, p->tstate_off, p->tsize);
+  std::vector<uint8_t> tocc;
+  tail_tables(t, n, tp, tc, ftail, tocc, p->tail_off, p->tstate_off, p->tsize);
   p->cn_stride = n + 2;
   std::vector<uint32_t> cn((size_t)(m + 1) * p->cn_stride);
   for (int M = 0; M <= m; ++M)
@@ -766,6 +811,8 @@ extern "C" int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int
   if ((rc = upload(p->tp_d, tp.data(), tp.size() * 4)) != PCVL_OK) goto fail;
   if ((rc = alloc((void**)&p->tc_d, tc.size() * 4, p->bytes)) != PCVL_OK) goto fail;
   if ((rc = upload(p->tc_d, tc.data(), tc.size() * 4)) != PCVL_OK) goto fail;
+  if ((rc = alloc((void**)&p->tocc_d, tocc.size(), p->bytes)) != PCVL_OK) goto fail;
+  if ((rc = upload(p->tocc_d, tocc.data(), tocc.size())) != PCVL_OK) goto fail;
   if ((rc = alloc((void**)&p->ftail_d, ftail.size() * sizeof(dd), p->bytes)) != PCVL_OK) goto fail;
   if ((rc = upload(p->ftail_d, ftail.data(), ftail.size() * sizeof(dd))) != PCVL_OK) goto fail;
   if ((rc = alloc((void**)&p->ucols_d, (size_t)m * m * B * sizeof(cdd), p->bytes)) != PCVL_OK) goto fail;
