@@ -362,6 +362,28 @@ def secondary(torch, _native, random_unitary, dev, flush):
                                     "forward_hbm_frac": fb / (t_f * 1e-3) / 1e9 / hbm}
     del plan
     torch.cuda.empty_cache()
+    # single large permanents spread over the whole chip (Haar submatrices of a 1024x1024
+    # unitary), Glynn and Ryser, with their relative difference
+    Ubig = random_unitary(1024, seed=0)
+    rng = np.random.default_rng(5)
+    for n in (32, 36):
+        a = np.ascontiguousarray(Ubig[np.ix_(rng.choice(1024, n, False), rng.choice(1024, n, False))])
+        ad = torch.from_numpy(a).to(dev)
+        o = torch.empty(1, dtype=torch.complex128, device=dev)
+        res_n = {}
+        for name, method in (("glynn", 0), ("ryser", 1)):
+            s0, e0 = torch.cuda.Event(True), torch.cuda.Event(True)
+            s0.record()
+            _native.permanent_batch(ad, np.array([0]), np.array([n]), o, method)
+            e0.record()
+            e0.synchronize()
+            res_n[name] = complex(o.cpu().item())
+            res_n[f"{name}_ms"] = s0.elapsed_time(e0)
+        res_n["glynn_tflops_fp64_equiv"] = glynn_flops(n) / (res_n["glynn_ms"] * 1e-3) / 1e12
+        res_n["glynn_ryser_rel_diff"] = abs(res_n["glynn"] - res_n["ryser"]) / abs(res_n["glynn"])
+        res_n["glynn"] = [res_n["glynn"].real, res_n["glynn"].imag]
+        res_n["ryser"] = [res_n["ryser"].real, res_n["ryser"].imag]
+        res[f"perm_single_n{n}"] = res_n
     # Clifford & Clifford, n=20, m=400
     U4 = torch.from_numpy(random_unitary(400, seed=0)).to(dev)
     cnt = 20000

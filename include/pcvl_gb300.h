@@ -125,6 +125,46 @@ int pcvl_cc2017_sample(const double* u_d, int32_t m, const int32_t* input_state_
                        uint64_t seed, uint64_t first_sample, int32_t precision,
                        int32_t* out_counts_d, void* stream);
 
+/* ------------------------------------------------------------------ learned proposal
+ * No counterpart in the reference (its samplers have no learned part).  Kernels of
+ * an autoregressive proposal network over output modes, trained on exact samples and
+ * used by a Metropolised independence sampler whose acceptance uses exact permanents
+ * (pcvl_permanent_batch).  bf16 arguments are __nv_bfloat16 arrays passed as void*.
+ *
+ * BF16 tensor-core GEMM with FP32 accumulation:
+ *   C[m * ldc + n] = alpha * sum_k A(m, k) B(n, k) + beta * C[m * ldc + n]  (+ epilogue)
+ *   A(m, k) = transA ? A[k * lda + m] : A[m * lda + k]
+ *   B(n, k) = transB ? B[k * ldb + n] : B[n * ldb + k]
+ * epilogue 0: none, 1: + bias[n], 2: + bias[n] then GELU (Cpre receives the value
+ * before GELU when not null).  C (f32) and/or Cb (bf16) receive the result. */
+int pcvl_gemm_bf16(const void* A, const void* B, int32_t M, int32_t N, int32_t K, int32_t lda, int32_t ldb,
+                   int32_t transA, int32_t transB, float alpha, float beta, const float* bias, int32_t epilogue,
+                   float* C, void* Cb, float* Cpre, int32_t ldc, void* stream);
+/* op 0: GELU backward, out = x * gelu'(y) (f32 out and/or bf16 out2); op 1: f32 x ->
+ * bf16 out.  n elements. */
+int pcvl_mlp_elementwise(int32_t op, const void* x, const void* y, int64_t n, void* out, void* out2, void* stream);
+/* out[n] = sum_m x[m * ld + n] for n < N (bias gradients). */
+int pcvl_colsum(const float* x, int32_t M, int32_t N, int32_t ld, float* out, void* stream);
+/* Row-wise log-softmax of R x N logits: log-probability of target[r] (logp_target),
+ * optional gradient (softmax - onehot) * scale (f32 grad and/or bf16 gradb), optional
+ * full log-probabilities (all_logp).  Rows with target < 0 get zero gradient. */
+int pcvl_softmax_xent(const float* logits, int32_t R, int32_t N, const int32_t* target, float scale,
+                      float* logp_target, float* grad, void* gradb, float* all_logp, void* stream);
+/* Network input rows: h = pos_emb[k] + sum_{l<k} mode_emb[seq[s * n + l]] (bf16, D
+ * columns), for every (s, k) (step < 0, row s * n + k) or for k = step (row s). */
+int pcvl_bag_embed(const int32_t* seq, int32_t S, int32_t n, int32_t step, const float* mode_emb,
+                   const float* pos_emb, int32_t D, void* h, void* stream);
+/* Gradients of the two embedding tables from dh (f32, rows s * n + k); accumulates. */
+int pcvl_bag_embed_backward(const int32_t* seq, int32_t S, int32_t n, const float* dh, int32_t D, float* dmode,
+                            float* dpos, void* stream);
+/* Adam step (bias-corrected, step >= 1) on f32 weights, refreshing a bf16 copy wb. */
+int pcvl_adam(float* w, const float* g, float* m1, float* m2, int64_t n, float lr, float b1, float b2, float eps,
+              int32_t step, void* wb, void* stream);
+/* One autoregressive draw for S chains from f32 logits (S x N): seq[s * n + step] and
+ * logq[s] += log-probability of the draw (Philox key seed, counter (chain0 + s, step)). */
+int pcvl_sample_step(const float* logits, int32_t S, int32_t N, int32_t step, uint64_t seed, uint64_t chain0,
+                     int32_t* seq, int32_t n, double* logq, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -37,6 +37,27 @@ SYMBOLS = {
     "pcvl_cc2017_sample": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64,
                                           ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p,
                                           ctypes.c_void_p]),
+    "pcvl_gemm_bf16": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int32] * 7 +
+                       [ctypes.c_float, ctypes.c_float, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
+    "pcvl_mlp_elementwise": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "pcvl_colsum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                   ctypes.c_void_p]),
+    "pcvl_softmax_xent": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                         ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_void_p]),
+    "pcvl_bag_embed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                      ctypes.c_void_p]),
+    "pcvl_bag_embed_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                               ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "pcvl_adam": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                 ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_int32,
+                                 ctypes.c_void_p, ctypes.c_void_p]),
+    "pcvl_sample_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                        ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_int32,
+                                        ctypes.c_void_p, ctypes.c_void_p]),
 }
 
 
@@ -215,3 +236,58 @@ def cc2017_sample(u: torch.Tensor, input_state, count: int, seed: int, first_sam
                                  int(first_sample), int(precision), out.data_ptr(), _stream_ptr(stream)),
           "pcvl_cc2017_sample")
     return out
+
+
+# ------------------------------------------------------------------ learned proposal kernels
+def _ptr(t):
+    return 0 if t is None else t.data_ptr()
+
+
+def gemm_bf16(A, B, M, N, K, lda, ldb, transA=0, transB=0, alpha=1.0, beta=0.0, bias=None, epilogue=0, C=None,
+              Cb=None, Cpre=None, ldc=None, stream=None):
+    """BF16 tensor-core GEMM with FP32 accumulation (see pcvl_gemm_bf16)."""
+    lib = load()
+    check(lib.pcvl_gemm_bf16(_ptr(A), _ptr(B), M, N, K, lda, ldb, transA, transB, alpha, beta, _ptr(bias),
+                             epilogue, _ptr(C), _ptr(Cb), _ptr(Cpre), N if ldc is None else ldc,
+                             _stream_ptr(stream)), "pcvl_gemm_bf16")
+
+
+def gelu_backward(dy, pre, out=None, outb=None, stream=None):
+    lib = load()
+    check(lib.pcvl_mlp_elementwise(0, _ptr(dy), _ptr(pre), dy.numel(), _ptr(out), _ptr(outb), _stream_ptr(stream)),
+          "pcvl_mlp_elementwise")
+
+
+def to_bf16(x, out, stream=None):
+    lib = load()
+    check(lib.pcvl_mlp_elementwise(1, _ptr(x), 0, x.numel(), _ptr(out), 0, _stream_ptr(stream)), "pcvl_mlp_elementwise")
+
+
+def colsum(x, M, N, ld, out, stream=None):
+    check(load().pcvl_colsum(_ptr(x), M, N, ld, _ptr(out), _stream_ptr(stream)), "pcvl_colsum")
+
+
+def softmax_xent(logits, R, N, target=None, scale=1.0, logp_target=None, grad=None, gradb=None, all_logp=None,
+                 stream=None):
+    check(load().pcvl_softmax_xent(_ptr(logits), R, N, _ptr(target), scale, _ptr(logp_target), _ptr(grad),
+                                   _ptr(gradb), _ptr(all_logp), _stream_ptr(stream)), "pcvl_softmax_xent")
+
+
+def bag_embed(seq, S, n, step, mode_emb, pos_emb, D, h, stream=None):
+    check(load().pcvl_bag_embed(_ptr(seq), S, n, step, _ptr(mode_emb), _ptr(pos_emb), D, _ptr(h),
+                                _stream_ptr(stream)), "pcvl_bag_embed")
+
+
+def bag_embed_backward(seq, S, n, dh, D, dmode, dpos, stream=None):
+    check(load().pcvl_bag_embed_backward(_ptr(seq), S, n, _ptr(dh), D, _ptr(dmode), _ptr(dpos), _stream_ptr(stream)),
+          "pcvl_bag_embed_backward")
+
+
+def adam(w, g, m1, m2, lr, b1, b2, eps, step, wb=None, stream=None):
+    check(load().pcvl_adam(_ptr(w), _ptr(g), _ptr(m1), _ptr(m2), w.numel(), lr, b1, b2, eps, step, _ptr(wb),
+                           _stream_ptr(stream)), "pcvl_adam")
+
+
+def sample_step(logits, S, N, step, seed, chain0, seq, n, logq, stream=None):
+    check(load().pcvl_sample_step(_ptr(logits), S, N, step, int(seed) & (2**64 - 1), int(chain0), _ptr(seq), n,
+                                  _ptr(logq), _stream_ptr(stream)), "pcvl_sample_step")

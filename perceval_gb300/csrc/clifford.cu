@@ -31,14 +31,15 @@
 namespace pcvl {
 
 // ------------------------------------------------------------ arithmetic policies
-struct ArDD {  // float-float (FP64-class)
+struct ArDD {  // float-float (FP64-class); products and sums stay unnormalised in the
+               // Glynn loop (bounded low parts, see cdd_mul_lazy), accumulators exact
   using C = cdd;
   using Acc = cdd;
   static __device__ __forceinline__ C zero() { return cdd_zero(); }
   static __device__ __forceinline__ C one() { return cdd_one(); }
-  static __device__ __forceinline__ C add(C a, C b) { return cdd_add(a, b); }
+  static __device__ __forceinline__ C add(C a, C b) { return cdd_add_lazy(a, b); }
   static __device__ __forceinline__ C sub(C a, C b) { return cdd_sub(a, b); }
-  static __device__ __forceinline__ C mul(C a, C b) { return cdd_mul(a, b); }
+  static __device__ __forceinline__ C mul(C a, C b) { return cdd_mul_lazy(a, b); }
   static __device__ __forceinline__ C neg(C a) { return cdd_neg(a); }
   static __device__ __forceinline__ C twice(C a) { return cdd_ldexp(a, 1); }
   static __device__ __forceinline__ C from(double2 v) { return cdd_from(v.x, v.y); }

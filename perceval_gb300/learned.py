@@ -1,0 +1,289 @@
+"""Learned-proposal Metropolised independence sampler for boson sampling.
+
+There is no counterpart in the reference; its exact sampler (Clifford & Clifford,
+perceval/backends/_clifford2017.py) is both the fallback and the judge here.
+
+Target.  For n photons in input modes ``in`` and a unitary U, an output *sequence*
+r = (r_1..r_n) of modes (one per photon, order kept) gets
+
+    pi(r) = |Perm(U[r, in])|^2 / n!
+
+so that the multiset of r has the boson-sampling probability |Perm|^2 / prod s!: every
+ordering of a multiset is equally likely.  The permanent is the exact float-float
+Glynn kernel (pcvl_permanent_batch).
+
+Proposal.  An autoregressive network q(r) = prod_k q(r_k | r_<k): the input row of
+step k is pos_emb[k] + sum_{l<k} mode_emb[r_l] (mode embedding dim D), followed by
+three GELU layers of width H and a linear map to logits over the m modes.  Weights
+are BF16 for the tensor-core GEMMs (pcvl_gemm_bf16, FP32 accumulation) with FP32
+master copies updated by Adam; every forward, backward and update step runs in this
+library's kernels.  The network is trained by maximum likelihood on exact samples
+of the GPU Clifford & Clifford sampler, each given a uniformly random photon order
+(a draw from pi).
+
+Sampler.  Proposals are independent of the chain state, so a batch of P proposals
+is drawn at once (network + pcvl_sample_step) and scored at once (P permanents);
+the accept/reject scan with acceptance min(1, pi(r') q(r) / (pi(r) q(r'))) runs on
+the host in FP64.  The stationary law is pi exactly, whatever the network.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _native
+
+BF16 = torch.bfloat16
+
+
+def _init(shape, fan_in, gen) -> torch.Tensor:
+    return (torch.randn(*shape, generator=gen, dtype=torch.float64) / math.sqrt(fan_in)).float()
+
+
+class ProposalMLP:
+    """Autoregressive proposal over output modes (see the module docstring)."""
+
+    def __init__(self, m: int, n: int, D: int = 128, H: int = 512, layers: int = 3, seed: int = 0):
+        _native.load()
+        self.m, self.n, self.D, self.H, self.L = m, n, D, H, layers
+        gen = torch.Generator().manual_seed(seed)
+        dev = torch.device("cuda")
+        self.mode_emb = (_init((m, D), 1.0, gen) * 0.1).to(dev)
+        self.pos_emb = (_init((n, D), 1.0, gen) * 0.1).to(dev)
+        dims = [D] + [H] * layers
+        self.W = [_init((dims[i + 1], dims[i]), dims[i], gen).to(dev) for i in range(layers)]
+        self.b = [torch.zeros(dims[i + 1], device=dev) for i in range(layers)]
+        self.Wo = _init((m, H), H, gen).to(dev) * 0.5
+        self.bo = torch.zeros(m, device=dev)
+        self.params = [self.mode_emb, self.pos_emb] + self.W + self.b + [self.Wo, self.bo]
+        self.Wb = [w.to(BF16) for w in self.W]
+        self.Wob = self.Wo.to(BF16)
+        self._adam = [(torch.zeros_like(p), torch.zeros_like(p)) for p in self.params]
+        self._step = 0
+
+    # ------------------------------------------------------------------ forward
+    def _forward_rows(self, h0b: torch.Tensor, R: int, keep: bool):
+        """Hidden stack and logits for R input rows (bf16 R x D)."""
+        acts_b, pres = [h0b], []
+        x = h0b
+        for i in range(self.L):
+            out_b = torch.empty(R, self.H, dtype=BF16, device="cuda")
+            pre = torch.empty(R, self.H, device="cuda") if keep else None
+            _native.gemm_bf16(x, self.Wb[i], R, self.H, x.shape[1], x.shape[1], x.shape[1], bias=self.b[i],
+                              epilogue=2, Cb=out_b, Cpre=pre)
+            acts_b.append(out_b)
+            pres.append(pre)
+            x = out_b
+        logits = torch.empty(R, self.m, device="cuda")
+        _native.gemm_bf16(x, self.Wob, R, self.m, self.H, self.H, self.H, bias=self.bo, epilogue=1, C=logits)
+        return logits, acts_b, pres
+
+    def logits(self, seq: torch.Tensor) -> torch.Tensor:
+        """Logits of every step of every sequence (S*n x m, row s*n + k)."""
+        S = seq.shape[0]
+        h0 = torch.empty(S * self.n, self.D, dtype=BF16, device="cuda")
+        _native.bag_embed(seq, S, self.n, -1, self.mode_emb, self.pos_emb, self.D, h0)
+        return self._forward_rows(h0, S * self.n, False)[0]
+
+    def log_q(self, seq: torch.Tensor) -> torch.Tensor:
+        """log q(r) of each sequence (float64, on the device)."""
+        S = seq.shape[0]
+        lg = self.logits(seq)
+        lp = torch.empty(S * self.n, device="cuda")
+        _native.softmax_xent(lg, S * self.n, self.m, target=seq.reshape(-1), logp_target=lp)
+        return lp.view(S, self.n).double().sum(dim=1)
+
+    # ------------------------------------------------------------------ training
+    def loss_and_grads(self, seq: torch.Tensor):
+        """Mean negative log-likelihood per photon and the gradient of every parameter."""
+        S, n, D, H, m = seq.shape[0], self.n, self.D, self.H, self.m
+        R = S * n
+        h0 = torch.empty(R, D, dtype=BF16, device="cuda")
+        _native.bag_embed(seq, S, n, -1, self.mode_emb, self.pos_emb, D, h0)
+        logits, acts_b, pres = self._forward_rows(h0, R, True)
+        lp = torch.empty(R, device="cuda")
+        dlog = torch.empty(R, m, device="cuda")
+        dlog_b = torch.empty(R, m, dtype=BF16, device="cuda")
+        _native.softmax_xent(logits, R, m, target=seq.reshape(-1), scale=1.0 / R, logp_target=lp, grad=dlog,
+                             gradb=dlog_b)
+        loss = -float(lp.double().mean())
+        grads = {}
+        # output layer
+        gWo = torch.empty(m, H, device="cuda")
+        _native.gemm_bf16(dlog_b, acts_b[-1], m, H, R, m, H, transA=1, transB=1, C=gWo)
+        gbo = torch.empty(m, device="cuda")
+        _native.colsum(dlog, R, m, m, gbo)
+        da = torch.empty(R, H, device="cuda")
+        _native.gemm_bf16(dlog_b, self.Wob, R, H, m, m, H, transB=1, C=da)
+        gW, gb = [None] * self.L, [None] * self.L
+        for i in range(self.L - 1, -1, -1):
+            dz = torch.empty(R, H, device="cuda")
+            dz_b = torch.empty(R, H, dtype=BF16, device="cuda")
+            _native.gelu_backward(da, pres[i], out=dz, outb=dz_b)
+            fan_in = acts_b[i].shape[1]
+            gW[i] = torch.empty(H, fan_in, device="cuda")
+            _native.gemm_bf16(dz_b, acts_b[i], H, fan_in, R, H, fan_in, transA=1, transB=1, C=gW[i])
+            gb[i] = torch.empty(H, device="cuda")
+            _native.colsum(dz, R, H, H, gb[i])
+            da = torch.empty(R, fan_in, device="cuda")
+            _native.gemm_bf16(dz_b, self.Wb[i], R, fan_in, H, H, fan_in, transB=1, C=da)
+        gmode = torch.zeros_like(self.mode_emb)
+        gpos = torch.zeros_like(self.pos_emb)
+        _native.bag_embed_backward(seq, S, n, da, D, gmode, gpos)
+        return loss, [gmode, gpos] + gW + gb + [gWo, gbo]
+
+    def adam_step(self, grads, lr: float = 1e-3, b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8):
+        self._step += 1
+        bf = [None, None] + self.Wb + [None] * self.L + [self.Wob, None]
+        for p, g, (m1, m2), wb in zip(self.params, grads, self._adam, bf):
+            _native.adam(p, g, m1, m2, lr, b1, b2, eps, self._step, wb)
+
+    def train(self, samples: np.ndarray, epochs: int = 5, batch: int = 256, lr: float = 1e-3, seed: int = 0,
+              log=None) -> list[float]:
+        """Maximum likelihood on sequences made from output samples (counts per mode),
+        each photon order drawn uniformly at random."""
+        rng = np.random.default_rng(seed)
+        seqs = counts_to_sequences(samples, rng)
+        losses = []
+        for ep in range(epochs):
+            order = rng.permutation(len(seqs))
+            tot, cnt = 0.0, 0
+            for i in range(0, len(seqs), batch):
+                idx = order[i:i + batch]
+                # fresh random photon order every epoch (the target is order-symmetric)
+                sb = np.stack([rng.permutation(seqs[j]) for j in idx]).astype(np.int32)
+                loss, grads = self.loss_and_grads(torch.from_numpy(sb).cuda())
+                self.adam_step(grads, lr=lr)
+                tot += loss * len(idx)
+                cnt += len(idx)
+            losses.append(tot / cnt)
+            if log:
+                log(f"epoch {ep}: nll/photon {losses[-1]:.4f}")
+        return losses
+
+    # ------------------------------------------------------------------ sampling
+    def sample(self, S: int, seed: int, chain0: int = 0) -> tuple[torch.Tensor, torch.Tensor]:
+        """S sequences from q and their log q (float64), all on the device."""
+        seq = torch.zeros(S, self.n, dtype=torch.int32, device="cuda")
+        logq = torch.zeros(S, dtype=torch.float64, device="cuda")
+        h0 = torch.empty(S, self.D, dtype=BF16, device="cuda")
+        for k in range(self.n):
+            _native.bag_embed(seq, S, self.n, k, self.mode_emb, self.pos_emb, self.D, h0)
+            lg = self._forward_rows(h0, S, False)[0]
+            _native.sample_step(lg, S, self.m, k, seed, chain0, seq, self.n, logq)
+        return seq, logq
+
+
+def counts_to_sequences(samples: np.ndarray, rng: np.random.Generator) -> list[np.ndarray]:
+    """Output counts (N x m) -> mode sequences with a uniformly random photon order."""
+    out = []
+    for row in np.asarray(samples):
+        s = np.repeat(np.arange(len(row)), row)
+        out.append(rng.permutation(s))
+    return out
+
+
+def sequences_to_counts(seq: np.ndarray, m: int) -> np.ndarray:
+    seq = np.asarray(seq)
+    out = np.zeros((seq.shape[0], m), dtype=np.int32)
+    for i, s in enumerate(seq):
+        np.add.at(out[i], s, 1)
+    return out
+
+
+def log_abs_perm2(U_dev: torch.Tensor, cols: np.ndarray, seq: torch.Tensor) -> np.ndarray:
+    """log |Perm(U[seq_s, cols])|^2 for every sequence (exact float-float permanents)."""
+    S, n = seq.shape
+    colsd = torch.as_tensor(cols, dtype=torch.long, device=U_dev.device)
+    mats = U_dev[seq.long()][:, :, colsd].contiguous()  # S x n x n
+    out = torch.empty(S, dtype=torch.complex128, device=U_dev.device)
+    _native.permanent_batch(mats.view(-1), np.arange(S, dtype=np.int64) * n * n, np.full(S, n, np.int32), out)
+    a = out.abs().cpu().numpy()
+    with np.errstate(divide="ignore"):
+        return 2.0 * np.log(a)
+
+
+@dataclass
+class MISResult:
+    samples: np.ndarray            # chain states (counts), chains x steps x m
+    accept_rate: float
+    proposals: int
+    seconds: float
+    log_pi: np.ndarray = field(default_factory=lambda: np.zeros(0))
+
+
+def run_mis(proposal: ProposalMLP, U: np.ndarray, input_state, chains: int, steps: int, seed: int = 0,
+            batch: int = 512) -> MISResult:
+    """Independent-proposal Metropolis-Hastings chains targeting pi (exact law)."""
+    import time
+    m = U.shape[0]
+    cols = np.repeat(np.arange(m), np.asarray(input_state))
+    U_dev = torch.from_numpy(np.ascontiguousarray(U)).cuda()
+    total = chains * (steps + 1)
+    rng = np.random.default_rng(seed)
+    t0 = time.perf_counter()
+    seqs, logq, logpi = [], [], []
+    for start in range(0, total, batch):
+        cnt = min(batch, total - start)
+        s, lq = proposal.sample(cnt, seed, chain0=start)
+        seqs.append(s.cpu().numpy())
+        logq.append(lq.cpu().numpy())
+        logpi.append(log_abs_perm2(U_dev, cols, s))
+    torch.cuda.synchronize()
+    seq = np.concatenate(seqs).reshape(chains, steps + 1, -1)
+    lq = np.concatenate(logq).reshape(chains, steps + 1)
+    lp = np.concatenate(logpi).reshape(chains, steps + 1)
+    states = np.empty((chains, steps, seq.shape[2]), dtype=np.int32)
+    state_lp = np.empty((chains, steps))
+    accepted = 0
+    for c in range(chains):
+        cur, cur_lw = seq[c, 0], lp[c, 0] - lq[c, 0]
+        for t in range(steps):
+            prop_lw = lp[c, t + 1] - lq[c, t + 1]
+            if np.log(rng.random()) < prop_lw - cur_lw:
+                cur, cur_lw = seq[c, t + 1], prop_lw
+                accepted += 1
+            states[c, t] = cur
+            state_lp[c, t] = cur_lw
+    secs = time.perf_counter() - t0
+    counts = np.stack([sequences_to_counts(states[c], m) for c in range(chains)])
+    return MISResult(counts, accepted / (chains * steps), total, secs, state_lp)
+
+
+def ess(x: np.ndarray) -> float:
+    """Effective sample size of one chain's scalar series (Geyer's initial positive
+    sequence estimator of the integrated autocorrelation time)."""
+    x = np.asarray(x, dtype=np.float64)
+    N = len(x)
+    if N < 4 or np.var(x) == 0:
+        return float(N)
+    xc = x - x.mean()
+    f = np.fft.rfft(xc, n=2 * N)
+    acf = np.fft.irfft(f * np.conj(f))[:N] / (np.arange(N, 0, -1))
+    acf /= acf[0]
+    tau = 1.0
+    for t in range(1, N - 1, 2):
+        pair = acf[t] + acf[t + 1]
+        if pair <= 0:
+            break
+        tau += 2 * pair
+    return N / tau
+
+
+def exact_moments(U: np.ndarray, input_state) -> tuple[np.ndarray, np.ndarray]:
+    """Exact E[n_i] and E[n_i n_j] of the output occupations for single-photon inputs:
+    E[n_i] = A_i = sum_k |U_ik|^2 and, for i != j,
+    E[n_i n_j] = A_i A_j + |sum_k conj(U_ik) U_jk|^2 - 2 sum_k |U_ik|^2 |U_jk|^2,
+    E[n_i^2]  = A_i + 2 A_i^2 - 2 sum_k |U_ik|^4   (sums over occupied input modes k)."""
+    inp = np.asarray(input_state)
+    assert inp.max() <= 1, "closed forms are for single-photon inputs"
+    V = np.asarray(U)[:, inp == 1]
+    P = np.abs(V) ** 2
+    A = P.sum(axis=1)
+    G = V.conj() @ V.T
+    E2 = np.outer(A, A) + np.abs(G) ** 2 - 2 * (P @ P.T)
+    np.fill_diagonal(E2, A + 2 * A ** 2 - 2 * (P ** 2).sum(axis=1))
+    return A, E2

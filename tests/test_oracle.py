@@ -159,3 +159,41 @@ def test_philox_known_answer(oracle):
     # philox4x32-10: counter 0 / key 0, and counter all-ones / key all-ones.
     assert oracle.philox((0, 0, 0, 0), (0, 0)) == (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)
     assert oracle.philox((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2) == (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)
+
+
+def test_mlp_reference_gradient_finite_differences():
+    # the float64 restatement of the proposal network, checked by central differences
+    # (bf16 rounding switched off so the function is smooth)
+    from oracle import mlp_ref
+    rng = np.random.default_rng(0)
+    m, n, D, H = 7, 3, 5, 6
+    params = {"mode_emb": rng.normal(size=(m, D)), "pos_emb": rng.normal(size=(n, D)),
+              "W": [rng.normal(size=(H, D)) / 2, rng.normal(size=(H, H)) / 2, rng.normal(size=(H, H)) / 2],
+              "b": [rng.normal(size=H) * 0.1 for _ in range(3)], "Wo": rng.normal(size=(m, H)) / 2,
+              "bo": rng.normal(size=m) * 0.1}
+    seq = rng.integers(0, m, size=(4, n))
+    saved = mlp_ref.bf16
+    mlp_ref.bf16 = lambda x: np.asarray(x, dtype=np.float64)
+    try:
+        _, g = mlp_ref.forward_backward(params, seq)
+        h = 1e-6
+        for key, idx in (("Wo", (2, 3)), ("bo", (4,)), ("mode_emb", (1, 2)), ("pos_emb", (2, 1))):
+            p = params[key]
+            old = p[idx]
+            p[idx] = old + h
+            lp, _ = mlp_ref.forward_backward(params, seq)
+            p[idx] = old - h
+            lm, _ = mlp_ref.forward_backward(params, seq)
+            p[idx] = old
+            assert (lp - lm) / (2 * h) == pytest.approx(g[key][idx], rel=1e-5, abs=1e-8)
+        for i in range(3):
+            W = params["W"][i]
+            old = W[1, 2]
+            W[1, 2] = old + h
+            lp, _ = mlp_ref.forward_backward(params, seq)
+            W[1, 2] = old - h
+            lm, _ = mlp_ref.forward_backward(params, seq)
+            W[1, 2] = old
+            assert (lp - lm) / (2 * h) == pytest.approx(g["W"][i][1, 2], rel=1e-5, abs=1e-8)
+    finally:
+        mlp_ref.bf16 = saved
