@@ -414,6 +414,60 @@ def secondary(torch, _native, random_unitary, dev, flush):
     return res
 
 
+def run_learned(args):
+    """Learned-proposal Metropolised sampler vs the plain GPU exact sampler at
+    n = 30, m = 900 (Haar seed 0, input modes 0..29), plus the n = 8, m = 64 companion.
+
+    Training data: exact Clifford & Clifford samples drawn by this library's sampler in
+    its FP32 mode (the float-float mode is the judged baseline).  ESS: Geyer's initial
+    positive sequence estimator on each chain's log pi trace, summed over chains; the
+    exact sampler's samples are independent (ESS = N).  Marginals: sample means of n_i
+    and n_i n_j against the closed forms."""
+    import torch
+    from perceval_gb300 import _native
+    from perceval_gb300.learned import ProposalMLP, ess, exact_moments, run_mis
+    from perceval_gb300.utils.matrix import random_unitary
+    _native.load()
+    out = {}
+    for (m, n, n_train, epochs, chains, steps, n_ref) in ((900, 30, args.learned_train, 6, 16, 32, 152),
+                                                           (64, 8, 20000, 10, 64, 400, 25600)):
+        U = random_unitary(m, seed=0)
+        inp = [1] * n + [0] * (m - n)
+        Ud = torch.from_numpy(U).cuda()
+        # exact training samples (FP32 sampler)
+        t0 = time.perf_counter()
+        train = _native.cc2017_sample(Ud, inp, n_train, seed=101, precision=1).cpu().numpy()
+        t_train_samples = time.perf_counter() - t0
+        net = ProposalMLP(m, n, D=128, H=512, layers=3, seed=0)
+        t0 = time.perf_counter()
+        losses = net.train(train, epochs=epochs, batch=256, lr=1e-3)
+        torch.cuda.synchronize()
+        t_fit = time.perf_counter() - t0
+        # Metropolised independence sampler (proposal sampling + exact permanents + scan)
+        res = run_mis(net, U, inp, chains=chains, steps=steps, seed=7, batch=512)
+        ess_mis = float(sum(ess(x) for x in res.log_pi))
+        # plain exact sampler (float-float), same unitary
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ref = _native.cc2017_sample(Ud, inp, n_ref, seed=202, precision=0).cpu().numpy()
+        t_ref = time.perf_counter() - t0
+        A, E2 = exact_moments(U, inp)
+        st = res.samples.reshape(-1, m).astype(np.float64)
+        refs = ref.astype(np.float64)
+        row = {"m": m, "n": n, "train_samples": n_train, "train_sampling_s": t_train_samples,
+               "fit_s": t_fit, "nll_first_last": [losses[0], losses[-1]],
+               "mis": {"chains": chains, "steps": steps, "proposals": res.proposals, "seconds": res.seconds,
+                       "accept_rate": res.accept_rate, "ess": ess_mis, "ess_per_s": ess_mis / res.seconds,
+                       "max_abs_err_E_n": float(np.abs(st.mean(0) - A).max()),
+                       "max_abs_err_E_nn": float(np.abs(st.T @ st / len(st) - E2).max())},
+               "exact_sampler": {"samples": n_ref, "seconds": t_ref, "ess_per_s": n_ref / t_ref,
+                                 "max_abs_err_E_n": float(np.abs(refs.mean(0) - A).max()),
+                                 "max_abs_err_E_nn": float(np.abs(refs.T @ refs / len(refs) - E2).max())}}
+        row["ess_per_s_ratio"] = row["mis"]["ess_per_s"] / row["exact_sampler"]["ess_per_s"]
+        out[f"n{n}_m{m}"] = row
+    print(json.dumps({"learned_proposal": out}), flush=True)
+
+
 def profile_case(name: str):
     """One untimed run of a single hot kernel on a small case, for ncu captures."""
     import torch
@@ -455,11 +509,16 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--skip-secondary", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--learned", action="store_true",
+                    help="run the learned-proposal sampler workload (n=30, m=900 and n=8, m=64) and exit")
+    ap.add_argument("--learned-train", type=int, default=2048, help="exact training samples at n=30")
     ap.add_argument("--profile-case", choices=["perm24", "slos20", "slos16b256", "cc2017"],
                     help="run one small untimed case of a single kernel (for ncu) and exit")
     args = ap.parse_args()
     if args.profile_case:
         profile_case(args.profile_case)
+    elif args.learned:
+        run_learned(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -22,6 +22,7 @@
 // lo bits (a shared table of column-sum parts, as in the permanent kernel) and hi
 // bits spread over the threads; each thread keeps its k accumulators in shared memory.
 #include <algorithm>
+#include <climits>
 #include <cstring>
 #include <vector>
 
@@ -51,6 +52,8 @@ struct ArDD {  // float-float (FP64-class); products and sums stay unnormalised 
     const dd r = dd_add(dd_mul(a.re, a.re), dd_mul(a.im, a.im));
     return dd_to_double(r);
   }
+  static __device__ __forceinline__ C scale(C a, int e) { return cdd_ldexp(a, e); }
+  static __device__ __forceinline__ float mag(C a) { return fabsf(a.re.hi) + fabsf(a.im.hi); }
 };
 
 struct f4 {
@@ -91,6 +94,8 @@ struct ArF32 {  // FP32 with compensated accumulation
   static __device__ __forceinline__ double norm2(C a) {
     return (double)a.x * (double)a.x + (double)a.y * (double)a.y;
   }
+  static __device__ __forceinline__ C scale(C a, int e) { return make_float2(ldexpf(a.x, e), ldexpf(a.y, e)); }
+  static __device__ __forceinline__ float mag(C a) { return fabsf(a.x) + fabsf(a.y); }
 };
 
 struct CCArgs {
@@ -131,6 +136,8 @@ __global__ void __launch_bounds__(kCCThreads) cc2017_kernel(CCArgs a) {
   double* w = reinterpret_cast<double*>(accs + KMAX * kCCThreads);  // m
   int* cols = reinterpret_cast<int*>(w + m);                 // KMAX
   int* rows = cols + KMAX;                                   // KMAX
+  int* cexp = rows + KMAX;                                   // KMAX column exponents
+  int* sexp = cexp + KMAX;                                   // KMAX sub-permanent exponents
   const C* U = reinterpret_cast<const C*>(a.uc);
 
   for (int64_t s = blockIdx.x; s < a.count; s += gridDim.x) {
@@ -161,6 +168,22 @@ __global__ void __launch_bounds__(kCCThreads) cc2017_kernel(CCArgs a) {
         const int F = d - 1;  // free sign bits (row 0 fixed to +1)
         const int L = min(LMAX, max(0, F - 7));
         const int Hb = F - L;
+        __syncthreads();
+        // Scale column c by 2^e_c so that its l1 norm lies in [2^(c0-1), 2^c0) with
+        // (k - 1) c0 + (k - 2) <= 120: every product of k - 1 column sums times the
+        // 2^(k-2) terms of the sum stays inside the FP32 range (a global scaling of U
+        // does not: aligned columns reach 1e56 at n = 30).  Exact (powers of two);
+        // undone below through the sub-permanent exponents.
+        if (tid < k) {
+          float l1 = 0.f;
+          for (int r = 0; r < d; ++r) l1 += Ar::mag(Bm[r * KMAX + tid]);
+          const int c0 = min(4, (120 - (k - 2)) / (k - 1));
+          int ex = 0;
+          if (l1 > 0.f) frexpf(l1, &ex);
+          const int e = l1 > 0.f ? c0 - ex : 0;
+          cexp[tid] = e;
+          for (int r = 0; r < d; ++r) Bm[r * KMAX + tid] = Ar::scale(Bm[r * KMAX + tid], e);
+        }
         __syncthreads();
         // lo table over rows 1..L
         for (int c = tid; c < k; c += blockDim.x) {
@@ -219,6 +242,19 @@ __global__ void __launch_bounds__(kCCThreads) cc2017_kernel(CCArgs a) {
           Acc tot = accs[l * kCCThreads];
           for (int t = 1; t < kCCThreads; ++t) tot = Ar::acc_merge(tot, accs[l * kCCThreads + t]);
           sub[l] = Ar::acc_value(tot);
+          // true sub_l is proportional to sub_l * 2^{e_l} (the scales of the other
+          // columns are common to all l); record its binary exponent
+          const float mg = Ar::mag(sub[l]);
+          int ex = 0;
+          if (mg > 0.f) frexpf(mg, &ex);
+          sexp[l] = mg > 0.f ? ex + cexp[l] : INT_MIN;
+        }
+        __syncthreads();
+        if (tid < k) {
+          int emax = INT_MIN;
+          for (int l = 0; l < k; ++l) emax = max(emax, sexp[l]);
+          // largest |sub_l| near 1: the weights below cannot overflow
+          sub[tid] = sexp[tid] == INT_MIN ? Ar::zero() : Ar::scale(sub[tid], cexp[tid] - emax);
         }
         __syncthreads();
       }
@@ -262,7 +298,7 @@ static size_t cc_smem(int m) {
   using C = typename Ar::C;
   size_t b = sizeof(C) * (KMAX * KMAX + (1 << 6) * KMAX + KMAX);
   b += sizeof(typename Ar::Acc) * KMAX * kCCThreads;
-  b += sizeof(double) * m + sizeof(int) * 2 * KMAX;
+  b += sizeof(double) * m + sizeof(int) * 4 * KMAX;
   return b;
 }
 

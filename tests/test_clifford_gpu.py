@@ -65,3 +65,27 @@ def test_larger_n_marginals(native):
     z = (mean - exact) / np.sqrt(exact / N + 1e-12)
     assert np.abs(z).max() < 6
     assert abs(mean.sum() - n) < 1e-9
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_n26_marginals_and_precision_agreement(native, precision):
+    # n = 26 on m = 676: Glynn sums of 2^24 column-sum products reach 1e21 with only a
+    # global scaling of U, and their squares leave the FP32 range; the per-column and
+    # per-step power-of-two normalisation keeps every weight finite.  One-mode marginals
+    # must match E[n_i] = sum_k |U_ik|^2 (6 sigma, Var n_i <= A_i (1 + A_i)).
+    m, n = 676, 26
+    U = random_unitary(m, seed=26)
+    inp = (1,) * n + (0,) * (m - n)
+    N = 304
+    Ud = torch.from_numpy(U).cuda()
+    got = native.cc2017_sample(Ud, inp, N, seed=3, precision=precision).cpu().numpy()
+    assert np.all(got.sum(axis=1) == n)
+    A = (np.abs(U[:, :n]) ** 2).sum(axis=1)
+    z = (got.mean(axis=0) - A) / np.sqrt(A * (1 + A) / N)
+    assert np.abs(z).max() < 6, np.abs(z).max()
+    if precision == 1:
+        # same Philox stream: FP32 and float-float pick the same rows unless a draw lands
+        # within the FP32 error of a CDF boundary
+        ref = native.cc2017_sample(Ud, inp, N, seed=3, precision=0).cpu().numpy()
+        agree = np.all(got == ref, axis=1).mean()
+        assert agree >= 0.8, agree
