@@ -8,19 +8,28 @@
 //   2. for k = 1..n, with rows r_0..r_{k-2} drawn so far and B = U[rows, cols[0..k-1]]
 //      ((k-1) x k), compute all k sub-permanents
 //          sub_l = Per(B without column l)
-//      (Glynn over the k-1 row signs, all l at once through prefix/suffix products of
+//      (Glynn over the k-1 row signs, all l at once through leave-one-out products of
 //      the column sums), weigh every output mode i by
 //          w_i = |sum_l U[i, cols[l]] sub_l|^2
 //      (Laplace expansion of the k x k permanent along the new row), and draw r_{k-1}
 //      with probability w_i / sum w (uniform from Philox counter (sample, k, 0); the
 //      first i whose running sum exceeds u * sum w, summed in index order);
 //   3. the sample is the histogram of the rows.
-// The common factor 2^{2-k} of the Glynn sums and a power-of-two scaling of U cancel
-// in the normalisation and are dropped.
+// Common factors of the sub-permanents (the Glynn 2^{2-k}, power-of-two column scales)
+// cancel in the normalisation and are dropped.
 //
-// One CTA per sample (grid-stride).  Step k splits the 2^{k-2} sign patterns into
-// lo bits (a shared table of column-sum parts, as in the permanent kernel) and hi
-// bits spread over the threads; each thread keeps its k accumulators in shared memory.
+// GPU organisation: a wavefront over photons.  Up to kWave samples are in flight and,
+// for every photon k, two kernels run over all of them:
+//   cc_sub_kernel   the k sub-permanents of every sample.  The 2^{k-2} sign patterns are
+//                   split into lo bits (a shared-memory table of column-sum parts) and
+//                   hi bits spread over lane groups and CTAs.  Four lanes share one
+//                   pattern and each owns K/4 columns: its suffix products and the
+//                   accumulators of its columns stay in registers, and the products of
+//                   the other lanes' columns come from a two-step shuffle butterfly.
+//                   One partial sum per (sample, chunk of hi patterns) goes to memory.
+//   cc_draw_kernel  one CTA per sample: adds the chunk partials, undoes the column
+//                   scaling, forms w_i in FP64 for every mode, and a block scan over
+//                   the modes locates the draw.
 #include <algorithm>
 #include <climits>
 #include <cstring>
@@ -31,47 +40,75 @@
 
 namespace pcvl {
 
+__device__ __forceinline__ float shx(float v, int mask) { return __shfl_xor_sync(0xffffffffu, v, mask); }
+
 // ------------------------------------------------------------ arithmetic policies
-struct ArDD {  // float-float (FP64-class); products and sums stay unnormalised in the
-               // Glynn loop (bounded low parts, see cdd_mul_lazy), accumulators exact
+struct ArDD {  // float-float (FP64-class): lazy products and sums in the pattern loop,
+               // exact two_sum accumulation of the high parts
   using C = cdd;
-  using Acc = cdd;
+  struct Acc {
+    float rh, rl, ih, il;
+  };
   static __device__ __forceinline__ C zero() { return cdd_zero(); }
   static __device__ __forceinline__ C one() { return cdd_one(); }
   static __device__ __forceinline__ C add(C a, C b) { return cdd_add_lazy(a, b); }
-  static __device__ __forceinline__ C sub(C a, C b) { return cdd_sub(a, b); }
+  static __device__ __forceinline__ C add_n(C a, C b) { return cdd_add(a, b); }
+  static __device__ __forceinline__ C sub_n(C a, C b) { return cdd_sub(a, b); }
   static __device__ __forceinline__ C mul(C a, C b) { return cdd_mul_lazy(a, b); }
   static __device__ __forceinline__ C neg(C a) { return cdd_neg(a); }
   static __device__ __forceinline__ C twice(C a) { return cdd_ldexp(a, 1); }
   static __device__ __forceinline__ C from(double2 v) { return cdd_from(v.x, v.y); }
-  static __device__ __forceinline__ Acc acc_zero() { return cdd_zero(); }
-  static __device__ __forceinline__ void acc_add(Acc& a, C x) { a = cdd_add(a, x); }
-  static __device__ __forceinline__ Acc acc_merge(Acc a, Acc b) { return cdd_add(a, b); }
-  static __device__ __forceinline__ C acc_value(Acc a) { return a; }
-  static __device__ __forceinline__ double norm2(C a) {
-    const dd r = dd_add(dd_mul(a.re, a.re), dd_mul(a.im, a.im));
-    return dd_to_double(r);
-  }
   static __device__ __forceinline__ C scale(C a, int e) { return cdd_ldexp(a, e); }
   static __device__ __forceinline__ float mag(C a) { return fabsf(a.re.hi) + fabsf(a.im.hi); }
+  static __device__ __forceinline__ C shfl(C v, int mask) {
+    return {{shx(v.re.hi, mask), shx(v.re.lo, mask)}, {shx(v.im.hi, mask), shx(v.im.lo, mask)}};
+  }
+  static __device__ __forceinline__ Acc acc_zero() { return {0.f, 0.f, 0.f, 0.f}; }
+  static __device__ __forceinline__ void acc_add(Acc& a, C x) {
+    const dd r = two_sum(a.rh, x.re.hi);
+    const dd i = two_sum(a.ih, x.im.hi);
+    a.rh = r.hi;
+    a.rl += r.lo + x.re.lo;
+    a.ih = i.hi;
+    a.il += i.lo + x.im.lo;
+  }
+  static __device__ __forceinline__ void acc_fold(Acc& a) {
+    const dd r = two_sum(a.rh, a.rl);
+    const dd i = two_sum(a.ih, a.il);
+    a = {r.hi, r.lo, i.hi, i.lo};
+  }
+  static __device__ __forceinline__ Acc acc_merge(Acc a, Acc b) {
+    const dd r = dd_add({a.rh, a.rl}, {b.rh, b.rl});
+    const dd i = dd_add({a.ih, a.il}, {b.ih, b.il});
+    return {r.hi, r.lo, i.hi, i.lo};
+  }
+  static __device__ __forceinline__ Acc acc_shfl(Acc v, int mask) {
+    return {shx(v.rh, mask), shx(v.rl, mask), shx(v.ih, mask), shx(v.il, mask)};
+  }
+  static __device__ __forceinline__ double2 acc_value(Acc a) {
+    return make_double2((double)a.rh + (double)a.rl, (double)a.ih + (double)a.il);
+  }
 };
 
-struct f4 {
-  float sr, cr, si, ci;  // Kahan-compensated complex: sum and compensation
-};
-struct ArF32 {  // FP32 with compensated accumulation
+struct ArF32 {  // FP32 with Kahan-compensated accumulation
   using C = float2;
-  using Acc = f4;
+  struct Acc {
+    float sr, cr, si, ci;  // sums and compensations
+  };
   static __device__ __forceinline__ C zero() { return make_float2(0.f, 0.f); }
   static __device__ __forceinline__ C one() { return make_float2(1.f, 0.f); }
   static __device__ __forceinline__ C add(C a, C b) { return make_float2(a.x + b.x, a.y + b.y); }
-  static __device__ __forceinline__ C sub(C a, C b) { return make_float2(a.x - b.x, a.y - b.y); }
+  static __device__ __forceinline__ C add_n(C a, C b) { return add(a, b); }
+  static __device__ __forceinline__ C sub_n(C a, C b) { return make_float2(a.x - b.x, a.y - b.y); }
   static __device__ __forceinline__ C mul(C a, C b) {
     return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
   }
   static __device__ __forceinline__ C neg(C a) { return make_float2(-a.x, -a.y); }
   static __device__ __forceinline__ C twice(C a) { return make_float2(2.f * a.x, 2.f * a.y); }
   static __device__ __forceinline__ C from(double2 v) { return make_float2((float)v.x, (float)v.y); }
+  static __device__ __forceinline__ C scale(C a, int e) { return make_float2(ldexpf(a.x, e), ldexpf(a.y, e)); }
+  static __device__ __forceinline__ float mag(C a) { return fabsf(a.x) + fabsf(a.y); }
+  static __device__ __forceinline__ C shfl(C v, int mask) { return make_float2(shx(v.x, mask), shx(v.y, mask)); }
   static __device__ __forceinline__ Acc acc_zero() { return {0.f, 0.f, 0.f, 0.f}; }
   static __device__ __forceinline__ void kahan(float& s, float& c, float x) {
     const float y = x - c;
@@ -83,6 +120,7 @@ struct ArF32 {  // FP32 with compensated accumulation
     kahan(a.sr, a.cr, x.x);
     kahan(a.si, a.ci, x.y);
   }
+  static __device__ __forceinline__ void acc_fold(Acc&) {}
   static __device__ __forceinline__ Acc acc_merge(Acc a, Acc b) {
     kahan(a.sr, a.cr, b.sr);
     kahan(a.sr, a.cr, -b.cr);
@@ -90,238 +128,385 @@ struct ArF32 {  // FP32 with compensated accumulation
     kahan(a.si, a.ci, -b.ci);
     return a;
   }
-  static __device__ __forceinline__ C acc_value(Acc a) { return make_float2(a.sr - a.cr, a.si - a.ci); }
-  static __device__ __forceinline__ double norm2(C a) {
-    return (double)a.x * (double)a.x + (double)a.y * (double)a.y;
+  static __device__ __forceinline__ Acc acc_shfl(Acc v, int mask) {
+    return {shx(v.sr, mask), shx(v.cr, mask), shx(v.si, mask), shx(v.ci, mask)};
   }
-  static __device__ __forceinline__ C scale(C a, int e) { return make_float2(ldexpf(a.x, e), ldexpf(a.y, e)); }
-  static __device__ __forceinline__ float mag(C a) { return fabsf(a.x) + fabsf(a.y); }
-};
-
-struct CCArgs {
-  const void* uc;        // converted, scaled U (Ar::C), row-major m x m
-  int m, n;
-  const int32_t* cols0;  // input columns (n entries, ascending)
-  int64_t count;
-  uint32_t k0, k1;       // Philox key (seed)
-  uint64_t first;
-  int32_t* out;          // count x m
+  static __device__ __forceinline__ double2 acc_value(Acc a) {
+    return make_double2((double)a.sr - (double)a.cr, (double)a.si - (double)a.ci);
+  }
 };
 
 constexpr int kCCThreads = 128;
+constexpr int kMaxPhotons = 32;
 
 template <class Ar>
-__global__ void cc_convert(const double2* __restrict__ u, int m, double scale, typename Ar::C* __restrict__ uc) {
+__global__ void cc_convert(const double2* __restrict__ u, int m, typename Ar::C* __restrict__ uc) {
   const int tot = m * m;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += gridDim.x * blockDim.x) {
-    double2 v = u[i];
-    v.x *= scale;
-    v.y *= scale;
-    uc[i] = Ar::from(v);
-  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += gridDim.x * blockDim.x) uc[i] = Ar::from(u[i]);
 }
 
-template <class Ar, int KMAX>
-__global__ void __launch_bounds__(kCCThreads) cc2017_kernel(CCArgs a) {
+// ------------------------------------------------------------ sub-permanents
+struct CCSubArgs {
+  const void* uc;         // U converted to Ar::C, row-major m x m
+  int m, k, L, Hb, chunks;
+  int64_t nsamp;          // samples in the wavefront
+  const int32_t* cols;    // [nsamp][32] shuffled input columns
+  const int32_t* rows;    // [nsamp][32] rows drawn so far
+  int32_t* cexp;          // [nsamp][32] column exponents (written by chunk 0)
+  double2* partials;      // [nsamp][chunks][K]
+};
+
+// K padded columns (K / 4 per lane), TW warps per sample team (1: four samples per
+// CTA, lo table of <= 16 patterns; 4: the CTA works on one sample, 64 lo patterns).
+template <class Ar, int K, int TW>
+struct SubCfg {
+  static constexpr int Q = K / 4;
+  static constexpr int TEAMS = 4 / TW;
+  static constexpr int LMAX = TW == 1 ? 4 : 6;
+  static constexpr size_t c_elems = (size_t)K * K + (size_t)(1 << LMAX) * K;
+  static constexpr size_t team_bytes = c_elems * sizeof(typename Ar::C) + (size_t)TW * K * sizeof(typename Ar::Acc);
+  static constexpr size_t smem = TEAMS * team_bytes;
+};
+
+template <int TW>
+__device__ __forceinline__ void team_sync() {
+  if constexpr (TW == 1)
+    __syncwarp();
+  else
+    __syncthreads();
+}
+
+template <class Ar, int K, int TW>
+__global__ void __launch_bounds__(kCCThreads) cc_sub_kernel(CCSubArgs a) {
   using C = typename Ar::C;
   using Acc = typename Ar::Acc;
+  using Cfg = SubCfg<Ar, K, TW>;
+  constexpr int Q = Cfg::Q;
+  constexpr int NT = 32 * TW;  // threads per team
+  constexpr int NG = 8 * TW;   // lane groups per team
   extern __shared__ __align__(16) unsigned char smem[];
-  const int m = a.m, n = a.n, tid = threadIdx.x;
-  constexpr int LMAX = 6;
-  // shared layout
-  C* Bm = reinterpret_cast<C*>(smem);                        // KMAX x KMAX
-  C* Tb = Bm + KMAX * KMAX;                                  // (1 << LMAX) x KMAX
-  C* sub = Tb + (1 << LMAX) * KMAX;                          // KMAX
-  Acc* accs = reinterpret_cast<Acc*>(sub + KMAX);            // KMAX x threads
-  double* w = reinterpret_cast<double*>(accs + KMAX * kCCThreads);  // m
-  int* cols = reinterpret_cast<int*>(w + m);                 // KMAX
-  int* rows = cols + KMAX;                                   // KMAX
-  int* cexp = rows + KMAX;                                   // KMAX column exponents
-  int* sexp = cexp + KMAX;                                   // KMAX sub-permanent exponents
+  const int team = threadIdx.x / NT;
+  const int tt = threadIdx.x - team * NT;
+  unsigned char* tb = smem + team * Cfg::team_bytes;
+  C* Bs = reinterpret_cast<C*>(tb);                                   // K x K (rows 0..k-2)
+  C* Ts = Bs + K * K;                                                 // (1 << L) x K
+  Acc* red = reinterpret_cast<Acc*>(tb + Cfg::c_elems * sizeof(C));  // TW x K
+
+  const int64_t tg = (int64_t)blockIdx.x * Cfg::TEAMS + team;
+  const int64_t s = tg / a.chunks;
+  if (s >= a.nsamp) return;  // the whole team leaves (a warp for TW = 1, the CTA for TW = 4)
+  const int chunk = (int)(tg - s * a.chunks);
+  const int m = a.m, k = a.k, d = k - 1, L = a.L, Hb = a.Hb;
+  const int32_t* rows = a.rows + s * kMaxPhotons;
+  const int32_t* cols = a.cols + s * kMaxPhotons;
   const C* U = reinterpret_cast<const C*>(a.uc);
 
-  for (int64_t s = blockIdx.x; s < a.count; s += gridDim.x) {
-    const uint64_t sid = a.first + (uint64_t)s;
-    const uint32_t s_lo = (uint32_t)sid, s_hi = (uint32_t)(sid >> 32);
-    if (tid == 0) {
-      for (int l = 0; l < n; ++l) cols[l] = a.cols0[l];
-      for (int q = n - 1; q >= 1; --q) {
-        const u4 r = philox4x32_10({s_lo, s_hi, 0xffffffffu, (uint32_t)q}, a.k0, a.k1);
-        const int j = (int)mulhi32(r.x, (uint32_t)(q + 1));
-        const int t = cols[q];
-        cols[q] = cols[j];
-        cols[j] = t;
-      }
+  // B (padding columns: S_c = 1 for every pattern, so they drop out of the products)
+  for (int e = tt; e < d * K; e += NT) {
+    const int r = e / K, c = e - r * K;
+    Bs[e] = c < k ? U[(size_t)rows[r] * m + cols[c]] : (r == 0 ? Ar::one() : Ar::zero());
+  }
+  team_sync<TW>();
+  // Scale column c by 2^e_c so that its l1 norm lies in [2^(c0-1), 2^c0) with
+  // (k - 1) c0 + (k - 2) <= 120: every product of k - 1 column sums and every sum of
+  // the 2^(k-2) terms stays inside the FP32 range.  Exact; the draw undoes it.
+  if (tt < k) {
+    float l1 = 0.f;
+    for (int r = 0; r < d; ++r) l1 += Ar::mag(Bs[r * K + tt]);
+    const int c0 = min(4, (120 - (k - 2)) / (k - 1));
+    int ex = 0;
+    if (l1 > 0.f) frexpf(l1, &ex);
+    const int e = l1 > 0.f ? c0 - ex : 0;
+    if (chunk == 0) a.cexp[s * kMaxPhotons + tt] = e;
+    for (int r = 0; r < d; ++r) Bs[r * K + tt] = Ar::scale(Bs[r * K + tt], e);
+  }
+  team_sync<TW>();
+  // lo table over rows 1..L: T[b][c] = sum_l (bit l of b ? -1 : +1) B[1 + l][c]
+  for (int c = tt; c < K; c += NT) {
+    C t0 = Ar::zero();
+    for (int l = 0; l < L; ++l) t0 = Ar::add_n(t0, Bs[(1 + l) * K + c]);
+    Ts[c] = t0;
+  }
+  team_sync<TW>();
+  for (int l = 0; l < L; ++l) {
+    const int half = 1 << l;
+    for (int e = tt; e < half * K; e += NT) {
+      const int b = e / K, c = e - b * K;
+      Ts[(b + half) * K + c] = Ar::sub_n(Ts[b * K + c], Ar::twice(Bs[(1 + l) * K + c]));
     }
-    __syncthreads();
+    team_sync<TW>();
+  }
 
-    for (int k = 1; k <= n; ++k) {
-      const int d = k - 1;  // rows chosen so far
-      if (k == 1) {
-        if (tid == 0) sub[0] = Ar::one();
-        __syncthreads();
-      } else {
-        for (int e = tid; e < d * k; e += blockDim.x) {
-          const int r = e / k, c = e - r * k;
-          Bm[r * KMAX + c] = U[(size_t)rows[r] * m + cols[c]];
-        }
-        const int F = d - 1;  // free sign bits (row 0 fixed to +1)
-        const int L = min(LMAX, max(0, F - 7));
-        const int Hb = F - L;
-        __syncthreads();
-        // Scale column c by 2^e_c so that its l1 norm lies in [2^(c0-1), 2^c0) with
-        // (k - 1) c0 + (k - 2) <= 120: every product of k - 1 column sums times the
-        // 2^(k-2) terms of the sum stays inside the FP32 range (a global scaling of U
-        // does not: aligned columns reach 1e56 at n = 30).  Exact (powers of two);
-        // undone below through the sub-permanent exponents.
-        if (tid < k) {
-          float l1 = 0.f;
-          for (int r = 0; r < d; ++r) l1 += Ar::mag(Bm[r * KMAX + tid]);
-          const int c0 = min(4, (120 - (k - 2)) / (k - 1));
-          int ex = 0;
-          if (l1 > 0.f) frexpf(l1, &ex);
-          const int e = l1 > 0.f ? c0 - ex : 0;
-          cexp[tid] = e;
-          for (int r = 0; r < d; ++r) Bm[r * KMAX + tid] = Ar::scale(Bm[r * KMAX + tid], e);
-        }
-        __syncthreads();
-        // lo table over rows 1..L
-        for (int c = tid; c < k; c += blockDim.x) {
-          C t0 = Ar::zero();
-          for (int l = 0; l < L; ++l) t0 = Ar::add(t0, Bm[(1 + l) * KMAX + c]);
-          Tb[c] = t0;
-        }
-        __syncthreads();
-        for (int l = 0; l < L; ++l) {
-          const int half = 1 << l;
-          for (int e = tid; e < half * k; e += blockDim.x) {
-            const int b = e / k, c = e - b * k;
-            Tb[(b + half) * KMAX + c] = Ar::sub(Tb[b * KMAX + c], Ar::twice(Bm[(1 + l) * KMAX + c]));
-          }
-          __syncthreads();
-        }
-        for (int l = 0; l < k; ++l) accs[l * kCCThreads + tid] = Ar::acc_zero();
-        const uint64_t nhi = 1ull << Hb;
-        for (uint64_t h = tid; h < nhi; h += blockDim.x) {
-          C H[KMAX];
+  // lane group grp (4 lanes, lane g owns columns 4j + g) takes hi patterns
+  // h0 + grp, h0 + grp + NG, ... of this chunk; every lane runs the same rounds so the
+  // shuffles see the full warp
+  const int lane = threadIdx.x & 31, g = lane & 3, grp = tt >> 2;
+  const uint64_t nhi = 1ull << Hb;
+  const uint64_t per = (nhi + (uint64_t)a.chunks - 1) / (uint64_t)a.chunks;
+  const uint64_t h0 = (uint64_t)chunk * per;
+  const uint64_t h1 = min(nhi, h0 + per);
+  const int nlo = 1 << L;
+  Acc acc[Q];
 #pragma unroll
-          for (int c = 0; c < KMAX; ++c) {
-            if (c < k) {
-              C v = Bm[c];  // row 0, sign +1
-              for (int t = 0; t < Hb; ++t) {
-                const C x = Bm[(1 + L + t) * KMAX + c];
-                v = ((h >> t) & 1ull) ? Ar::sub(v, x) : Ar::add(v, x);
-              }
-              H[c] = v;
-            }
-          }
-          const int hsign = __popcll(h) & 1;
-          for (int b = 0; b < (1 << L); ++b) {
-            const C* Tr = Tb + b * KMAX;
-            C suf[KMAX + 1];
-            suf[KMAX] = Ar::one();
+  for (int j = 0; j < Q; ++j) acc[j] = Ar::acc_zero();
+
+  for (uint64_t base = h0; base < h1; base += NG) {
+    const uint64_t h = base + grp;
+    const bool active = h < h1;  // uniform within the lane group
+    C Hq[Q];
 #pragma unroll
-            for (int c = KMAX - 1; c >= 0; --c) suf[c] = (c < k) ? Ar::mul(Ar::add(H[c], Tr[c]), suf[c + 1]) : suf[c + 1];
-            const bool neg = (__popc(b) & 1) ^ hsign;
-            C pre = Ar::one();
-#pragma unroll
-            for (int l = 0; l < KMAX; ++l) {
-              if (l < k) {
-                C term = Ar::mul(pre, suf[l + 1]);
-                if (neg) term = Ar::neg(term);
-                Acc acc = accs[l * kCCThreads + tid];
-                Ar::acc_add(acc, term);
-                accs[l * kCCThreads + tid] = acc;
-                pre = Ar::mul(pre, Ar::add(H[l], Tr[l]));
-              }
-            }
-          }
-        }
-        __syncthreads();
-        for (int l = tid; l < k; l += blockDim.x) {
-          Acc tot = accs[l * kCCThreads];
-          for (int t = 1; t < kCCThreads; ++t) tot = Ar::acc_merge(tot, accs[l * kCCThreads + t]);
-          sub[l] = Ar::acc_value(tot);
-          // true sub_l is proportional to sub_l * 2^{e_l} (the scales of the other
-          // columns are common to all l); record its binary exponent
-          const float mg = Ar::mag(sub[l]);
-          int ex = 0;
-          if (mg > 0.f) frexpf(mg, &ex);
-          sexp[l] = mg > 0.f ? ex + cexp[l] : INT_MIN;
-        }
-        __syncthreads();
-        if (tid < k) {
-          int emax = INT_MIN;
-          for (int l = 0; l < k; ++l) emax = max(emax, sexp[l]);
-          // largest |sub_l| near 1: the weights below cannot overflow
-          sub[tid] = sexp[tid] == INT_MIN ? Ar::zero() : Ar::scale(sub[tid], cexp[tid] - emax);
-        }
-        __syncthreads();
+    for (int j = 0; j < Q; ++j) {
+      const int c = 4 * j + g;
+      C v = Bs[c];  // row 0, sign +1
+      for (int t = 0; t < Hb; ++t) {
+        const C x = Bs[(1 + L + t) * K + c];
+        v = ((h >> t) & 1ull) ? Ar::sub_n(v, x) : Ar::add_n(v, x);
       }
-      // weights of every output mode for the next photon
-      for (int i = tid; i < m; i += blockDim.x) {
-        C z = Ar::zero();
-        for (int l = 0; l < k; ++l) z = Ar::add(z, Ar::mul(U[(size_t)i * m + cols[l]], sub[l]));
-        w[i] = Ar::norm2(z);
-      }
-      __syncthreads();
-      if (tid == 0) {
-        double W = 0.0;
-        for (int i = 0; i < m; ++i) W += w[i];
-        const u4 r = philox4x32_10({s_lo, s_hi, (uint32_t)k, 0u}, a.k0, a.k1);
-        const double target = u01_from(r.x, r.y) * W;
-        double run = 0.0;
-        int pick = -1, last_pos = 0;
-        for (int i = 0; i < m; ++i) {
-          if (w[i] > 0.0) last_pos = i;
-          run += w[i];
-          if (run > target) {
-            pick = i;
-            break;
-          }
-        }
-        rows[k - 1] = pick >= 0 ? pick : last_pos;
-      }
-      __syncthreads();
+      Hq[j] = v;
     }
-    int32_t* o = a.out + (size_t)s * m;
-    for (int i = tid; i < m; i += blockDim.x) o[i] = 0;
+    const int hs = __popcll(h) & 1;
+    for (int b = 0; b < nlo; ++b) {
+      const C* Tr = Ts + b * K + g;
+      C S[Q], sq[Q];
+#pragma unroll
+      for (int j = 0; j < Q; ++j) S[j] = Ar::add(Hq[j], Tr[4 * j]);
+      sq[Q - 1] = S[Q - 1];
+#pragma unroll
+      for (int j = Q - 2; j >= 0; --j) sq[j] = Ar::mul(S[j], sq[j + 1]);
+      // product of the other three lanes' columns
+      const C x1 = Ar::shfl(sq[0], 1);
+      const C x2 = Ar::shfl(Ar::mul(sq[0], x1), 2);
+      C pre = Ar::mul(x1, x2);
+      const bool neg = ((__popc(b) & 1) ^ hs) != 0;
+      if (active) {
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+          const C term = j + 1 < Q ? Ar::mul(pre, sq[j + 1]) : pre;
+          Ar::acc_add(acc[j], neg ? Ar::neg(term) : term);
+          if (j + 1 < Q) pre = Ar::mul(pre, S[j]);
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < Q; ++j) Ar::acc_fold(acc[j]);
+  }
+
+  // lanes with the same g hold the same columns: reduce over the warp's 8 groups
+#pragma unroll
+  for (int j = 0; j < Q; ++j) {
+    Acc v = acc[j];
+    v = Ar::acc_merge(v, Ar::acc_shfl(v, 4));
+    v = Ar::acc_merge(v, Ar::acc_shfl(v, 8));
+    v = Ar::acc_merge(v, Ar::acc_shfl(v, 16));
+    acc[j] = v;
+  }
+  double2* out = a.partials + ((size_t)s * a.chunks + chunk) * K;
+  if constexpr (TW == 1) {
+    if (lane < 4) {
+#pragma unroll
+      for (int j = 0; j < Q; ++j) out[4 * j + g] = Ar::acc_value(acc[j]);
+    }
+  } else {
+    const int w = tt >> 5;
+    if (lane < 4) {
+#pragma unroll
+      for (int j = 0; j < Q; ++j) red[w * K + 4 * j + g] = acc[j];
+    }
     __syncthreads();
-    if (tid == 0)
-      for (int k = 0; k < n; ++k) o[rows[k]] += 1;
+    if (tt < K) {
+      Acc v = red[tt];
+      for (int w2 = 1; w2 < TW; ++w2) v = Ar::acc_merge(v, red[w2 * K + tt]);
+      out[tt] = Ar::acc_value(v);
+    }
+  }
+}
+
+// ------------------------------------------------------------ draw
+struct CCDrawArgs {
+  const double2* u;  // U, row-major m x m (FP64)
+  int m, n, k, K, chunks;
+  int64_t nsamp, s0;  // wavefront size and index of its first sample in the call
+  uint64_t first;
+  uint32_t k0, k1;
+  const int32_t* cols0;  // input columns (n, ascending)
+  int32_t* cols;
+  int32_t* rows;
+  const int32_t* cexp;
+  const double2* partials;
+  int32_t* out;  // count x m
+};
+
+constexpr int kDrawThreads = 128;
+
+__global__ void __launch_bounds__(kDrawThreads) cc_draw_kernel(CCDrawArgs a) {
+  __shared__ double2 sub[kMaxPhotons];
+  __shared__ int sx[kMaxPhotons];
+  __shared__ int cl[kMaxPhotons];
+  __shared__ double wtot[kDrawThreads / 32];
+  __shared__ double tgt;
+  __shared__ int pick, lastpos;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int m = a.m, k = a.k;
+  const int per = (m + kDrawThreads - 1) / kDrawThreads;
+  const int i0 = min(m, tid * per), i1 = min(m, i0 + per);
+
+  for (int64_t sl = blockIdx.x; sl < a.nsamp; sl += gridDim.x) {
+    const uint64_t sid = a.first + (uint64_t)(a.s0 + sl);
+    const uint32_t s_lo = (uint32_t)sid, s_hi = (uint32_t)(sid >> 32);
+    int32_t* cols = a.cols + sl * kMaxPhotons;
+    int32_t* rows = a.rows + sl * kMaxPhotons;
+    if (k == 1) {
+      if (tid == 0) {
+        for (int l = 0; l < a.n; ++l) cols[l] = a.cols0[l];
+        for (int q = a.n - 1; q >= 1; --q) {
+          const u4 r = philox4x32_10({s_lo, s_hi, 0xffffffffu, (uint32_t)q}, a.k0, a.k1);
+          const int j = (int)mulhi32(r.x, (uint32_t)(q + 1));
+          const int t = cols[q];
+          cols[q] = cols[j];
+          cols[j] = t;
+        }
+        sub[0] = make_double2(1.0, 0.0);
+      }
+    } else if (tid < k) {
+      double2 v = make_double2(0.0, 0.0);
+      const double2* p = a.partials + (size_t)sl * a.chunks * a.K + tid;
+      for (int c = 0; c < a.chunks; ++c) {
+        v.x += p[(size_t)c * a.K].x;
+        v.y += p[(size_t)c * a.K].y;
+      }
+      sub[tid] = v;
+      const double mg = fabs(v.x) + fabs(v.y);
+      sx[tid] = mg > 0.0 ? ilogb(mg) + a.cexp[sl * kMaxPhotons + tid] : INT_MIN;
+    }
+    if (tid == 0) {
+      pick = INT_MAX;
+      lastpos = -1;
+    }
+    __syncthreads();
+    if (tid < k) {
+      cl[tid] = cols[tid];
+      if (k > 1) {
+        // true sub_l is proportional to sub_l 2^{e_l}; bring the largest near 1
+        int emax = INT_MIN;
+        for (int l = 0; l < k; ++l) emax = max(emax, sx[l]);
+        const double2 v = sub[tid];
+        const int e = a.cexp[sl * kMaxPhotons + tid] - emax;
+        sub[tid] = sx[tid] == INT_MIN ? make_double2(0.0, 0.0) : make_double2(ldexp(v.x, e), ldexp(v.y, e));
+      }
+    }
+    __syncthreads();
+    auto weight = [&](int i) {
+      const double2* ur = a.u + (size_t)i * m;
+      double zr = 0.0, zi = 0.0;
+      for (int l = 0; l < k; ++l) {
+        const double2 x = ur[cl[l]], y = sub[l];
+        zr = fma(x.x, y.x, fma(-x.y, y.y, zr));
+        zi = fma(x.x, y.y, fma(x.y, y.x, zi));
+      }
+      return zr * zr + zi * zi;
+    };
+    double loc = 0.0;
+    int lp = -1;
+    for (int i = i0; i < i1; ++i) {
+      const double w = weight(i);
+      loc += w;
+      if (w > 0.0) lp = i;
+    }
+    double incl = loc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (lane == 31) wtot[wid] = incl;
+    if (lp >= 0) atomicMax(&lastpos, lp);
+    __syncthreads();
+    double base = incl - loc, W = 0.0;
+    for (int w2 = 0; w2 < kDrawThreads / 32; ++w2) {
+      if (w2 < wid) base += wtot[w2];
+      W += wtot[w2];
+    }
+    if (tid == 0) {
+      const u4 r = philox4x32_10({s_lo, s_hi, (uint32_t)k, 0u}, a.k0, a.k1);
+      tgt = u01_from(r.x, r.y) * W;
+    }
+    __syncthreads();
+    const double target = tgt;
+    if (i0 < i1 && base + loc > target) {
+      double run = base;
+      for (int i = i0; i < i1; ++i) {
+        run += weight(i);
+        if (run > target) {
+          atomicMin(&pick, i);
+          break;
+        }
+      }
+    }
+    __syncthreads();
+    if (tid == 0) rows[k - 1] = pick != INT_MAX ? pick : (lastpos >= 0 ? lastpos : 0);
+    if (k == a.n) {
+      __syncthreads();
+      int32_t* o = a.out + (size_t)(a.s0 + sl) * m;
+      for (int i = tid; i < m; i += kDrawThreads) o[i] = 0;
+      __syncthreads();
+      if (tid == 0)
+        for (int q = 0; q < a.n; ++q) o[rows[q]] += 1;
+    }
     __syncthreads();
   }
 }
 
-template <class Ar, int KMAX>
-static size_t cc_smem(int m) {
-  using C = typename Ar::C;
-  size_t b = sizeof(C) * (KMAX * KMAX + (1 << 6) * KMAX + KMAX);
-  b += sizeof(typename Ar::Acc) * KMAX * kCCThreads;
-  b += sizeof(double) * m + sizeof(int) * 4 * KMAX;
-  return b;
+// ------------------------------------------------------------ host side
+struct StepPlan {
+  int K, TW, L, Hb, chunks;
+};
+
+static StepPlan plan_step(int k, int64_t nsamp, int target_ctas) {
+  StepPlan p{};
+  const int F = k - 2;
+  p.K = k <= 8 ? 8 : k <= 12 ? 12 : (k + 3) / 4 * 4;
+  p.TW = k <= 12 ? 1 : 4;
+  p.L = std::min(p.TW == 1 ? 4 : 6, F);
+  p.Hb = F - p.L;
+  p.chunks = 1;
+  if (p.TW == 4) {
+    const int64_t max_chunks = std::max<int64_t>(1, (1ll << p.Hb) / 32);
+    const int64_t want = (target_ctas + nsamp - 1) / nsamp;
+    p.chunks = (int)std::min<int64_t>(max_chunks, std::max<int64_t>(1, want));
+  }
+  return p;
 }
 
-template <class Ar, int KMAX>
-static int cc_launch(const CCArgs& a, cudaStream_t s) {
-  const size_t smem = cc_smem<Ar, KMAX>(a.m);
-  cudaError_t e = cudaFuncSetAttribute(cc2017_kernel<Ar, KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return (int)e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cc2017_kernel<Ar, KMAX>, kCCThreads, smem);
-  if (e != cudaSuccess) return (int)e;
-  const int64_t grid = std::min<int64_t>(a.count, (int64_t)num_sms() * std::max(1, per_sm));
-  cc2017_kernel<Ar, KMAX><<<(unsigned)grid, kCCThreads, smem, s>>>(a);
+template <class Ar, int K, int TW>
+static int launch_sub(const CCSubArgs& a, cudaStream_t s) {
+  using Cfg = SubCfg<Ar, K, TW>;
+  const size_t smem = Cfg::smem;
+  if (smem > 48 * 1024) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(cc_sub_kernel<Ar, K, TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+  }
+  const int64_t teams = a.nsamp * a.chunks;
+  const int64_t grid = (teams + Cfg::TEAMS - 1) / Cfg::TEAMS;
+  cc_sub_kernel<Ar, K, TW><<<(unsigned)grid, kCCThreads, smem, s>>>(a);
   return (int)cudaGetLastError();
 }
 
 template <class Ar>
-static int cc_dispatch(const CCArgs& a, cudaStream_t s) {
-  if (a.n <= 8) return cc_launch<Ar, 8>(a, s);
-  if (a.n <= 16) return cc_launch<Ar, 16>(a, s);
-  if (a.n <= 24) return cc_launch<Ar, 24>(a, s);
-  return cc_launch<Ar, 32>(a, s);
+static int sub_dispatch(const StepPlan& p, const CCSubArgs& a, cudaStream_t s) {
+  switch (p.K) {
+    case 8: return launch_sub<Ar, 8, 1>(a, s);
+    case 12: return launch_sub<Ar, 12, 1>(a, s);
+    case 16: return launch_sub<Ar, 16, 4>(a, s);
+    case 20: return launch_sub<Ar, 20, 4>(a, s);
+    case 24: return launch_sub<Ar, 24, 4>(a, s);
+    case 28: return launch_sub<Ar, 28, 4>(a, s);
+    case 32: return launch_sub<Ar, 32, 4>(a, s);
+    default: return (int)cudaErrorInvalidValue;
+  }
 }
+
+constexpr int64_t kWave = 32768;  // samples in flight
 
 }  // namespace pcvl
 
@@ -341,41 +526,89 @@ extern "C" int pcvl_cc2017_sample(const double* u_d, int32_t m, const int32_t* i
     for (int v = 0; v < input_state_h[i]; ++v) cols.push_back(i);
   }
   const int n = (int)cols.size();
-  PCVL_CHECK(n <= 32, "n=%d photons exceeds 32", n);
+  PCVL_CHECK(n <= kMaxPhotons, "n=%d photons exceeds %d", n, kMaxPhotons);
   if (count == 0) return PCVL_OK;
   if (n == 0) {
     PCVL_CUDA(cudaMemsetAsync(out_counts_d, 0, (size_t)count * m * sizeof(int32_t), s));
     return PCVL_OK;
   }
+  // wavefronts of equal size
+  const int64_t waves = (count + kWave - 1) / kWave;
+  const int64_t W = (count + waves - 1) / waves;
+  const int target_ctas = 8 * num_sms();
+  int max_chunks = 1;
+  for (int k = 2; k <= n; ++k) max_chunks = std::max(max_chunks, plan_step(k, std::min(W, count), target_ctas).chunks);
+  // also the last (possibly shorter) wavefront
+  const int64_t last = count - (waves - 1) * W;
+  for (int k = 2; k <= n; ++k) max_chunks = std::max(max_chunks, plan_step(k, last, target_ctas).chunks);
+
   const size_t csz = precision == 0 ? sizeof(cdd) : sizeof(float2);
-  const size_t o_cols = align_up((size_t)m * m * csz, 256);
+  const size_t o_cols0 = align_up((size_t)m * m * csz, 256);
+  const size_t o_cols = o_cols0 + 256;
+  const size_t st_bytes = align_up((size_t)W * kMaxPhotons * sizeof(int32_t), 256);
+  const size_t o_rows = o_cols + st_bytes;
+  const size_t o_cexp = o_rows + st_bytes;
+  const size_t o_part = o_cexp + st_bytes;
+  const size_t total = o_part + (size_t)W * max_chunks * kMaxPhotons * sizeof(double2);
   void* ws = nullptr;
-  PCVL_TRY(workspace(WS_CC2017, o_cols + 256, &ws));
+  PCVL_TRY(workspace(WS_CC2017, total, &ws));
   unsigned char* base = (unsigned char*)ws;
-  PCVL_TRY(stage_h2d(cols.data(), cols.size() * sizeof(int32_t), base + o_cols, s));
-  // |U_ij| ~ m^{-1/2} for Haar unitaries: scale by 2^round(log2 sqrt m) (exact), which
-  // keeps the column-sum products near 1 and cancels in the normalisation
-  const double scale = std::ldexp(1.0, (int)std::lround(0.5 * std::log2((double)m)));
+  PCVL_TRY(stage_h2d(cols.data(), cols.size() * sizeof(int32_t), base + o_cols0, s));
   const int cgrid = std::max(1, std::min(1024, (m * m + 255) / 256));
   if (precision == 0)
-    cc_convert<ArDD><<<cgrid, 256, 0, s>>>((const double2*)u_d, m, scale, (cdd*)base);
+    cc_convert<ArDD><<<cgrid, 256, 0, s>>>((const double2*)u_d, m, (cdd*)base);
   else
-    cc_convert<ArF32><<<cgrid, 256, 0, s>>>((const double2*)u_d, m, scale, (float2*)base);
+    cc_convert<ArF32><<<cgrid, 256, 0, s>>>((const double2*)u_d, m, (float2*)base);
   PCVL_CUDA(cudaGetLastError());
-  CCArgs a{};
-  a.uc = base;
-  a.m = m;
-  a.n = n;
-  a.cols0 = (const int32_t*)(base + o_cols);
-  a.count = count;
-  a.k0 = (uint32_t)seed;
-  a.k1 = (uint32_t)(seed >> 32);
-  a.first = first_sample;
-  a.out = out_counts_d;
-  const int rc = precision == 0 ? cc_dispatch<ArDD>(a, s) : cc_dispatch<ArF32>(a, s);
-  if (rc != 0) {
-    set_error("CC2017 kernel launch failed: %s", cudaGetErrorString((cudaError_t)rc));
-    return PCVL_ERR_CUDA;
+
+  CCSubArgs sa{};
+  sa.uc = base;
+  sa.m = m;
+  sa.cols = (const int32_t*)(base + o_cols);
+  sa.rows = (const int32_t*)(base + o_rows);
+  sa.cexp = (int32_t*)(base + o_cexp);
+  sa.partials = (double2*)(base + o_part);
+  CCDrawArgs da{};
+  da.u = (const double2*)u_d;
+  da.m = m;
+  da.n = n;
+  da.first = first_sample;
+  da.k0 = (uint32_t)seed;
+  da.k1 = (uint32_t)(seed >> 32);
+  da.cols0 = (const int32_t*)(base + o_cols0);
+  da.cols = (int32_t*)(base + o_cols);
+  da.rows = (int32_t*)(base + o_rows);
+  da.cexp = (const int32_t*)(base + o_cexp);
+  da.partials = (const double2*)(base + o_part);
+  da.out = out_counts_d;
+  const int draw_grid_cap = 16 * num_sms();
+
+  for (int64_t s0 = 0; s0 < count; s0 += W) {
+    const int64_t nw = std::min(W, count - s0);
+    da.s0 = s0;
+    da.nsamp = nw;
+    sa.nsamp = nw;
+    for (int k = 1; k <= n; ++k) {
+      da.k = k;
+      da.K = 1;
+      da.chunks = 1;
+      if (k >= 2) {
+        const StepPlan p = plan_step(k, nw, target_ctas);
+        sa.k = k;
+        sa.L = p.L;
+        sa.Hb = p.Hb;
+        sa.chunks = p.chunks;
+        const int rc = precision == 0 ? sub_dispatch<ArDD>(p, sa, s) : sub_dispatch<ArF32>(p, sa, s);
+        if (rc != 0) {
+          set_error("CC2017 sub-permanent launch failed: %s", cudaGetErrorString((cudaError_t)rc));
+          return PCVL_ERR_CUDA;
+        }
+        da.K = p.K;
+        da.chunks = p.chunks;
+      }
+      cc_draw_kernel<<<(unsigned)std::min<int64_t>(nw, draw_grid_cap), kDrawThreads, 0, s>>>(da);
+      PCVL_CUDA(cudaGetLastError());
+    }
   }
   return PCVL_OK;
 }

@@ -14,7 +14,8 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("m,inp,precision", [
     (5, (1, 1, 1, 0, 0), 0), (6, (2, 0, 1, 0, 1, 0), 0), (8, (1, 1, 1, 1, 1, 1, 0, 0), 0),
-    (10, (1,) * 10, 0), (12, (2, 2, 0, 0, 1, 1, 1, 1, 0, 0, 0, 1), 0), (6, (2, 0, 1, 0, 1, 0), 1)])
+    (10, (1,) * 10, 0), (12, (2, 2, 0, 0, 1, 1, 1, 1, 0, 0, 0, 1), 0), (20, (1,) * 14 + (0,) * 6, 0),
+    (6, (2, 0, 1, 0, 1, 0), 1)])
 def test_samples_equal_oracle(native, oracle, m, inp, precision):
     U = random_unitary(m, seed=m)
     N = 300
