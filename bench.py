@@ -197,12 +197,18 @@ def run_ours(args):
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
-    from perceval_gb300 import _native
+    from perceval_gb300 import _native, autotune
     from perceval_gb300.utils.matrix import random_unitary
     _native.load()
     dev = torch.device("cuda")
     out_dir = ROOT / "gpurun_out"
     out_dir.mkdir(exist_ok=True)
+    # launch shapes of the permanent bins: the cached autotuner table for this GPU, or a
+    # fresh tuning run (about 20 s, untimed) that is then cached
+    t_tune = time.perf_counter()
+    table = autotune.ensure_tuned(range(8, 25), log=lambda s: print(s, file=sys.stderr))
+    tuning = {"sizes": "8..24", "source": "cached table" if table is None else "tuned in this run",
+              "seconds": round(time.perf_counter() - t_tune, 1)}
 
     mats, flat, offs, sizes = make_batch(seed=rank)
     flops_total = float(sum(glynn_flops(int(n)) for n in sizes))
@@ -210,10 +216,11 @@ def run_ours(args):
     out_d = torch.empty(N_MATS, dtype=torch.complex128, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     bins = len(set(int(n) for n in sizes))
-    launches_per_step = bins + 2  # prepare + one per size bin + reduce
+    launches_per_step = bins + 2  # graph nodes: prepare + one per size bin + reduce
+    plan = _native.PermPlan(offs, sizes)  # fixed batch shape: one CUDA graph per step
 
     def step():
-        _native.permanent_batch(flat_d, offs, sizes, out_d)
+        plan(flat_d, out_d)
 
     def barrier():
         if ws > 1:
@@ -247,7 +254,7 @@ def run_ours(args):
 
     def e2e_step():
         dev_in.copy_(host_in, non_blocking=True)
-        _native.permanent_batch(dev_in, offs, sizes, out_d)
+        plan(dev_in, out_d)
         host_out.copy_(out_d, non_blocking=True)
 
     for _ in range(max(1, args.warmup)):
@@ -297,12 +304,30 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "complex128 I/O, float-float (f32x2) arithmetic", "data": "synthetic",
             "config": {"workload": WORKLOAD, "l2": "flushed between timed steps (256 MiB write)",
-                       "parallelism": f"replicas x{ws}", "launch": "one pcvl_permanent_batch per step"},
+                       "parallelism": f"replicas x{ws}",
+                       "launch": f"one CUDA graph per step (pcvl_perm_plan_execute: prepare, {bins} size bins as "
+                                 "concurrent branches, reduce)",
+                       "tuning": tuning},
             "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "roofline": roofline,
             "clocks": clocks.summary()}
 
     if rank == 0 and not args.skip_secondary:
-        line["secondary"] = secondary(torch, _native, random_unitary, dev, flush)
+        sec = {}
+        # the same batch through the plan-free call (host planning, staged descriptors and
+        # one launch per bin on the stream), device-timed like the headline
+        kb = []
+        for _ in range(3):
+            flush.zero_()
+            s, e = torch.cuda.Event(True), torch.cuda.Event(True)
+            s.record()
+            _native.permanent_batch(flat_d, offs, sizes, out_d)
+            e.record()
+            e.synchronize()
+            kb.append(s.elapsed_time(e))
+        sec["perm_batch_call_8192"] = {"ms": statistics.median(kb),
+                                       "perms_per_s": N_MATS / (statistics.median(kb) * 1e-3)}
+        sec.update(secondary(torch, _native, random_unitary, dev, flush))
+        line["secondary"] = sec
     if rank == 0 and ws == 1 and not args.skip_cpu:
         line["cpu_baseline"] = cpu_perm_baseline()
     if rank == 0:
@@ -411,6 +436,27 @@ def secondary(torch, _native, random_unitary, dev, flush):
     nb.prob_amplitudes(outs)
     t_naive = time.perf_counter() - t0
     res["small_m12_n6"] = {"slos_all_prob_ms": t_slos * 1e3, "outputs": len(p), "naive_1000_amplitudes_ms": t_naive * 1e3}
+    # launch latency of a small batch (1000 permanents of 6x6 Haar submatrices): the
+    # plan-free call against one graph launch of a plan, wall clock per call
+    sub = np.stack([U12[np.ix_(rng.choice(12, 6, replace=False), rng.choice(12, 6, replace=False))]
+                    for _ in range(1000)])
+    sd = torch.from_numpy(sub.reshape(-1)).to(dev)
+    so = torch.empty(1000, dtype=torch.complex128, device=dev)
+    s_offs = np.arange(1000, dtype=np.int64) * 36
+    s_sizes = np.full(1000, 6, dtype=np.int32)
+    small_plan = _native.PermPlan(s_offs, s_sizes)
+
+    def wall_us(fn, reps=200):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps * 1e6
+
+    res["perm_1000x6_latency"] = {"batch_call_us": wall_us(lambda: _native.permanent_batch(sd, s_offs, s_sizes, so)),
+                                  "plan_graph_us": wall_us(lambda: small_plan(sd, so))}
     return res
 
 
@@ -471,9 +517,10 @@ def run_learned(args):
 def profile_case(name: str):
     """One untimed run of a single hot kernel on a small case, for ncu captures."""
     import torch
-    from perceval_gb300 import _native
+    from perceval_gb300 import _native, autotune
     from perceval_gb300.utils.matrix import random_unitary
     _native.load()
+    autotune.load()  # the launch shapes the headline run tuned and cached, if any
     dev = torch.device("cuda")
     if name == "perm24":
         # 64 matrices of the n = 24 bin (one perm_bin_kernel<24> launch)

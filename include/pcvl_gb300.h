@@ -40,7 +40,7 @@ int pcvl_release_workspace(void);
  *
  * Batched exact permanents of `count` square complex128 matrices stored row-major
  * in mats_d; matrix i starts at complex element offsets_h[i] and has size
- * sizes_h[i] (0 <= n <= 48; the permanent of the 0x0 matrix is 1).  Results go to
+ * sizes_h[i] (0 <= n <= 40; the permanent of the 0x0 matrix is 1).  Results go to
  * out_d[i] (complex128).  method: 0 = Glynn (Gray-code over 2^(n-1) sign
  * vectors), 1 = Ryser (over 2^n column subsets).  Matrices are binned by size;
  * each bin's launch spreads Gray-code chunks across the whole chip, so one large
@@ -67,6 +67,32 @@ int pcvl_permanent_batch(const double* mats_d, const int64_t* offsets_h, const i
  * race on it and must be serialised by the caller. */
 int pcvl_permanent_batch_noalloc(const double* mats_d, const int64_t* offsets_h, const int32_t* sizes_h,
                                  int32_t count, double* out_d, int32_t method, void* stream);
+
+/* Launch-shape tuning of the permanent kernels (no reference counterpart; written by the
+ * autotuner in perceval_gb300/autotune.py).  For method (0 Glynn, 1 Ryser) and size n:
+ * lo_bits = sign bits every thread enumerates from the shared-memory table (-1: built-in
+ * min(7, max(0, F - 7)) with F the free bits), ctas_per_sm = target CTAs per SM over a
+ * size bin (0: built-in 8).  Applies to later calls and plans on every device; results
+ * change only by rounding.  Host-only, thread-safe. */
+int pcvl_perm_set_tuning(int32_t method, int32_t n, int32_t lo_bits, int32_t ctas_per_sm);
+/* The effective lo bits and CTAs per SM for (method, n). */
+int pcvl_perm_get_tuning(int32_t method, int32_t n, int32_t* lo_bits, int32_t* ctas_per_sm);
+
+/* Permanent plans (no reference counterpart): the batch layout of pcvl_permanent_batch
+ * fixed once for given sizes and offsets and executed as one CUDA graph (prepare, every
+ * size bin as a concurrent branch, reduce).  Execute only swaps the input and output
+ * pointers, so repeated batches of one shape (a sampler's proposal batches, a backend's
+ * output lists) skip the host planning and the per-bin launches.  The tuning table is read
+ * at creation.  The plan owns its device buffers; executions of one plan must be ordered
+ * (one stream), and a plan is not thread-safe. */
+typedef struct pcvl_perm_plan pcvl_perm_plan;
+
+int pcvl_perm_plan_create(pcvl_perm_plan** plan, const int64_t* offsets_h, const int32_t* sizes_h,
+                          int32_t count, int32_t method);
+int pcvl_perm_plan_execute(pcvl_perm_plan* plan, const double* mats_d, double* out_d, void* stream);
+/* Device bytes the plan holds. */
+int pcvl_perm_plan_bytes(const pcvl_perm_plan* plan, int64_t* bytes);
+int pcvl_perm_plan_destroy(pcvl_perm_plan* plan);
 
 /* ------------------------------------------------------------------ SLOS
  * Replaces the numeric SLOS path of perceval/backends/_slos.py:

@@ -25,6 +25,14 @@ SYMBOLS = {
     "pcvl_permanent_batch_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                     ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
                                                     ctypes.c_void_p]),
+    "pcvl_perm_set_tuning": (ctypes.c_int, [ctypes.c_int32] * 4),
+    "pcvl_perm_get_tuning": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+                                            ctypes.POINTER(ctypes.c_int32)]),
+    "pcvl_perm_plan_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p, ctypes.c_void_p,
+                                             ctypes.c_int32, ctypes.c_int32]),
+    "pcvl_perm_plan_execute": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "pcvl_perm_plan_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
+    "pcvl_perm_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "pcvl_slos_plan_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.c_void_p,
                                              ctypes.c_int32, ctypes.c_int32]),
     "pcvl_slos_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
@@ -147,6 +155,68 @@ def permanent_batch_noalloc(mats: torch.Tensor, offsets: np.ndarray, sizes: np.n
                                            out.data_ptr(), int(method), _stream_ptr(stream)),
           "pcvl_permanent_batch_noalloc")
     return out
+
+
+def set_perm_tuning(method: int, n: int, lo_bits: int = -1, ctas_per_sm: int = 0):
+    """Launch shape of the size-n permanent bin (-1 / 0: built-in choice).  Host-only."""
+    check(load(require_cuda=False).pcvl_perm_set_tuning(int(method), int(n), int(lo_bits), int(ctas_per_sm)),
+          "pcvl_perm_set_tuning")
+
+
+def get_perm_tuning(method: int, n: int) -> tuple[int, int]:
+    """Effective (lo_bits, ctas_per_sm) of the size-n permanent bin."""
+    lo, ct = ctypes.c_int32(), ctypes.c_int32()
+    check(load(require_cuda=False).pcvl_perm_get_tuning(int(method), int(n), ctypes.byref(lo), ctypes.byref(ct)),
+          "pcvl_perm_get_tuning")
+    return lo.value, ct.value
+
+
+class PermPlan:
+    """Owner of a ``pcvl_perm_plan``: permanents of a fixed batch shape, executed as one
+    CUDA graph per call (see pcvl_perm_plan_create)."""
+
+    def __init__(self, offsets: np.ndarray, sizes: np.ndarray, method: int = 0):
+        self._lib = load()
+        self.offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        self.sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+        self.count = int(self.sizes.shape[0])
+        if self.offsets.shape[0] != self.count or self.count < 1:
+            raise ValueError("offsets and sizes must describe the same (non-zero) number of matrices")
+        self.span = int((self.offsets + self.sizes.astype(np.int64) ** 2).max())
+        h = ctypes.c_void_p()
+        check(self._lib.pcvl_perm_plan_create(ctypes.byref(h), self.offsets.ctypes.data, self.sizes.ctypes.data,
+                                              self.count, int(method)), "pcvl_perm_plan_create")
+        self._h = h
+
+    @property
+    def nbytes(self) -> int:
+        v = ctypes.c_int64()
+        check(self._lib.pcvl_perm_plan_bytes(self._h, ctypes.byref(v)), "pcvl_perm_plan_bytes")
+        return v.value
+
+    def __call__(self, mats: torch.Tensor, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        _dev_tensor(mats, torch.complex128, "mats")
+        if mats.numel() < self.span:
+            raise ValueError("a matrix extends beyond the end of mats")
+        if out is None:
+            out = torch.empty(self.count, dtype=torch.complex128, device=mats.device)
+        _dev_tensor(out, torch.complex128, "out")
+        if out.numel() < self.count:
+            raise ValueError("out is smaller than the plan's matrix count")
+        check(self._lib.pcvl_perm_plan_execute(self._h, mats.data_ptr(), out.data_ptr(), _stream_ptr(stream)),
+              "pcvl_perm_plan_execute")
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.pcvl_perm_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ------------------------------------------------------------------ SLOS

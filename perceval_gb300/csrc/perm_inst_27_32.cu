@@ -3,5 +3,7 @@
 #include "permanent_kernel.cuh"
 
 namespace pcvl {
-int launch_perm_bin_27_32(int n, const PermBinArgs& a) { return launch_perm_bin_range<27, 32>(n, a); }
+int launch_perm_bin_27_32(int n, const PermBinArgs& a, PermNode* node) {
+  return launch_perm_bin_range<27, 32>(n, a, node);
+}
 }  // namespace pcvl

@@ -3,5 +3,7 @@
 #include "permanent_kernel.cuh"
 
 namespace pcvl {
-int launch_perm_bin_33_36(int n, const PermBinArgs& a) { return launch_perm_bin_range<33, 36>(n, a); }
+int launch_perm_bin_33_36(int n, const PermBinArgs& a, PermNode* node) {
+  return launch_perm_bin_range<33, 36>(n, a, node);
+}
 }  // namespace pcvl

@@ -3,5 +3,7 @@
 #include "permanent_kernel.cuh"
 
 namespace pcvl {
-int launch_perm_bin_37_40(int n, const PermBinArgs& a) { return launch_perm_bin_range<37, 40>(n, a); }
+int launch_perm_bin_37_40(int n, const PermBinArgs& a, PermNode* node) {
+  return launch_perm_bin_range<37, 40>(n, a, node);
+}
 }  // namespace pcvl

@@ -12,8 +12,10 @@
 //  3. perm_reduce: per matrix, Neumaier-compensated FP64 sum of its partials, times
 //     2^{1-n} (Glynn) or (-1)^n (Ryser), times 2^{-sum e_i}.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <mutex>
+#include <new>
 #include <vector>
 
 #include "permanent_kernel.cuh"
@@ -101,16 +103,49 @@ __global__ void perm_reduce(const double2* __restrict__ partials, const PermDesc
   out[i] = make_double2(re, im);
 }
 
-static int launch_bin(int n, const PermBinArgs& a) {
-  if (n <= 12) return launch_perm_bin_1_12(n, a);
-  if (n <= 20) return launch_perm_bin_13_20(n, a);
-  if (n <= 26) return launch_perm_bin_21_26(n, a);
-  if (n <= 32) return launch_perm_bin_27_32(n, a);
-  if (n <= 36) return launch_perm_bin_33_36(n, a);
-  return launch_perm_bin_37_40(n, a);
+static int launch_bin(int n, const PermBinArgs& a, PermNode* node = nullptr) {
+  if (n <= 12) return launch_perm_bin_1_12(n, a, node);
+  if (n <= 20) return launch_perm_bin_13_20(n, a, node);
+  if (n <= 26) return launch_perm_bin_21_26(n, a, node);
+  if (n <= 32) return launch_perm_bin_27_32(n, a, node);
+  if (n <= 36) return launch_perm_bin_33_36(n, a, node);
+  return launch_perm_bin_37_40(n, a, node);
 }
 
-// Chooses lo bits, patterns per thread and CTAs per matrix for one size bin.
+// Tuning table: per method and size, the lo bits and the target CTAs per SM of a bin,
+// packed as (L + 1) | ctas << 8 (0 in a field: the built-in choice).  Written by
+// pcvl_perm_set_tuning (the autotuner), read without locks by every launch.
+static std::atomic<uint32_t> g_tune[2][kPermMaxN + 1];
+
+constexpr int kDefaultCtasPerSm = 8;
+constexpr size_t kMaxPermSmem = 227 * 1024;
+
+static int default_lo_bits(int F) { return std::min(7, std::max(0, F - 7)); }
+
+// Launch shape of one size bin: lo bits, hi bits, patterns per thread, CTAs per matrix.
+struct BinShape {
+  int L, Hbits;
+  int64_t P, items_per_mat;
+};
+
+static BinShape bin_shape(int n, int ryser, int64_t nmat, int sms) {
+  const uint32_t t = g_tune[ryser][n].load(std::memory_order_relaxed);
+  const int F = ryser ? n : n - 1;  // free bits
+  const int tl = (int)(t & 0xffu) - 1;
+  const int tc = (int)((t >> 8) & 0xffu);
+  BinShape s;
+  s.L = tl >= 0 ? std::min(tl, F) : default_lo_bits(F);
+  s.Hbits = F - s.L;
+  const int ctas = tc > 0 ? tc : kDefaultCtasPerSm;
+  const int64_t nhi = int64_t(1) << s.Hbits;
+  // aim for >= ctas CTAs per SM over the bin, never fewer patterns than one per thread
+  int64_t P = nhi * nmat / ((int64_t)kPermThreads * ctas * sms);
+  P = std::max<int64_t>(1, std::min<int64_t>(P, std::max<int64_t>(1, nhi / kPermThreads)));
+  s.P = P;
+  s.items_per_mat = (nhi + kPermThreads * P - 1) / (kPermThreads * P);
+  return s;
+}
+
 struct BinPlan {
   int n = 0;
   int L = 0, Hbits = 0;
@@ -119,16 +154,81 @@ struct BinPlan {
 };
 
 static void plan_bin(BinPlan& b, int ryser, int sms) {
-  const int F = ryser ? b.n : b.n - 1;  // free bits
-  b.L = std::min(7, std::max(0, F - 7));
-  b.Hbits = F - b.L;
-  const int64_t nhi = int64_t(1) << b.Hbits;
-  const int64_t total_hi = nhi * (int64_t)b.mids.size();
-  // aim for >= 8 CTAs per SM over the bin, never fewer patterns than one per thread
-  int64_t P = total_hi / ((int64_t)kPermThreads * 8 * sms);
-  P = std::max<int64_t>(1, std::min<int64_t>(P, std::max<int64_t>(1, nhi / kPermThreads)));
-  b.P = P;
-  b.items_per_mat = (nhi + kPermThreads * P - 1) / (kPermThreads * P);
+  const BinShape s = bin_shape(b.n, ryser, (int64_t)b.mids.size(), sms);
+  b.L = s.L;
+  b.Hbits = s.Hbits;
+  b.P = s.P;
+  b.items_per_mat = s.items_per_mat;
+}
+
+// Device layout of one batch: [prepared cdd][exps][offs][sizes][mids][descs][partials];
+// the small arrays travel as one host blob covering [offs, partials).
+struct BatchLayout {
+  std::vector<BinPlan> bins;  // indexed by n; empty bins have no mids
+  std::vector<PermDesc> descs;
+  int64_t total_elems = 0, total_items = 0;
+  size_t o_prep = 0, o_exps = 0, o_offs = 0, o_size = 0, o_mids = 0, o_desc = 0, o_part = 0, total = 0;
+  std::vector<unsigned char> blob;
+};
+
+static int make_layout(const int64_t* offsets_h, const int32_t* sizes_h, int32_t count, int ryser,
+                       BatchLayout& L) {
+  L.bins.assign(kPermMaxN + 1, BinPlan());
+  for (int i = 0; i < count; ++i) {
+    const int n = sizes_h[i];
+    PCVL_CHECK(n >= 0 && n <= kPermMaxN, "matrix %d: size %d outside [0, %d]", i, n, kPermMaxN);
+    PCVL_CHECK(offsets_h[i] >= 0, "matrix %d: negative offset", i);
+    L.total_elems = std::max<int64_t>(L.total_elems, offsets_h[i] + (int64_t)n * n);
+    if (n > 0) L.bins[n].mids.push_back(i);
+  }
+  const int sms = num_sms();
+  L.descs.assign(count, PermDesc{0, 0, 0});
+  for (int n = 1; n <= kPermMaxN; ++n) {
+    BinPlan& b = L.bins[n];
+    if (b.mids.empty()) continue;
+    b.n = n;
+    plan_bin(b, ryser, sms);
+    for (size_t k = 0; k < b.mids.size(); ++k)
+      L.descs[b.mids[k]] = {L.total_items + (int64_t)k * b.items_per_mat, (int32_t)b.items_per_mat, n};
+    L.total_items += (int64_t)b.mids.size() * b.items_per_mat;
+  }
+  L.o_prep = 0;
+  L.o_exps = align_up(L.o_prep + (size_t)L.total_elems * sizeof(cdd), 256);
+  L.o_offs = align_up(L.o_exps + (size_t)count * 4, 256);
+  L.o_size = align_up(L.o_offs + (size_t)count * 8, 256);
+  L.o_mids = align_up(L.o_size + (size_t)count * 4, 256);
+  L.o_desc = align_up(L.o_mids + (size_t)count * 4, 256);
+  L.o_part = align_up(L.o_desc + (size_t)count * sizeof(PermDesc), 256);
+  L.total = align_up(L.o_part + (size_t)std::max<int64_t>(L.total_items, 1) * sizeof(double2), 256);
+  L.blob.assign(L.o_part - L.o_offs, 0);
+  memcpy(L.blob.data(), offsets_h, (size_t)count * 8);
+  memcpy(L.blob.data() + (L.o_size - L.o_offs), sizes_h, (size_t)count * 4);
+  std::vector<int32_t> mids_all;
+  mids_all.reserve(count);
+  for (int n = 1; n <= kPermMaxN; ++n)
+    for (int32_t id : L.bins[n].mids) mids_all.push_back(id);
+  if (!mids_all.empty()) memcpy(L.blob.data() + (L.o_mids - L.o_offs), mids_all.data(), mids_all.size() * 4);
+  memcpy(L.blob.data() + (L.o_desc - L.o_offs), L.descs.data(), (size_t)count * sizeof(PermDesc));
+  return PCVL_OK;
+}
+
+// Bin kernel arguments of a layout placed at device address base.
+static PermBinArgs bin_args(const BatchLayout& L, unsigned char* base, int n, int64_t mid_off, int ryser,
+                            cudaStream_t stream) {
+  const BinPlan& b = L.bins[n];
+  PermBinArgs a;
+  a.A = (const cdd*)(base + L.o_prep);
+  a.offs = (const int64_t*)(base + L.o_offs);
+  a.mids = (const int32_t*)(base + L.o_mids) + mid_off;
+  a.nmat = (int32_t)b.mids.size();
+  a.L = b.L;
+  a.Hbits = b.Hbits;
+  a.P = b.P;
+  a.items_per_mat = b.items_per_mat;
+  a.ryser = ryser;
+  a.partials = (double2*)(base + L.o_part) + L.descs[b.mids[0]].base;
+  a.stream = stream;
+  return a;
 }
 
 }  // namespace pcvl
@@ -143,99 +243,245 @@ extern "C" int pcvl_permanent_batch(const double* mats_d, const int64_t* offsets
   PCVL_CHECK(mats_d && offsets_h && sizes_h && out_d, "null pointer argument");
   PCVL_CHECK(method == 0 || method == 1, "method must be 0 (Glynn) or 1 (Ryser), got %d", method);
   const int ryser = method;
-
-  int64_t total_elems = 0;
-  std::vector<BinPlan> bins(kPermMaxN + 1);
-  for (int i = 0; i < count; ++i) {
-    const int n = sizes_h[i];
-    PCVL_CHECK(n >= 0 && n <= kPermMaxN, "matrix %d: size %d outside [0, %d]", i, n, kPermMaxN);
-    PCVL_CHECK(offsets_h[i] >= 0, "matrix %d: negative offset", i);
-    total_elems = std::max<int64_t>(total_elems, offsets_h[i] + (int64_t)n * n);
-    if (n > 0) bins[n].mids.push_back(i);
-  }
-  const int sms = num_sms();
-
-  std::vector<PermDesc> descs(count);
-  int64_t total_items = 0;
-  for (int n = 1; n <= kPermMaxN; ++n) {
-    BinPlan& b = bins[n];
-    if (b.mids.empty()) continue;
-    b.n = n;
-    plan_bin(b, ryser, sms);
-    for (size_t k = 0; k < b.mids.size(); ++k) {
-      descs[b.mids[k]] = {total_items + (int64_t)k * b.items_per_mat, (int32_t)b.items_per_mat, n};
-    }
-    total_items += (int64_t)b.mids.size() * b.items_per_mat;
-  }
-  for (int i = 0; i < count; ++i)
-    if (sizes_h[i] == 0) descs[i] = {0, 0, 0};
-
-  // workspace: [prepared cdd][exps][offs][sizes][mids][descs][partials]
-  size_t o_prep = 0;
-  size_t o_exps = align_up(o_prep + (size_t)total_elems * sizeof(cdd), 256);
-  size_t o_offs = align_up(o_exps + (size_t)count * 4, 256);
-  size_t o_size = align_up(o_offs + (size_t)count * 8, 256);
-  size_t o_mids = align_up(o_size + (size_t)count * 4, 256);
-  size_t o_desc = align_up(o_mids + (size_t)count * 4, 256);
-  size_t o_part = align_up(o_desc + (size_t)count * sizeof(PermDesc), 256);
-  size_t total = align_up(o_part + (size_t)std::max<int64_t>(total_items, 1) * sizeof(double2), 256);
+  BatchLayout L;
+  PCVL_TRY(make_layout(offsets_h, sizes_h, count, ryser, L));
   void* ws = nullptr;
-  PCVL_TRY(workspace(WS_PERM, total, &ws));
+  PCVL_TRY(workspace(WS_PERM, L.total, &ws));
   unsigned char* base = (unsigned char*)ws;
+  PCVL_TRY(stage_h2d(L.blob.data(), L.blob.size(), base + L.o_offs, stream));
 
-  // one host blob for the small arrays -> one staged copy
-  std::vector<unsigned char> blob(o_part - o_offs);
-  memcpy(blob.data(), offsets_h, (size_t)count * 8);
-  memcpy(blob.data() + (o_size - o_offs), sizes_h, (size_t)count * 4);
-  int64_t mid_pos = 0;
-  std::vector<int32_t> mids_all(count);
-  for (int n = 1; n <= kPermMaxN; ++n)
-    for (int32_t id : bins[n].mids) mids_all[mid_pos++] = id;
-  memcpy(blob.data() + (o_mids - o_offs), mids_all.data(), (size_t)mid_pos * 4);
-  memcpy(blob.data() + (o_desc - o_offs), descs.data(), (size_t)count * sizeof(PermDesc));
-  PCVL_TRY(stage_h2d(blob.data(), blob.size(), base + o_offs, stream));
-
-  cdd* prep = (cdd*)(base + o_prep);
-  int32_t* exps_d = (int32_t*)(base + o_exps);
-  const int64_t* offs_d = (const int64_t*)(base + o_offs);
-  const int32_t* sizes_d = (const int32_t*)(base + o_size);
-  int32_t* mids_d = (int32_t*)(base + o_mids);
-  const PermDesc* descs_d = (const PermDesc*)(base + o_desc);
-  double2* parts = (double2*)(base + o_part);
-
+  cdd* prep = (cdd*)(base + L.o_prep);
+  int32_t* exps_d = (int32_t*)(base + L.o_exps);
+  const int64_t* offs_d = (const int64_t*)(base + L.o_offs);
+  const int32_t* sizes_d = (const int32_t*)(base + L.o_size);
+  const PermDesc* descs_d = (const PermDesc*)(base + L.o_desc);
+  double2* parts = (double2*)(base + L.o_part);
   {
     const int threads = 256;
     const int blocks = (int)(((int64_t)count * 32 + threads - 1) / threads);
     perm_prepare<<<blocks, threads, 0, stream>>>((const double2*)mats_d, offs_d, sizes_d, count, prep, exps_d);
     PCVL_CUDA(cudaGetLastError());
   }
-
   int64_t mid_off = 0;
   for (int n = 1; n <= kPermMaxN; ++n) {
-    BinPlan& b = bins[n];
-    if (b.mids.empty()) continue;
-    PermBinArgs a;
-    a.A = prep;
-    a.offs = offs_d;
-    a.mids = mids_d + mid_off;
-    a.nmat = (int32_t)b.mids.size();
-    a.L = b.L;
-    a.Hbits = b.Hbits;
-    a.P = b.P;
-    a.items_per_mat = b.items_per_mat;
-    a.ryser = ryser;
-    a.partials = parts + descs[b.mids[0]].base;
-    a.stream = stream;
+    if (L.bins[n].mids.empty()) continue;
+    const PermBinArgs a = bin_args(L, base, n, mid_off, ryser, stream);
     const int rc = launch_bin(n, a);
     if (rc != 0) {
       set_error("permanent kernel launch for n=%d failed: %s", n, cudaGetErrorString((cudaError_t)rc));
       return PCVL_ERR_CUDA;
     }
-    mid_off += (int64_t)b.mids.size();
+    mid_off += (int64_t)L.bins[n].mids.size();
   }
-
   perm_reduce<<<(count + 127) / 128, 128, 0, stream>>>(parts, descs_d, exps_d, count, ryser, (double2*)out_d);
   PCVL_CUDA(cudaGetLastError());
+  return PCVL_OK;
+}
+
+// ------------------------------------------------------------------ tuning
+extern "C" int pcvl_perm_set_tuning(int32_t method, int32_t n, int32_t lo_bits, int32_t ctas_per_sm) {
+  PCVL_CHECK(method == 0 || method == 1, "method must be 0 (Glynn) or 1 (Ryser), got %d", method);
+  PCVL_CHECK(n >= 1 && n <= kPermMaxN, "n=%d outside [1, %d]", n, kPermMaxN);
+  PCVL_CHECK(lo_bits >= -1 && lo_bits <= 12, "lo_bits=%d outside [-1, 12]", lo_bits);
+  PCVL_CHECK(ctas_per_sm >= 0 && ctas_per_sm <= 64, "ctas_per_sm=%d outside [0, 64]", ctas_per_sm);
+  if (lo_bits >= 0) {
+    const int F = method ? n : n - 1;
+    const int l = std::min(lo_bits, F);
+    const size_t smem = (size_t)(n * n + (1 << l) * n) * sizeof(cdd);
+    PCVL_CHECK(smem <= kMaxPermSmem, "n=%d with %d lo bits needs %zu bytes of shared memory (max %zu)", n, l, smem,
+               kMaxPermSmem);
+  }
+  g_tune[method][n].store((uint32_t)(lo_bits + 1) | ((uint32_t)ctas_per_sm << 8), std::memory_order_relaxed);
+  return PCVL_OK;
+}
+
+extern "C" int pcvl_perm_get_tuning(int32_t method, int32_t n, int32_t* lo_bits, int32_t* ctas_per_sm) {
+  PCVL_CHECK(method == 0 || method == 1, "method must be 0 (Glynn) or 1 (Ryser), got %d", method);
+  PCVL_CHECK(n >= 1 && n <= kPermMaxN, "n=%d outside [1, %d]", n, kPermMaxN);
+  PCVL_CHECK(lo_bits && ctas_per_sm, "null pointer argument");
+  const uint32_t t = g_tune[method][n].load(std::memory_order_relaxed);
+  const int F = method ? n : n - 1;
+  const int tl = (int)(t & 0xffu) - 1;
+  const int tc = (int)((t >> 8) & 0xffu);
+  *lo_bits = tl >= 0 ? std::min(tl, F) : default_lo_bits(F);
+  *ctas_per_sm = tc > 0 ? tc : kDefaultCtasPerSm;
+  return PCVL_OK;
+}
+
+// ------------------------------------------------------------------ plans (CUDA graphs)
+// A plan fixes the sizes and offsets of a batch.  Its device buffers hold the prepared
+// matrices, descriptors and partials; the launch sequence is one CUDA graph: prepare,
+// then every size bin as an independent branch (bins run concurrently), then reduce.
+// Executing again only updates the input and output pointers of the first and last
+// nodes and relaunches the graph.
+struct pcvl_perm_plan {
+  int device = 0, count = 0, ryser = 0;
+  size_t bytes = 0;
+  unsigned char* dev = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphNode_t prep_node = nullptr, red_node = nullptr;
+  unsigned prep_blocks = 0, red_blocks = 0;
+  // arguments of the prepare and reduce kernels (src and out change per call)
+  const double2* src = nullptr;
+  const int64_t* offs_d = nullptr;
+  const int32_t* sizes_d = nullptr;
+  cdd* prep = nullptr;
+  int32_t* exps_d = nullptr;
+  double2* parts = nullptr;
+  const PermDesc* descs_d = nullptr;
+  double2* out = nullptr;
+};
+
+namespace {
+
+void destroy_perm_plan(pcvl_perm_plan* p) {
+  if (!p) return;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  if (p->dev) cudaFree(p->dev);
+  delete p;
+}
+
+cudaKernelNodeParams prep_params(pcvl_perm_plan* p, void** args) {
+  args[0] = &p->src;
+  args[1] = &p->offs_d;
+  args[2] = &p->sizes_d;
+  args[3] = &p->count;
+  args[4] = &p->prep;
+  args[5] = &p->exps_d;
+  cudaKernelNodeParams kp{};
+  kp.func = reinterpret_cast<void*>(perm_prepare);
+  kp.gridDim = dim3(p->prep_blocks);
+  kp.blockDim = dim3(256);
+  kp.sharedMemBytes = 0;
+  kp.kernelParams = args;
+  return kp;
+}
+
+cudaKernelNodeParams red_params(pcvl_perm_plan* p, void** args) {
+  args[0] = &p->parts;
+  args[1] = &p->descs_d;
+  args[2] = &p->exps_d;
+  args[3] = &p->count;
+  args[4] = &p->ryser;
+  args[5] = &p->out;
+  cudaKernelNodeParams kp{};
+  kp.func = reinterpret_cast<void*>(perm_reduce);
+  kp.gridDim = dim3(p->red_blocks);
+  kp.blockDim = dim3(128);
+  kp.sharedMemBytes = 0;
+  kp.kernelParams = args;
+  return kp;
+}
+
+}  // namespace
+
+extern "C" int pcvl_perm_plan_create(pcvl_perm_plan** plan, const int64_t* offsets_h, const int32_t* sizes_h,
+                                     int32_t count, int32_t method) {
+  PCVL_CHECK(plan, "null plan pointer");
+  *plan = nullptr;
+  PCVL_CHECK(offsets_h && sizes_h, "null pointer argument");
+  PCVL_CHECK(count >= 1, "a plan needs at least one matrix (got %d)", count);
+  PCVL_CHECK(method == 0 || method == 1, "method must be 0 (Glynn) or 1 (Ryser), got %d", method);
+  BatchLayout L;
+  PCVL_TRY(make_layout(offsets_h, sizes_h, count, method, L));
+  pcvl_perm_plan* p = new (std::nothrow) pcvl_perm_plan();
+  PCVL_CHECK(p, "out of host memory");
+  p->count = count;
+  p->ryser = method;
+  p->bytes = L.total;
+  cudaError_t e = cudaGetDevice(&p->device);
+  if (e == cudaSuccess) e = cudaMalloc(&p->dev, L.total);
+  if (e != cudaSuccess) {
+    destroy_perm_plan(p);
+    set_error("permanent plan: device allocation of %zu bytes failed: %s", L.total, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? PCVL_ERR_MEMORY : PCVL_ERR_CUDA;
+  }
+  e = cudaMemcpy(p->dev + L.o_offs, L.blob.data(), L.blob.size(), cudaMemcpyHostToDevice);
+  p->offs_d = (const int64_t*)(p->dev + L.o_offs);
+  p->sizes_d = (const int32_t*)(p->dev + L.o_size);
+  p->prep = (cdd*)(p->dev + L.o_prep);
+  p->exps_d = (int32_t*)(p->dev + L.o_exps);
+  p->parts = (double2*)(p->dev + L.o_part);
+  p->descs_d = (const PermDesc*)(p->dev + L.o_desc);
+  p->prep_blocks = (unsigned)(((int64_t)count * 32 + 255) / 256);
+  p->red_blocks = (unsigned)((count + 127) / 128);
+  if (e == cudaSuccess) e = cudaGraphCreate(&p->graph, 0);
+  void* pargs[6];
+  void* rargs[6];
+  if (e == cudaSuccess) {
+    const cudaKernelNodeParams kp = prep_params(p, pargs);
+    e = cudaGraphAddKernelNode(&p->prep_node, p->graph, nullptr, 0, &kp);
+  }
+  std::vector<cudaGraphNode_t> bin_nodes;
+  int64_t mid_off = 0;
+  for (int n = 1; n <= kPermMaxN && e == cudaSuccess; ++n) {
+    if (L.bins[n].mids.empty()) continue;
+    PermBinArgs a = bin_args(L, p->dev, n, mid_off, method, nullptr);
+    PermNode nd{};
+    const int rc = launch_bin(n, a, &nd);
+    if (rc != 0) {
+      e = (cudaError_t)rc;
+      break;
+    }
+    void* args[1] = {&a};
+    cudaKernelNodeParams kp{};
+    kp.func = nd.func;
+    kp.gridDim = dim3(nd.grid);
+    kp.blockDim = dim3(kPermThreads);
+    kp.sharedMemBytes = (unsigned)nd.smem;
+    kp.kernelParams = args;
+    cudaGraphNode_t node = nullptr;
+    e = cudaGraphAddKernelNode(&node, p->graph, &p->prep_node, 1, &kp);
+    bin_nodes.push_back(node);
+    mid_off += (int64_t)L.bins[n].mids.size();
+  }
+  if (e == cudaSuccess) {
+    const cudaKernelNodeParams kp = red_params(p, rargs);
+    if (bin_nodes.empty())
+      e = cudaGraphAddKernelNode(&p->red_node, p->graph, &p->prep_node, 1, &kp);
+    else
+      e = cudaGraphAddKernelNode(&p->red_node, p->graph, bin_nodes.data(), bin_nodes.size(), &kp);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+  if (e != cudaSuccess) {
+    destroy_perm_plan(p);
+    set_error("permanent plan: graph construction failed: %s", cudaGetErrorString(e));
+    return PCVL_ERR_CUDA;
+  }
+  *plan = p;
+  return PCVL_OK;
+}
+
+extern "C" int pcvl_perm_plan_execute(pcvl_perm_plan* p, const double* mats_d, double* out_d, void* stream_) {
+  PCVL_CHECK(p && mats_d && out_d, "null pointer argument");
+  int dev = 0;
+  PCVL_CUDA(cudaGetDevice(&dev));
+  PCVL_CHECK(dev == p->device, "the plan belongs to device %d, the current device is %d", p->device, dev);
+  void* args[6];
+  if ((const double2*)mats_d != p->src) {
+    p->src = (const double2*)mats_d;
+    const cudaKernelNodeParams kp = prep_params(p, args);
+    PCVL_CUDA(cudaGraphExecKernelNodeSetParams(p->exec, p->prep_node, &kp));
+  }
+  if ((double2*)out_d != p->out) {
+    p->out = (double2*)out_d;
+    const cudaKernelNodeParams kp = red_params(p, args);
+    PCVL_CUDA(cudaGraphExecKernelNodeSetParams(p->exec, p->red_node, &kp));
+  }
+  PCVL_CUDA(cudaGraphLaunch(p->exec, (cudaStream_t)stream_));
+  return PCVL_OK;
+}
+
+extern "C" int pcvl_perm_plan_bytes(const pcvl_perm_plan* p, int64_t* bytes) {
+  PCVL_CHECK(p && bytes, "null pointer argument");
+  *bytes = (int64_t)p->bytes;
+  return PCVL_OK;
+}
+
+extern "C" int pcvl_perm_plan_destroy(pcvl_perm_plan* p) {
+  destroy_perm_plan(p);
   return PCVL_OK;
 }
 
@@ -329,14 +575,11 @@ extern "C" int pcvl_permanent_batch_noalloc(const double* mats_d, const int64_t*
     mid_base[n] = mids_so_far;
     item_base[n] = total_items;
     if (bin_count[n] == 0) continue;
-    const int F = ryser ? n : n - 1;
-    L[n] = std::min(7, std::max(0, F - 7));
-    Hb[n] = F - L[n];
-    const int64_t nhi = int64_t(1) << Hb[n];
-    int64_t p = nhi * bin_count[n] / ((int64_t)kPermThreads * 8 * sms);
-    p = std::max<int64_t>(1, std::min<int64_t>(p, std::max<int64_t>(1, nhi / kPermThreads)));
-    P[n] = p;
-    ipm[n] = (nhi + kPermThreads * p - 1) / (kPermThreads * p);
+    const BinShape sh = bin_shape(n, ryser, bin_count[n], sms);
+    L[n] = sh.L;
+    Hb[n] = sh.Hbits;
+    P[n] = sh.P;
+    ipm[n] = sh.items_per_mat;
     total_items += bin_count[n] * ipm[n];
     mids_so_far += bin_count[n];
   }

@@ -173,8 +173,16 @@ __global__ void __launch_bounds__(kPermThreads) perm_bin_kernel(PermBinArgs a) {
   }
 }
 
+// Launch shape of one bin, for callers that build a CUDA graph node instead of launching.
+struct PermNode {
+  void* func;
+  unsigned grid;
+  size_t smem;
+};
+
+// Launches the bin on a.stream, or (node != nullptr) only fills in its launch shape.
 template <int N>
-int launch_perm_bin_n(const PermBinArgs& a) {
+int launch_perm_bin_n(const PermBinArgs& a, PermNode* node) {
   const size_t smem = (size_t)(N * N + (1 << a.L) * N) * sizeof(cdd);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(perm_bin_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -182,27 +190,33 @@ int launch_perm_bin_n(const PermBinArgs& a) {
     if (e != cudaSuccess) return (int)e;
   }
   const int64_t items = (int64_t)a.nmat * a.items_per_mat;
+  if (node) {
+    node->func = reinterpret_cast<void*>(perm_bin_kernel<N>);
+    node->grid = (unsigned)items;
+    node->smem = smem;
+    return 0;
+  }
   perm_bin_kernel<N><<<(unsigned)items, kPermThreads, smem, a.stream>>>(a);
   return (int)cudaGetLastError();
 }
 
 // Dispatch over the sizes instantiated in one translation unit.
 template <int LO, int HI>
-int launch_perm_bin_range(int n, const PermBinArgs& a) {
+int launch_perm_bin_range(int n, const PermBinArgs& a, PermNode* node) {
   if constexpr (LO > HI) {
     return -1;
   } else {
-    if (n == LO) return launch_perm_bin_n<LO>(a);
-    return launch_perm_bin_range<LO + 1, HI>(n, a);
+    if (n == LO) return launch_perm_bin_n<LO>(a, node);
+    return launch_perm_bin_range<LO + 1, HI>(n, a, node);
   }
 }
 
-int launch_perm_bin_1_12(int n, const PermBinArgs& a);
-int launch_perm_bin_13_20(int n, const PermBinArgs& a);
-int launch_perm_bin_21_26(int n, const PermBinArgs& a);
-int launch_perm_bin_27_32(int n, const PermBinArgs& a);
-int launch_perm_bin_33_36(int n, const PermBinArgs& a);
-int launch_perm_bin_37_40(int n, const PermBinArgs& a);
+int launch_perm_bin_1_12(int n, const PermBinArgs& a, PermNode* node);
+int launch_perm_bin_13_20(int n, const PermBinArgs& a, PermNode* node);
+int launch_perm_bin_21_26(int n, const PermBinArgs& a, PermNode* node);
+int launch_perm_bin_27_32(int n, const PermBinArgs& a, PermNode* node);
+int launch_perm_bin_33_36(int n, const PermBinArgs& a, PermNode* node);
+int launch_perm_bin_37_40(int n, const PermBinArgs& a, PermNode* node);
 
 constexpr int kPermMaxN = 40;
 

@@ -194,13 +194,28 @@ def sequences_to_counts(seq: np.ndarray, m: int) -> np.ndarray:
     return out
 
 
+_PERM_PLANS: dict = {}
+
+
+def _perm_plan(S: int, n: int) -> "_native.PermPlan":
+    """Cached permanent plan (one CUDA graph) for S packed n x n matrices: proposal
+    batches repeat the same shape every round."""
+    key = (S, n, torch.cuda.current_device())
+    plan = _PERM_PLANS.get(key)
+    if plan is None:
+        if len(_PERM_PLANS) >= 8:
+            _PERM_PLANS.pop(next(iter(_PERM_PLANS))).close()
+        plan = _native.PermPlan(np.arange(S, dtype=np.int64) * n * n, np.full(S, n, np.int32))
+        _PERM_PLANS[key] = plan
+    return plan
+
+
 def log_abs_perm2(U_dev: torch.Tensor, cols: np.ndarray, seq: torch.Tensor) -> np.ndarray:
     """log |Perm(U[seq_s, cols])|^2 for every sequence (exact float-float permanents)."""
     S, n = seq.shape
     colsd = torch.as_tensor(cols, dtype=torch.long, device=U_dev.device)
     mats = U_dev[seq.long()][:, :, colsd].contiguous()  # S x n x n
-    out = torch.empty(S, dtype=torch.complex128, device=U_dev.device)
-    _native.permanent_batch(mats.view(-1), np.arange(S, dtype=np.int64) * n * n, np.full(S, n, np.int32), out)
+    out = _perm_plan(S, n)(mats.view(-1))
     a = out.abs().cpu().numpy()
     with np.errstate(divide="ignore"):
         return 2.0 * np.log(a)
