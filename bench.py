@@ -455,6 +455,21 @@ def secondary(torch, _native, random_unitary, dev, flush):
         torch.cuda.synchronize()
         return (time.perf_counter() - t0) / reps * 1e6
 
+    # Gurvits estimates (NaiveApprox): 1000 Haar submatrices n = 20, 10^4 draws each;
+    # a draw is 2n^2 real FMAs of column sums plus n complex products (FP32)
+    rng2 = np.random.default_rng(11)
+    gm = np.stack([Ubig[np.ix_(rng2.choice(1024, 20, False), rng2.choice(1024, 20, False))] for _ in range(1000)])
+    gd = torch.from_numpy(gm.reshape(-1)).to(dev)
+    g_offs = np.arange(1000, dtype=np.int64) * 400
+    g_sizes = np.full(1000, 20, dtype=np.int32)
+    g_out = torch.empty(1000, dtype=torch.complex128, device=dev)
+    g_err = torch.empty(1000, dtype=torch.float64, device=dev)
+    g_iters = 10000
+    t_g = timed(lambda: _native.permanent_estimate_batch(gd, g_offs, g_sizes, g_out, g_err, g_iters, 1, 0), reps=3)
+    draws = 1000 * g_iters
+    res["gurvits_1000x20_1e4"] = {"ms": t_g, "draws_per_s": draws / (t_g * 1e-3),
+                                  "fp32_tflops": draws * (4 * 20 * 20 + 6 * 20) / (t_g * 1e-3) / 1e12,
+                                  "median_err_bound": float(g_err.median())}
     res["perm_1000x6_latency"] = {"batch_call_us": wall_us(lambda: _native.permanent_batch(sd, s_offs, s_sizes, so)),
                                   "plan_graph_us": wall_us(lambda: small_plan(sd, so))}
     return res
@@ -540,6 +555,14 @@ def profile_case(name: str):
         plan = _native.SlosPlan(16, [1] * 8 + [0] * 8, batch=256, keep_layers=True)
         plan.forward(clements_mesh_unitary(ph, 16).contiguous().to(dev))
         plan.backward(torch.ones(plan.count * 256, dtype=torch.float64, device=dev))
+    elif name == "gurvits20":
+        U = random_unitary(1024, seed=0)
+        rng = np.random.default_rng(11)
+        gm = np.stack([U[np.ix_(rng.choice(1024, 20, False), rng.choice(1024, 20, False))] for _ in range(1000)])
+        out = torch.empty(1000, dtype=torch.complex128, device=dev)
+        err = torch.empty(1000, dtype=torch.float64, device=dev)
+        _native.permanent_estimate_batch(torch.from_numpy(gm.reshape(-1)).to(dev), np.arange(1000) * 400,
+                                         np.full(1000, 20), out, err, 10000, 1, 0)
     elif name == "cc2017":
         U4 = torch.from_numpy(random_unitary(400, seed=0)).to(dev)
         _native.cc2017_sample(U4, [1] * 20 + [0] * 380, 608, seed=1)
@@ -559,7 +582,7 @@ def main():
     ap.add_argument("--learned", action="store_true",
                     help="run the learned-proposal sampler workload (n=30, m=900 and n=8, m=64) and exit")
     ap.add_argument("--learned-train", type=int, default=2048, help="exact training samples at n=30")
-    ap.add_argument("--profile-case", choices=["perm24", "slos20", "slos16b256", "cc2017"],
+    ap.add_argument("--profile-case", choices=["perm24", "slos20", "slos16b256", "cc2017", "gurvits20"],
                     help="run one small untimed case of a single kernel (for ncu) and exit")
     args = ap.parse_args()
     if args.profile_case:

@@ -68,6 +68,19 @@ int pcvl_permanent_batch(const double* mats_d, const int64_t* offsets_h, const i
 int pcvl_permanent_batch_noalloc(const double* mats_d, const int64_t* offsets_h, const int32_t* sizes_h,
                                  int32_t count, double* out_d, int32_t method, void* stream);
 
+/* Monte-Carlo permanent estimates.  Replaces xq.estimate_permanent_cx(M, iterations),
+ * which returns (estimate, error) to NaiveApproxBackend (perceval/backends/_naive_approx.py:52-59).
+ * Matrices are packed as for pcvl_permanent_batch (0 <= n <= 40).  out_d[i]
+ * (complex128) = mean of `iterations` Gurvits draws X(x) = prod_i x_i prod_j
+ * (sum_i x_i a_ij), x uniform on {-1,+1}^n; err_d[i] (double) = a 99% error bound from
+ * Hoeffding's inequality on the real and imaginary parts, B sqrt(4 ln 400 / iterations),
+ * with B >= ||A||_2^n from a rigorous spectral-norm bound.  Draw k of matrix i uses
+ * Philox4x32-10 with key = seed and counter index first_sample + i * iterations + k.
+ * n = 0 gives 1 and n = 1 the element itself, both with error 0 (exact). */
+int pcvl_permanent_estimate_batch(const double* mats_d, const int64_t* offsets_h, const int32_t* sizes_h,
+                                  int32_t count, int64_t iterations, uint64_t seed, uint64_t first_sample,
+                                  double* out_d, double* err_d, void* stream);
+
 /* Launch-shape tuning of the permanent kernels (no reference counterpart; written by the
  * autotuner in perceval_gb300/autotune.py).  For method (0 Glynn, 1 Ryser) and size n:
  * lo_bits = sign bits every thread enumerates from the shared-memory table (-1: built-in

@@ -58,6 +58,8 @@ def lib():
         L.oracle_slos_grad.argtypes = [i32, vp, vp, vp, vp]
         L.oracle_philox.argtypes = [ctypes.c_uint32] * 6 + [vp]
         L.oracle_cc2017.argtypes = [vp, i32, vp, i64, u64, u64, vp]
+        L.oracle_glynn_term.argtypes = [i32, vp, vp, vp]
+        L.oracle_gurvits.argtypes = [i32, vp, i64, u64, u64, vp]
         L.oracle_num_threads.restype = i32
         L.oracle_set_threads.argtypes = [i32]
         _lib = L
@@ -163,6 +165,25 @@ def cc2017(U, input_state, count: int, seed: int, first: int = 0) -> np.ndarray:
     lib().oracle_cc2017(U.ctypes.data, len(s), s.ctypes.data, int(count), int(seed) & (2**64 - 1), int(first),
                         out.ctypes.data)
     return out
+
+
+def glynn_term(a, x_bits: int) -> complex:
+    """One Gurvits draw X(x) for the sign vector whose set bits are the -1 entries."""
+    a = _c128(a)
+    w = np.array([x_bits & 0xffffffff, (x_bits >> 32) & 0xffffffff], dtype=np.uint32)
+    out = np.zeros(2)
+    lib().oracle_glynn_term(a.shape[0], a.ctypes.data, w.ctypes.data, out.ctypes.data)
+    return complex(out[0], out[1])
+
+
+def gurvits(a, iterations: int, seed: int, first: int = 0) -> complex:
+    """Mean of `iterations` draws with the GPU estimator's Philox stream (draw k has
+    global index first + k)."""
+    a = _c128(a)
+    out = np.zeros(2)
+    lib().oracle_gurvits(a.shape[0], a.ctypes.data, int(iterations), int(seed) & (2**64 - 1), int(first),
+                         out.ctypes.data)
+    return complex(out[0], out[1])
 
 
 # ---------------------------------------------------------------- brute force

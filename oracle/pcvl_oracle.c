@@ -12,7 +12,10 @@
  *    :93-99, normalisation :187-214);
  *  - Clifford & Clifford (2018) algorithm B: perceval/backends/_clifford2017.py,
  *    docs/source/backends.rst:104-116, with the same Philox4x32-10 stream and
- *    draw procedure as the GPU sampler so samples can be compared one by one.
+ *    draw procedure as the GPU sampler so samples can be compared one by one;
+ *  - Gurvits' randomised permanent estimator (xq.estimate_permanent_cx, called at
+ *    perceval/backends/_naive_approx.py:52-59; docs/source/backends.rst:182-187), with
+ *    the same sign draws as the GPU estimator.
  * Fock states of n photons on m modes are ranked in descending lexicographic order
  * (tests/utils/test_statevector.py:430-438).
  */
@@ -478,6 +481,45 @@ void oracle_cc2017(const double* U_, int m, const int* in, int64_t count, uint64
     for (int k = 0; k < n; ++k) o[rows[k]]++;
   }
   free(cols0);
+}
+
+/* ---------------------------------------------------------------- Gurvits estimator */
+/* One draw: X(x) = (prod_i x_i) prod_j (sum_i x_i a_ij), x_i = -1 where bit i of the
+ * 128-bit word w is set (w[0] bits 0..31, w[1] bits 32..63). */
+void oracle_glynn_term(int n, const double* a_, const uint32_t* w, double* out) {
+  const cplx* a = (const cplx*)a_;
+  int par = 0;
+  cplx prod = 1;
+  for (int i = 0; i < n; ++i) par ^= (int)((w[i >> 5] >> (i & 31)) & 1u);
+  for (int j = 0; j < n; ++j) {
+    cplx y = 0;
+    for (int i = 0; i < n; ++i) {
+      const double sgn = ((w[i >> 5] >> (i & 31)) & 1u) ? -1.0 : 1.0;
+      y += sgn * a[i * n + j];
+    }
+    prod *= y;
+  }
+  if (par) prod = -prod;
+  out[0] = creal(prod);
+  out[1] = cimag(prod);
+}
+
+/* Mean of `iterations` draws; draw k has global index first + k and takes its signs
+ * from Philox4x32-10 with key = seed and counter (index lo, index hi, 0x67757276, 0). */
+void oracle_gurvits(int n, const double* a, int64_t iterations, uint64_t seed, uint64_t first, double* out) {
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  double sr = 0, cr = 0, si = 0, ci = 0;
+  for (int64_t k = 0; k < iterations; ++k) {
+    const uint64_t idx = first + (uint64_t)k;
+    const u4 r = philox((u4){(uint32_t)idx, (uint32_t)(idx >> 32), 0x67757276u, 0u}, k0, k1);
+    const uint32_t w[2] = {r.x, r.y};
+    double x[2];
+    oracle_glynn_term(n, a, w, x);
+    neumaier(&sr, &cr, x[0]);
+    neumaier(&si, &ci, x[1]);
+  }
+  out[0] = (sr + cr) / (double)iterations;
+  out[1] = (si + ci) / (double)iterations;
 }
 
 int oracle_num_threads(void) {

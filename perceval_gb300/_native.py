@@ -25,6 +25,10 @@ SYMBOLS = {
     "pcvl_permanent_batch_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                     ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
                                                     ctypes.c_void_p]),
+    "pcvl_permanent_estimate_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                     ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64,
+                                                     ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
+                                                     ctypes.c_void_p]),
     "pcvl_perm_set_tuning": (ctypes.c_int, [ctypes.c_int32] * 4),
     "pcvl_perm_get_tuning": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
                                             ctypes.POINTER(ctypes.c_int32)]),
@@ -155,6 +159,29 @@ def permanent_batch_noalloc(mats: torch.Tensor, offsets: np.ndarray, sizes: np.n
                                            out.data_ptr(), int(method), _stream_ptr(stream)),
           "pcvl_permanent_batch_noalloc")
     return out
+
+
+def permanent_estimate_batch(mats: torch.Tensor, offsets: np.ndarray, sizes: np.ndarray, out: torch.Tensor,
+                             err: torch.Tensor, iterations: int, seed: int, first_sample: int = 0,
+                             stream=None) -> tuple[torch.Tensor, torch.Tensor]:
+    """Gurvits estimates of packed permanents and their 99% error bounds
+    (see pcvl_permanent_estimate_batch)."""
+    lib = load()
+    _dev_tensor(mats, torch.complex128, "mats")
+    _dev_tensor(out, torch.complex128, "out")
+    _dev_tensor(err, torch.float64, "err")
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+    count = int(sizes.shape[0])
+    if offsets.shape[0] != count or out.numel() < count or err.numel() < count:
+        raise ValueError("offsets, sizes, out and err must describe the same number of matrices")
+    if count and int((offsets + sizes.astype(np.int64) ** 2).max()) > mats.numel():
+        raise ValueError("a matrix extends beyond the end of mats")
+    check(lib.pcvl_permanent_estimate_batch(mats.data_ptr(), offsets.ctypes.data, sizes.ctypes.data, count,
+                                            int(iterations), int(seed) & (2**64 - 1), int(first_sample),
+                                            out.data_ptr(), err.data_ptr(), _stream_ptr(stream)),
+          "pcvl_permanent_estimate_batch")
+    return out, err
 
 
 def set_perm_tuning(method: int, n: int, lo_bits: int = -1, ctas_per_sm: int = 0):

@@ -1,19 +1,21 @@
 """Backend registry and factory (perceval/backends/__init__.py:39-62).
 
 ``BackendFactory.get_backend(name)`` returns a GPU backend for the names of the hot
-path ("SLOS", "Naive", "CliffordClifford2017"); an unknown name logs a warning and
-falls back to SLOS, as in the reference.
+path ("SLOS", "Naive", "NaiveApprox", "CliffordClifford2017"); an unknown name logs a
+warning and falls back to SLOS, as in the reference.
 """
 import logging
 
 from ._abstract_backends import ABackend, ASamplingBackend, AStrongSimulationBackend
 from ._clifford2017 import Clifford2017Backend
 from ._naive import NaiveBackend
+from ._naive_approx import NaiveApproxBackend
 from ._slos import SLOSBackend
 
 BACKEND_LIST = {
     "CliffordClifford2017": Clifford2017Backend,
     "Naive": NaiveBackend,
+    "NaiveApprox": NaiveApproxBackend,
     "SLOS": SLOSBackend,
 }
 
@@ -33,4 +35,4 @@ class BackendFactory:
 
 
 __all__ = ["ABackend", "ASamplingBackend", "AStrongSimulationBackend", "BACKEND_LIST", "BackendFactory",
-           "Clifford2017Backend", "NaiveBackend", "SLOSBackend"]
+           "Clifford2017Backend", "NaiveApproxBackend", "NaiveBackend", "SLOSBackend"]

@@ -66,11 +66,16 @@ class NaiveBackend(AStrongSimulationBackend):
             where.append(i)
             norms.append(math.sqrt(s.prodnfact() * pin))
         if where:
-            dev = torch.from_numpy(np.concatenate(mats)).to("cuda")
-            out = torch.empty(len(where), dtype=torch.complex128, device="cuda")
-            _native.permanent_batch(dev, np.array(offs), np.array(sizes), out, self._method)
-            res[np.array(where)] = out.cpu().numpy() / np.array(norms)
+            perms = self._permanents(np.concatenate(mats), np.array(offs), np.array(sizes))
+            res[np.array(where)] = perms / np.array(norms)
         return res
+
+    def _permanents(self, flat: np.ndarray, offs: np.ndarray, sizes: np.ndarray) -> np.ndarray:
+        """Permanents of packed matrices, one batched launch (_naive.py:70-71)."""
+        dev = torch.from_numpy(flat).to("cuda")
+        out = torch.empty(len(sizes), dtype=torch.complex128, device="cuda")
+        _native.permanent_batch(dev, offs, sizes, out, self._method)
+        return out.cpu().numpy()
 
     def all_prob(self, input_state=None):
         if input_state is not None:
