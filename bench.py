@@ -436,6 +436,32 @@ def secondary(torch, _native, random_unitary, dev, flush):
     nb.prob_amplitudes(outs)
     t_naive = time.perf_counter() - t0
     res["small_m12_n6"] = {"slos_all_prob_ms": t_slos * 1e3, "outputs": len(p), "naive_1000_amplitudes_ms": t_naive * 1e3}
+    # many input states of one circuit (the per-input loop of Simulator._probs_svd_fast):
+    # 500 distinct 6-photon inputs on m = 12, one batched plan against one plan per input
+    rng3 = np.random.default_rng(4)
+    many = set()
+    while len(many) < 500:
+        st = np.zeros(12, dtype=int)
+        np.add.at(st, rng3.integers(0, 12, 6), 1)
+        many.add(tuple(int(v) for v in st))
+    many = [BasicState(list(st)) for st in sorted(many)]
+    bm = BackendFactory.get_backend("SLOS")
+    bm.set_circuit(U12)
+    bm.all_probs_many(many[:8])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pm = bm.all_probs_many(many)
+    t_many = time.perf_counter() - t0
+    bl = BackendFactory.get_backend("SLOS")
+    bl.set_circuit(U12)
+    t0 = time.perf_counter()
+    dev_max = 0.0
+    for st, pref in zip(many, pm):
+        bl.set_input_state(st)
+        dev_max = max(dev_max, float(np.abs(np.asarray(bl.all_prob()) - pref).max()))
+    t_loop = time.perf_counter() - t0
+    res["slos_500_inputs_m12_n6"] = {"batched_ms": t_many * 1e3, "per_input_loop_ms": t_loop * 1e3,
+                                     "max_abs_diff": dev_max}
     # launch latency of a small batch (1000 permanents of 6x6 Haar submatrices): the
     # plan-free call against one graph launch of a plan, wall clock per call
     sub = np.stack([U12[np.ix_(rng.choice(12, 6, replace=False), rng.choice(12, 6, replace=False))]

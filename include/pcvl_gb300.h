@@ -127,6 +127,14 @@ typedef struct pcvl_slos_plan pcvl_slos_plan;
 
 int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int32_t* input_state_h,
                           int32_t batch, int32_t keep_layers);
+/* Plan whose `batch` entries each have their own input state (input_states_h: batch x m,
+ * host; every state must hold the same photon count).  No reference counterpart as one
+ * call: it batches the per-input-state loop of Simulator._probs_svd_fast
+ * (perceval/simulators/simulator.py:412-514), which calls set_input_state +
+ * prob_iterator once per distinct input.  Entry b's outputs are normalised by its own
+ * prod(in_b!). */
+int pcvl_slos_plan_create_multi(pcvl_slos_plan** plan, int32_t m, const int32_t* input_states_h,
+                                int32_t batch, int32_t keep_layers);
 int pcvl_slos_plan_destroy(pcvl_slos_plan* plan);
 /* Number of output states C(m+n-1, n) of the plan. */
 int pcvl_slos_output_count(const pcvl_slos_plan* plan, int64_t* count);
@@ -135,6 +143,8 @@ int pcvl_slos_plan_bytes(const pcvl_slos_plan* plan, int64_t* bytes);
 /* Propagates the input state through u_d (batch x m x m complex128, row = output
  * mode, column = input mode, circuit-major). */
 int pcvl_slos_forward(pcvl_slos_plan* plan, const double* u_d, void* stream);
+/* Same, with one m x m unitary u_d shared by every entry of the plan. */
+int pcvl_slos_forward_shared(pcvl_slos_plan* plan, const double* u_d, void* stream);
 /* probs_d[r * batch + b] = |c|^2 * prod(out!) / prod(in!)   (float64; state-major,
  * circuit innermost) */
 int pcvl_slos_probabilities(pcvl_slos_plan* plan, double* probs_d, void* stream);

@@ -39,7 +39,10 @@ SYMBOLS = {
     "pcvl_perm_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "pcvl_slos_plan_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.c_void_p,
                                              ctypes.c_int32, ctypes.c_int32]),
+    "pcvl_slos_plan_create_multi": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
+                                                   ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
     "pcvl_slos_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "pcvl_slos_forward_shared": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "pcvl_slos_output_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     "pcvl_slos_plan_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     "pcvl_slos_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
@@ -248,19 +251,31 @@ class PermPlan:
 
 # ------------------------------------------------------------------ SLOS
 class SlosPlan:
-    """Owner of a ``pcvl_slos_plan``: fixed (m, input state, batch)."""
+    """Owner of a ``pcvl_slos_plan``: fixed (m, input state(s), batch).
+
+    ``input_state`` is one state shared by the ``batch`` entries, or a (batch x m)
+    array of per-entry states with one photon count (``pcvl_slos_plan_create_multi``).
+    """
 
     def __init__(self, m: int, input_state, batch: int = 1, keep_layers: bool = False):
         self._lib = load()
         inp = np.ascontiguousarray(input_state, dtype=np.int32)
-        if inp.shape != (m,):
-            raise ValueError("input_state must have m entries")
         h = ctypes.c_void_p()
-        check(self._lib.pcvl_slos_plan_create(ctypes.byref(h), int(m), inp.ctypes.data, int(batch),
-                                              1 if keep_layers else 0), "pcvl_slos_plan_create")
+        if inp.ndim == 2:
+            if inp.shape[1] != m or inp.shape[0] < 1:
+                raise ValueError("input states must form a (batch x m) array")
+            batch = inp.shape[0]
+            check(self._lib.pcvl_slos_plan_create_multi(ctypes.byref(h), int(m), inp.ctypes.data, int(batch),
+                                                        1 if keep_layers else 0), "pcvl_slos_plan_create_multi")
+            self.input_state = [tuple(int(v) for v in row) for row in inp]
+        else:
+            if inp.shape != (m,):
+                raise ValueError("input_state must have m entries")
+            check(self._lib.pcvl_slos_plan_create(ctypes.byref(h), int(m), inp.ctypes.data, int(batch),
+                                                  1 if keep_layers else 0), "pcvl_slos_plan_create")
+            self.input_state = tuple(int(v) for v in inp)
         self._h = h
         self.m, self.batch, self.keep_layers = m, batch, keep_layers
-        self.input_state = tuple(int(v) for v in inp)
         c = ctypes.c_int64()
         check(self._lib.pcvl_slos_output_count(h, ctypes.byref(c)), "pcvl_slos_output_count")
         self.count = int(c.value)
@@ -272,10 +287,16 @@ class SlosPlan:
         return int(b.value)
 
     def forward(self, u: torch.Tensor, stream=None):
+        """Propagate: ``u`` holds batch x m x m unitaries, or one m x m unitary shared by
+        every entry."""
         _dev_tensor(u, torch.complex128, "u")
-        if u.numel() != self.batch * self.m * self.m:
-            raise ValueError("u must hold batch x m x m elements")
-        check(self._lib.pcvl_slos_forward(self._h, u.data_ptr(), _stream_ptr(stream)), "pcvl_slos_forward")
+        if u.numel() == self.batch * self.m * self.m:
+            check(self._lib.pcvl_slos_forward(self._h, u.data_ptr(), _stream_ptr(stream)), "pcvl_slos_forward")
+        elif u.numel() == self.m * self.m:
+            check(self._lib.pcvl_slos_forward_shared(self._h, u.data_ptr(), _stream_ptr(stream)),
+                  "pcvl_slos_forward_shared")
+        else:
+            raise ValueError("u must hold batch x m x m or m x m elements")
 
     def probabilities(self, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
         if out is None:

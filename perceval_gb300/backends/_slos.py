@@ -9,6 +9,12 @@ recomputes their coefficients (_slos.py:130-141); a different size resets them.
 Outputs come back in descending-lexicographic order (the reference's
 ``allstate_iterator`` order).  ``all_prob`` returns a list up to 2^22 outputs and a
 numpy array above; ``all_prob_tensor`` leaves the probabilities on the device.
+
+``all_probs_many`` / ``prob_distributions`` evaluate many input states of the circuit
+at once (the per-input loop of Simulator._probs_svd_fast, simulator.py:454-468): states
+with the same photon count share every layer's Fock space, so each such group runs as
+one batched plan whose entries add their own input modes, one launch per photon layer
+for the whole group.
 """
 from __future__ import annotations
 
@@ -108,11 +114,56 @@ class SLOSBackend(AStrongSimulationBackend):
             e.amps = e.plan.amplitudes()
         return e.amps
 
-    def _mask_indices(self) -> np.ndarray | None:
+    def _mask_indices(self, m: int | None = None, n: int | None = None) -> np.ndarray | None:
         if self._mask is None:
             return None
-        arr = fock_space_array(self._input_state.m, self._input_state.n)
+        if m is None:
+            m, n = self._input_state.m, self._input_state.n
+        arr = fock_space_array(m, n)
         return np.nonzero(self._mask.match_array(arr))[0]
+
+    def all_probs_many(self, input_states, max_device_bytes: int = 1 << 31) -> list[np.ndarray]:
+        """Probabilities of every output (descending-lexicographic order, mask applied)
+        for each of ``input_states``, evaluated as batched plans grouped by photon count."""
+        assert self._circuit is not None, "set_circuit first"
+        states = [FockState(s) for s in input_states]
+        m = self._circuit.m
+        groups: dict[int, list[int]] = {}
+        for i, s in enumerate(states):
+            assert s.m == m, "input state size mismatch"
+            groups.setdefault(s.n, []).append(i)
+        U = self._unitary_device()
+        res: list = [None] * len(states)
+        for n, idxs in sorted(groups.items()):
+            count = math.comb(m + n - 1, n)
+            # two float-float layers per entry dominate a plan's memory
+            per_entry = 2 * 16 * max(count, 1)
+            step = max(1, min(len(idxs), max_device_bytes // per_entry))
+            sel = self._mask_indices(m, n)
+            for c0 in range(0, len(idxs), step):
+                chunk = idxs[c0:c0 + step]
+                arr = np.array([list(states[i]) for i in chunk], dtype=np.int32)
+                plan = _native.SlosPlan(m, arr, keep_layers=False)
+                try:
+                    plan.forward(U)
+                    host = plan.probabilities().view(plan.count, len(chunk)).cpu().numpy()
+                finally:
+                    plan.close()
+                for col, i in enumerate(chunk):
+                    p = np.ascontiguousarray(host[:, col])
+                    res[i] = p if sel is None else p[sel]
+        return res
+
+    def prob_distributions(self, input_states) -> list[BSDistribution]:
+        """``prob_distribution`` of each input state, computed by ``all_probs_many``."""
+        states = [FockState(s) for s in input_states]
+        out = []
+        for s, probs in zip(states, self.all_probs_many(states)):
+            bsd = BSDistribution()
+            for o, p in zip(self._get_iterator(s), probs):
+                bsd.add(o, p)
+            out.append(bsd)
+        return out
 
     def all_prob(self, input_state=None):
         if input_state is not None:

@@ -36,6 +36,12 @@
 // B == 1 the lanes take consecutive states; with B >= 2 the lanes take 32 circuits
 // of one state (blockIdx.y selects the 32-circuit chunk), so loads are coalesced
 // across circuits and the index work is shared by the 32 lanes.
+//
+// Batch entries.  Entry b of a plan has its own unitary U_b and its own input state
+// (all with the same photon count n: every layer is the same Fock space).  Layer k of
+// entry b adds a photon in input mode col[k][b] (its own _Path order), so the layer
+// reads u_j(b) = U_b[j, col[k][b]]; the normalisation 1 / prod(in_b!) is per entry.  A
+// plan for one input state is the case where every entry has the same columns.
 #include <algorithm>
 #include <cstring>
 #include <new>
@@ -63,6 +69,7 @@ struct SlosArgs {
   int cn_stride;
   const uint32_t* tail;   // TP (forward) or TC (adjoint)
   const dd* ftail;        // prod tau_j! per tail state
+  const dd* inv_in;       // 1 / prod(in_b!) per batch entry
   const uint8_t* tocc;    // occupied tail modes per tail state (bit j)
   uint32_t tail_off[kSlosMaxN + 2];    // entry offset of the block of r tail photons
   uint32_t tstate_off[kSlosMaxN + 2];  // state offset of that block
@@ -447,45 +454,51 @@ __global__ void __launch_bounds__(256) slos_fin(SlosArgs a, dd inv_in, int mode,
       const uint32_t chunk = batched ? kChunkB : kChunk;
       const uint32_t t0 = ch * chunk, t1 = min(S, t0 + chunk);
       if (batched) {
-        if (b < a.B)
+        if (b < a.B) {
+          const dd fb = dd_mul(d.f, a.inv_in[b]);
           for (uint32_t tau = t0; tau < t1; ++tau)
-            fin_state(a, d.f, r, (size_t)(d.A + tau) * a.B + b, mode, w_in, out_real, out_c, seed, tau);
+            fin_state(a, fb, r, (size_t)(d.A + tau) * a.B + b, mode, w_in, out_real, out_c, seed, tau);
+        }
       } else {
+        const dd fb = dd_mul(d.f, a.inv_in[0]);
         for (uint32_t tau = t0 + lane; tau < t1; tau += 32)
-          fin_state(a, d.f, r, d.A + tau, mode, w_in, out_real, out_c, seed, tau);
+          fin_state(a, fb, r, d.A + tau, mode, w_in, out_real, out_c, seed, tau);
       }
     } else {
       const uint32_t pi = lu * 32 + lane;
       if (pi < a.npf[r]) {
         describe<MMAX, false, true>(pi, q, r, a, cn, d, inv_in, d.base);
-        for (uint32_t tau = 0; tau < S; ++tau) fin_state(a, d.f, r, d.A + tau, mode, w_in, out_real, out_c, seed, tau);
+        const dd fb = dd_mul(d.f, a.inv_in[0]);
+        for (uint32_t tau = 0; tau < S; ++tau) fin_state(a, fb, r, d.A + tau, mode, w_in, out_real, out_c, seed, tau);
       }
     }
   }
 }
 
-// grad[b][j][mk] += sum over CTAs of gpart[cta][j][b]
-__global__ void slos_grad_reduce(const cdd* __restrict__ gpart, int nblk, int m, int B, int mk,
-                                 double2* __restrict__ grad) {
+// grad[b][j][col[b]] += sum over CTAs of gpart[cta][j][b]  (col: the layer's column per entry)
+__global__ void slos_grad_reduce(const cdd* __restrict__ gpart, int nblk, int m, int B,
+                                 const int32_t* __restrict__ col, double2* __restrict__ grad) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;  // i = j * B + b
   if (i >= m * B) return;
   const int j = i / B, b = i - j * B;
   cdd s = cdd_zero();
   for (int q = 0; q < nblk; ++q) s = cdd_add(s, gpart[(size_t)q * m * B + i]);
-  double2* g = &grad[((size_t)b * m + j) * m + mk];
+  double2* g = &grad[((size_t)b * m + j) * m + col[b]];
   g->x += dd_to_double(s.re);
   g->y += dd_to_double(s.im);
 }
 
-// ucol[mk][j][b] = U_b[j][mk] as float-float, for every column mk
-__global__ void slos_convert_u(const double2* __restrict__ u, int m, int B, cdd* __restrict__ ucols) {
-  const size_t tot = (size_t)B * m * m;
+// ucols[k][j][b] = U_b[j][col[k][b]] as float-float, for the n layers (ustride: elements
+// between consecutive entries' unitaries; 0 = one unitary shared by every entry)
+__global__ void slos_convert_u(const double2* __restrict__ u, int m, int n, int B, size_t ustride,
+                               const int32_t* __restrict__ col, cdd* __restrict__ ucols) {
+  const size_t tot = (size_t)n * m * B;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
-    const size_t b = i / ((size_t)m * m);
-    const int rem = (int)(i - b * m * m);
-    const int j = rem / m, col = rem - j * m;
-    const double2 v = u[i];
-    ucols[((size_t)col * m + j) * B + b] = cdd_from(v.x, v.y);
+    const size_t kj = i / B;
+    const int b = (int)(i - kj * B);
+    const int k = (int)(kj / m), j = (int)(kj - (size_t)k * m);
+    const double2 v = u[(size_t)b * ustride + (size_t)j * m + col[(size_t)k * B + b]];
+    ucols[i] = cdd_from(v.x, v.y);
   }
 }
 
@@ -546,13 +559,14 @@ using namespace pcvl;
 struct pcvl_slos_plan {
   int m = 0, n = 0, B = 0;
   bool keep = false;
-  std::vector<int> input;
-  std::vector<int> order;         // input mode of photon k (k = 1..n) -> order[k-1]
+  std::vector<int> inputs;        // B x m input states (same photon count)
+  std::vector<int32_t> col;       // n x B: input mode of photon k of entry b -> col[(k-1) * B + b]
   std::vector<uint64_t> sizes;    // layer sizes, k = 0..n
-  double prodfact_in = 1.0;
   int cn_stride = 0;
   uint32_t* cn_d = nullptr;
-  cdd* ucols_d = nullptr;         // [col][j][b]
+  int32_t* col_d = nullptr;
+  dd* inv_in_d = nullptr;         // 1 / prod(in_b!) per entry
+  cdd* ucols_d = nullptr;         // [k][j][b]
   std::vector<cdd*> layers;       // keep: every layer; else layers[k % 2] ping-pong
   cdd* adj_d[2] = {nullptr, nullptr};
   cdd* gpart_d = nullptr;
@@ -573,6 +587,8 @@ namespace {
 void free_plan(pcvl_slos_plan* p) {
   if (!p) return;
   cudaFree(p->cn_d);
+  cudaFree(p->col_d);
+  cudaFree(p->inv_in_d);
   cudaFree(p->ucols_d);
   for (cdd* l : p->layers) cudaFree(l);
   cudaFree(p->adj_d[0]);
@@ -697,6 +713,7 @@ SlosArgs make_args(const pcvl_slos_plan* p, int k) {
   a.cn = p->cn_d;
   a.cn_stride = p->cn_stride;
   a.ftail = p->ftail_d;
+  a.inv_in = p->inv_in_d;
   a.tocc = p->tocc_d;
   for (int r = 0; r <= p->n + 1; ++r) {
     a.tail_off[r] = p->tail_off[r];
@@ -735,16 +752,22 @@ int grid_for_units(const SlosArgs& a) {
 
 }  // namespace
 
-extern "C" int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int32_t* input_state_h,
-                                     int32_t batch, int32_t keep_layers) {
-  PCVL_CHECK(plan && input_state_h, "null pointer argument");
+// Plan for `batch` entries with input states inputs[b * m .. b * m + m - 1].
+static int create_plan(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, int32_t batch, int32_t keep_layers) {
+  PCVL_CHECK(plan && inputs, "null pointer argument");
   *plan = nullptr;
   PCVL_CHECK(m >= 1 && m <= kSlosMaxM, "m=%d outside [1, %d]", m, kSlosMaxM);
   PCVL_CHECK(batch >= 1, "batch must be >= 1");
-  int n = 0;
-  for (int i = 0; i < m; ++i) {
-    PCVL_CHECK(input_state_h[i] >= 0, "negative photon count in input state");
-    n += input_state_h[i];
+  int n = -1;
+  for (int b = 0; b < batch; ++b) {
+    int nb = 0;
+    for (int i = 0; i < m; ++i) {
+      PCVL_CHECK(inputs[(size_t)b * m + i] >= 0, "negative photon count in input state %d", b);
+      nb += inputs[(size_t)b * m + i];
+    }
+    PCVL_CHECK(n < 0 || nb == n, "input state %d has %d photons, state 0 has %d: a plan needs one photon count", b,
+               nb, n);
+    n = nb;
   }
   PCVL_CHECK(n <= kSlosMaxN, "n=%d photons exceeds %d", n, kSlosMaxN);
 
@@ -754,10 +777,18 @@ extern "C" int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int
   p->n = n;
   p->B = batch;
   p->keep = keep_layers != 0;
-  p->input.assign(input_state_h, input_state_h + m);
-  p->order = path_order(p->input);
-  for (int i = 0; i < m; ++i)
-    for (int v = 2; v <= p->input[i]; ++v) p->prodfact_in *= v;
+  p->inputs.assign(inputs, inputs + (size_t)batch * m);
+  p->col.assign((size_t)std::max(n, 1) * batch, 0);
+  std::vector<dd> inv_in(batch);
+  for (int b = 0; b < batch; ++b) {
+    const std::vector<int> in(inputs + (size_t)b * m, inputs + (size_t)(b + 1) * m);
+    const std::vector<int> order = path_order(in);
+    for (int k = 0; k < n; ++k) p->col[(size_t)k * batch + b] = order[k];
+    double f = 1.0;
+    for (int i = 0; i < m; ++i)
+      for (int v = 2; v <= in[i]; ++v) f *= v;
+    inv_in[b] = dd_from_double(1.0 / f);
+  }
   p->sizes.resize(n + 1);
   for (int k = 0; k <= n; ++k) {
     p->sizes[k] = fock_count(m, k);
@@ -815,7 +846,12 @@ extern "C" int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int
   if ((rc = upload(p->tocc_d, tocc.data(), tocc.size())) != PCVL_OK) goto fail;
   if ((rc = alloc((void**)&p->ftail_d, ftail.size() * sizeof(dd), p->bytes)) != PCVL_OK) goto fail;
   if ((rc = upload(p->ftail_d, ftail.data(), ftail.size() * sizeof(dd))) != PCVL_OK) goto fail;
-  if ((rc = alloc((void**)&p->ucols_d, (size_t)m * m * B * sizeof(cdd), p->bytes)) != PCVL_OK) goto fail;
+  if ((rc = alloc((void**)&p->col_d, p->col.size() * 4, p->bytes)) != PCVL_OK) goto fail;
+  if ((rc = upload(p->col_d, p->col.data(), p->col.size() * 4)) != PCVL_OK) goto fail;
+  if ((rc = alloc((void**)&p->inv_in_d, B * sizeof(dd), p->bytes)) != PCVL_OK) goto fail;
+  if ((rc = upload(p->inv_in_d, inv_in.data(), B * sizeof(dd))) != PCVL_OK) goto fail;
+  if ((rc = alloc((void**)&p->ucols_d, (size_t)std::max(n, 1) * m * B * sizeof(cdd), p->bytes)) != PCVL_OK)
+    goto fail;
   if (p->keep) {
     p->layers.assign(n + 1, nullptr);
     for (int k = 0; k <= n; ++k)
@@ -842,6 +878,21 @@ fail:
   return rc;
 }
 
+extern "C" int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int32_t* input_state_h,
+                                     int32_t batch, int32_t keep_layers) {
+  PCVL_CHECK(plan && input_state_h, "null pointer argument");
+  PCVL_CHECK(m >= 1 && m <= kSlosMaxM, "m=%d outside [1, %d]", m, kSlosMaxM);
+  PCVL_CHECK(batch >= 1, "batch must be >= 1");
+  std::vector<int32_t> inputs((size_t)batch * m);
+  for (int b = 0; b < batch; ++b) std::copy(input_state_h, input_state_h + m, inputs.begin() + (size_t)b * m);
+  return create_plan(plan, m, inputs.data(), batch, keep_layers);
+}
+
+extern "C" int pcvl_slos_plan_create_multi(pcvl_slos_plan** plan, int32_t m, const int32_t* input_states_h,
+                                           int32_t batch, int32_t keep_layers) {
+  return create_plan(plan, m, input_states_h, batch, keep_layers);
+}
+
 extern "C" int pcvl_slos_plan_destroy(pcvl_slos_plan* plan) {
   free_plan(plan);
   return PCVL_OK;
@@ -859,13 +910,12 @@ extern "C" int pcvl_slos_plan_bytes(const pcvl_slos_plan* plan, int64_t* bytes) 
   return PCVL_OK;
 }
 
-extern "C" int pcvl_slos_forward(pcvl_slos_plan* p, const double* u_d, void* stream_) {
-  PCVL_CHECK(p && u_d, "null pointer argument");
-  cudaStream_t s = (cudaStream_t)stream_;
+static int forward(pcvl_slos_plan* p, const double* u_d, size_t ustride, cudaStream_t s) {
   const int m = p->m, B = p->B;
-  {
-    const int g = (int)std::max<uint64_t>(1, std::min<uint64_t>(((uint64_t)B * m * m + 255) / 256, 4096));
-    slos_convert_u<<<g, 256, 0, s>>>((const double2*)u_d, m, B, p->ucols_d);
+  if (p->n > 0) {
+    const uint64_t tot = (uint64_t)p->n * m * B;
+    const int g = (int)std::max<uint64_t>(1, std::min<uint64_t>((tot + 255) / 256, 4096));
+    slos_convert_u<<<g, 256, 0, s>>>((const double2*)u_d, m, p->n, B, ustride, p->col_d, p->ucols_d);
   }
   PCVL_CUDA(cudaGetLastError());
   slos_fill_vacuum<<<(B + 255) / 256, 256, 0, s>>>(p->layers[0], B);
@@ -874,7 +924,7 @@ extern "C" int pcvl_slos_forward(pcvl_slos_plan* p, const double* u_d, void* str
     SlosArgs a = make_args(p, k);
     a.in = p->keep ? p->layers[k - 1] : p->layers[(k - 1) % 2];
     a.out = p->keep ? p->layers[k] : p->layers[k % 2];
-    a.ucol = p->ucols_d + (size_t)p->order[k - 1] * m * B;
+    a.ucol = p->ucols_d + (size_t)(k - 1) * m * B;
     a.tail = p->tp_d;
     const int rc = dispatch(Kern::Fwd, a, grid_for_units(a), s);
     if (rc != 0) {
@@ -886,12 +936,22 @@ extern "C" int pcvl_slos_forward(pcvl_slos_plan* p, const double* u_d, void* str
   return PCVL_OK;
 }
 
+extern "C" int pcvl_slos_forward(pcvl_slos_plan* p, const double* u_d, void* stream) {
+  PCVL_CHECK(p && u_d, "null pointer argument");
+  return forward(p, u_d, (size_t)p->m * p->m, (cudaStream_t)stream);
+}
+
+extern "C" int pcvl_slos_forward_shared(pcvl_slos_plan* p, const double* u_d, void* stream) {
+  PCVL_CHECK(p && u_d, "null pointer argument");
+  return forward(p, u_d, 0, (cudaStream_t)stream);
+}
+
 static int finalize(pcvl_slos_plan* p, int mode, const double* w, double* out_real, double2* out_c, cdd* seed,
                     cudaStream_t s) {
   PCVL_CHECK(p->forwarded, "pcvl_slos_forward has not run on this plan");
   SlosArgs a = make_args(p, p->n);
   a.in = p->final_layer();
-  const int rc = dispatch(Kern::Fin, a, grid_for_units(a), s, dd_from_double(1.0 / p->prodfact_in),
+  const int rc = dispatch(Kern::Fin, a, grid_for_units(a), s, dd_from_double(1.0),
                           mode, w, out_real, out_c, seed);
   if (rc != 0) {
     set_error("SLOS finalize launch failed: %s", cudaGetErrorString((cudaError_t)rc));
@@ -922,8 +982,7 @@ extern "C" int pcvl_slos_backward(pcvl_slos_plan* p, const double* weights_d, do
     SlosArgs a = make_args(p, k - 1);  // tiles of the parent layer
     a.in = p->adj_d[k % 2];
     a.out = p->adj_d[(k - 1) % 2];
-    const int mk = p->order[k - 1];
-    a.ucol = p->ucols_d + (size_t)mk * m * B;
+    a.ucol = p->ucols_d + (size_t)(k - 1) * m * B;
     a.cpar = p->layers[k - 1];
     a.gpart = p->gpart_d;
     a.tail = p->tc_d;
@@ -933,7 +992,8 @@ extern "C" int pcvl_slos_backward(pcvl_slos_plan* p, const double* weights_d, do
       set_error("SLOS adjoint layer %d launch failed: %s", k, cudaGetErrorString((cudaError_t)rc));
       return PCVL_ERR_CUDA;
     }
-    slos_grad_reduce<<<(m * B + 255) / 256, 256, 0, s>>>(p->gpart_d, grid, m, B, mk, (double2*)grad_u_d);
+    slos_grad_reduce<<<(m * B + 255) / 256, 256, 0, s>>>(p->gpart_d, grid, m, B, p->col_d + (size_t)(k - 1) * B,
+                                                         (double2*)grad_u_d);
     PCVL_CUDA(cudaGetLastError());
   }
   return PCVL_OK;
