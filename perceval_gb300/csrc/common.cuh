@@ -177,6 +177,7 @@ PCVL_HD void cacc_fma(cacc& a, cdd x, cdd y) {
 }
 PCVL_HD cdd cacc_finish(const cacc& a) { return {two_sum(a.rh, a.rl), two_sum(a.ih, a.il)}; }
 
+
 // ------------------------------------------------------------------ Philox4x32-10
 // Counter-based generator of Salmon, Moraes, Dror and Shaw, "Parallel random numbers:
 // as easy as 1, 2, 3" (SC 2011): ten rounds of two 32x32->64 multiplies with the

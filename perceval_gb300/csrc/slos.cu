@@ -80,10 +80,17 @@ struct SlosArgs {
   uint32_t uoff[kSlosMaxN + 2];
   uint32_t npf[kSlosMaxN + 1];
   uint32_t cpt[kSlosMaxN + 1];
+  // units of the single-circuit forward kernel: tiles of >= chunk1 states in chunks of
+  // chunk1 (cpt1 > 0), smaller tiles in groups of grp1 tiles (about chunk1 states)
+  uint32_t chunk1;
+  uint32_t uoff1[kSlosMaxN + 2];
+  uint32_t cpt1[kSlosMaxN + 1];
+  uint32_t grp1[kSlosMaxN + 1];
 };
 
 constexpr uint32_t kChunk = 256;   // states per unit of a large tile (single circuit)
 constexpr uint32_t kChunkB = 8;    // states per unit (batched)
+constexpr uint32_t kChunk1 = 1024; // largest unit of the single-circuit forward kernel (states)
 
 __device__ __forceinline__ uint32_t cn_at(const uint32_t* cn, int stride, int M, int x) {
   return x < 0 ? 0u : cn[M * stride + x];
@@ -249,54 +256,135 @@ __global__ void __launch_bounds__(256) slos_fwdb(SlosArgs a) {
   }
 }
 
-// Single-circuit forward layer.  Every lane keeps its tile's parent offsets in its
-// own shared-memory slot and loops over the set bits of its state's occupation mask
-// (prefix bits from the tile, tail bits from a per-tail-state table), so a warp runs
-// as many multiply-adds as its busiest lane, not one per mode.
+// class of a forward-single unit (uniform across the warp)
+__device__ __forceinline__ int unit_class1(const SlosArgs& a, uint32_t u) {
+  int r = 0;
+  while (r < a.k && a.uoff1[r + 1] <= u) ++r;
+  return r;
+}
+
+// Words per thread of the single-circuit forward kernel's shared slots: the parent
+// offsets of one tile (MMAX) and its A, tb and prefix mask.
+template <int MMAX>
+__host__ __device__ constexpr int fwd1_slot() {
+  return MMAX + 4;
+}
+
+// Single-circuit forward layer.
+//  * Tiles of >= chunk1 states: a unit is chunk1 states of one tile, so the warp shares
+//    the tile.  Lane 0 unranks it into its slot; the prefix modes are a warp-uniform loop
+//    over the tile's mask (parent offsets and u_j are broadcast reads, parent loads
+//    coalesced), then each lane adds its state's tail modes from the tail tables.  A
+//    lane takes two states 32 apart per round, so every broadcast read feeds two
+//    independent load / multiply-add chains.  (Paired f32x2 forms of the float-float
+//    multiply-add were measured slower here: the kernel waits on its gathers.)
+//  * Smaller tiles: a unit is a group of grp1 consecutive tiles (about chunk1 states).
+//    Lane l unranks tile l of the group into its own slot (all lanes at once), then the
+//    warp sweeps the group's states in rank order, one state per lane; each lane loops
+//    over the set bits of its state's occupation (prefix bits from its tile's slot, tail
+//    bits from the table), so a warp runs as many multiply-adds as its busiest lane.
 template <int MMAX>
 __global__ void __launch_bounds__(256) slos_fwd1(SlosArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int SL = fwd1_slot<MMAX>();
   uint32_t* cn;
   const cdd* u = load_shared<MMAX, false, false>(a, smem_raw, cn);
-  uint32_t* sbase = reinterpret_cast<uint32_t*>(smem_raw + smem_cn_bytes(a.m, a.cn_stride) +
-                                                (size_t)MMAX * 32 * sizeof(cdd)) +
-                    (size_t)threadIdx.x * MMAX;
+  uint32_t* slots = reinterpret_cast<uint32_t*>(smem_raw + smem_cn_bytes(a.m, a.cn_stride) +
+                                                (size_t)MMAX * 32 * sizeof(cdd));
   const int lane = threadIdx.x & 31, p = a.p;
-  const uint32_t total = a.uoff[a.k + 1];
+  uint32_t* myslot = slots + (size_t)threadIdx.x * SL;
+  const uint32_t* wslots = slots + (size_t)(threadIdx.x - lane) * SL;  // the warp's 32 slots
+  const uint32_t total = a.uoff1[a.k + 1];
   const uint32_t nw = gridDim.x * kWarps;
   for (uint32_t unit = blockIdx.x * kWarps + (threadIdx.x >> 5); unit < total; unit += nw) {
-    const int r = unit_class(a, unit);
+    const int r = unit_class1(a, unit);
     const int q = a.k - r;
-    const uint32_t S = a.tsize[r], lu = unit - a.uoff[r], cpt = a.cpt[r];
-    uint32_t pi, t0, t1, tstep;
-    if (cpt > 0) {  // one tile, a chunk of its states, one state per lane
-      pi = lu / cpt;
-      t0 = (lu - pi * cpt) * kChunk + lane;
-      t1 = min(S, (lu - pi * cpt) * kChunk + kChunk);
-      tstep = 32;
-    } else {        // small tiles: one tile per lane, all its states
-      pi = lu * 32 + lane;
-      t0 = 0;
-      t1 = pi < a.npf[r] ? S : 0;
-      tstep = 1;
-    }
-    if (t0 >= t1) continue;
-    Desc<MMAX> d;
-    describe<MMAX, false, false>(pi, q, r, a, cn, d, dd{0.f, 0.f}, sbase);
+    const uint32_t S = a.tsize[r], lu = unit - a.uoff1[r], cpt = a.cpt1[r];
     const uint8_t* occ_t = a.tocc + a.tstate_off[r];
     const uint32_t* rows = a.tail + a.tail_off[r];
-    for (uint32_t tau = t0; tau < t1; tau += tstep) {
-      uint32_t occ = d.mask | ((uint32_t)__ldg(&occ_t[tau]) << p);
+    if (cpt > 0) {  // warp-uniform branch: the class of the unit
+      const uint32_t pi = lu / cpt;
+      const uint32_t c0 = (lu - pi * cpt) * a.chunk1;
+      const uint32_t c1 = min(S, c0 + a.chunk1);
+      uint32_t A = 0, tb = 0, mask = 0;
+      if (lane == 0) {
+        Desc<MMAX> d;
+        describe<MMAX, false, false>(pi, q, r, a, cn, d, dd{0.f, 0.f}, myslot);
+        A = d.A;
+        tb = d.tb;
+        mask = d.mask;
+      }
+      __syncwarp();
+      A = __shfl_sync(0xffffffffu, A, 0);
+      tb = __shfl_sync(0xffffffffu, tb, 0);
+      mask = __shfl_sync(0xffffffffu, mask, 0);
+      for (uint32_t t0 = c0 + lane; t0 < c1; t0 += 64) {
+        const uint32_t t1 = t0 + 32;
+        const bool two = t1 < c1;
+        cacc acc0 = cacc_zero(), acc1 = cacc_zero();
+        for (uint32_t mm = mask; mm; mm &= mm - 1) {
+          const int j = __ffs(mm) - 1;
+          const uint32_t bj = wslots[j];
+          const cdd uj = u[j];
+          cacc_fma(acc0, ld_cdd(&a.in[bj + t0]), uj);
+          if (two) cacc_fma(acc1, ld_cdd(&a.in[bj + t1]), uj);
+        }
+        {
+          const uint32_t* row = rows + (size_t)t0 * a.t;
+          for (uint32_t o = __ldg(&occ_t[t0]); o; o &= o - 1) {
+            const int jl = __ffs(o) - 1;
+            cacc_fma(acc0, ld_cdd(&a.in[tb + __ldg(&row[jl])]), u[p + jl]);
+          }
+          a.out[A + t0] = cacc_finish(acc0);
+        }
+        if (two) {
+          const uint32_t* row = rows + (size_t)t1 * a.t;
+          for (uint32_t o = __ldg(&occ_t[t1]); o; o &= o - 1) {
+            const int jl = __ffs(o) - 1;
+            cacc_fma(acc1, ld_cdd(&a.in[tb + __ldg(&row[jl])]), u[p + jl]);
+          }
+          a.out[A + t1] = cacc_finish(acc1);
+        }
+      }
+      __syncwarp();  // lane 0's slot is rewritten by the next unit
+      continue;
+    }
+    // group of G tiles: lane l unranks tile g0 + l
+    const uint32_t G = a.grp1[r];
+    const uint32_t g0 = lu * G;
+    const uint32_t ng = min(G, a.npf[r] - g0);
+    if ((uint32_t)lane < ng) {
+      Desc<MMAX> d;
+      describe<MMAX, false, false>(g0 + lane, q, r, a, cn, d, dd{0.f, 0.f}, myslot);
+      myslot[MMAX] = d.A;
+      myslot[MMAX + 1] = d.tb;
+      myslot[MMAX + 2] = d.mask;
+    }
+    __syncwarp();
+    // state f = g * S + tau of the group, f = lane, lane + 32, ...
+    const uint32_t q32 = 32 / S, r32 = 32 - q32 * S;
+    uint32_t g = (uint32_t)lane / S, tau = (uint32_t)lane - g * S;
+    while (g < ng) {
+      const uint32_t* ws = wslots + (size_t)g * SL;
+      uint32_t occ = ws[MMAX + 2] | ((uint32_t)__ldg(&occ_t[tau]) << p);
+      const uint32_t tb = ws[MMAX + 1];
       const uint32_t* row = rows + (size_t)tau * a.t - p;
       cacc acc = cacc_zero();
       while (occ) {
         const int j = __ffs(occ) - 1;
         occ &= occ - 1;
-        const uint32_t ad = j < p ? sbase[j] + tau : d.tb + __ldg(&row[j]);
+        const uint32_t ad = j < p ? ws[j] + tau : tb + __ldg(&row[j]);
         cacc_fma(acc, ld_cdd(&a.in[ad]), u[j]);
       }
-      a.out[d.A + tau] = cacc_finish(acc);
+      a.out[ws[MMAX] + tau] = cacc_finish(acc);
+      g += q32;
+      tau += r32;
+      if (tau >= S) {
+        tau -= S;
+        ++g;
+      }
     }
+    __syncwarp();  // the slots are rewritten by the next unit
   }
 }
 
@@ -475,6 +563,79 @@ __global__ void __launch_bounds__(256) slos_fin(SlosArgs a, dd inv_in, int mode,
   }
 }
 
+// Single-circuit finalisation over the forward kernel's units (uoff1 / cpt1 / grp1):
+// large tiles in chunks with one unranking per unit (lane 0, broadcast), smaller tiles
+// in groups unranked by all lanes at once and swept in rank order, one state per lane.
+template <int MMAX>
+__global__ void __launch_bounds__(256) slos_fin1(SlosArgs a, int mode, const double* __restrict__ w_in,
+                                                double* __restrict__ out_real, double2* __restrict__ out_c,
+                                                cdd* __restrict__ seed) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t* cn = reinterpret_cast<uint32_t*>(smem_raw);
+  const int ncn = (a.m + 1) * a.cn_stride;
+  for (int i = threadIdx.x; i < ncn; i += blockDim.x) cn[i] = a.cn[i];
+  // per thread: A, f.hi, f.lo of the tile it unranked
+  uint32_t* slots = reinterpret_cast<uint32_t*>(smem_raw + smem_cn_bytes(a.m, a.cn_stride));
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  uint32_t* myslot = slots + (size_t)threadIdx.x * 4;
+  const uint32_t* wslots = slots + (size_t)(threadIdx.x - lane) * 4;
+  const dd inv0 = a.inv_in[0];
+  const uint32_t total = a.uoff1[a.k + 1];
+  const uint32_t nw = gridDim.x * kWarps;
+  for (uint32_t unit = blockIdx.x * kWarps + (threadIdx.x >> 5); unit < total; unit += nw) {
+    const int r = unit_class1(a, unit);
+    const int q = a.k - r;
+    const uint32_t S = a.tsize[r], lu = unit - a.uoff1[r], cpt = a.cpt1[r];
+    if (cpt > 0) {
+      const uint32_t pi = lu / cpt;
+      const uint32_t c0 = (lu - pi * cpt) * a.chunk1;
+      const uint32_t c1 = min(S, c0 + a.chunk1);
+      uint32_t A = 0;
+      float fh = 0.f, fl = 0.f;
+      if (lane == 0) {
+        Desc<MMAX> d;
+        describe<MMAX, false, true>(pi, q, r, a, cn, d, inv0, d.base);
+        A = d.A;
+        fh = d.f.hi;
+        fl = d.f.lo;
+      }
+      A = __shfl_sync(0xffffffffu, A, 0);
+      fh = __shfl_sync(0xffffffffu, fh, 0);
+      fl = __shfl_sync(0xffffffffu, fl, 0);
+      const dd f = {fh, fl};
+      for (uint32_t tau = c0 + lane; tau < c1; tau += 32)
+        fin_state(a, f, r, A + tau, mode, w_in, out_real, out_c, seed, tau);
+      continue;
+    }
+    const uint32_t G = a.grp1[r];
+    const uint32_t g0 = lu * G;
+    const uint32_t ng = min(G, a.npf[r] - g0);
+    if ((uint32_t)lane < ng) {
+      Desc<MMAX> d;
+      describe<MMAX, false, true>(g0 + lane, q, r, a, cn, d, inv0, d.base);
+      myslot[0] = d.A;
+      myslot[1] = __float_as_uint(d.f.hi);
+      myslot[2] = __float_as_uint(d.f.lo);
+    }
+    __syncwarp();
+    const uint32_t q32 = 32 / S, r32 = 32 - q32 * S;
+    uint32_t g = (uint32_t)lane / S, tau = (uint32_t)lane - g * S;
+    while (g < ng) {
+      const uint32_t* ws = wslots + (size_t)g * 4;
+      const dd f = {__uint_as_float(ws[1]), __uint_as_float(ws[2])};
+      fin_state(a, f, r, ws[0] + tau, mode, w_in, out_real, out_c, seed, tau);
+      g += q32;
+      tau += r32;
+      if (tau >= S) {
+        tau -= S;
+        ++g;
+      }
+    }
+    __syncwarp();  // the slots are rewritten by the next unit
+  }
+}
+
 // grad[b][j][col[b]] += sum over CTAs of gpart[cta][j][b]  (col: the layer's column per entry)
 __global__ void slos_grad_reduce(const cdd* __restrict__ gpart, int nblk, int m, int B,
                                  const int32_t* __restrict__ col, double2* __restrict__ grad) {
@@ -525,7 +686,7 @@ static int launch_kernel(Kern kind, const SlosArgs& a, int grid, dd inv_in, int 
       if (batched) {
         slos_fwdb<MMAX><<<g, 256, smem, s>>>(a);
       } else {
-        const size_t smem1 = smem + (size_t)256 * MMAX * sizeof(uint32_t);
+        const size_t smem1 = smem + (size_t)256 * fwd1_slot<MMAX>() * sizeof(uint32_t);
         cudaFuncSetAttribute(slos_fwd1<MMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
         slos_fwd1<MMAX><<<g, 256, smem1, s>>>(a);
       }
@@ -537,7 +698,12 @@ static int launch_kernel(Kern kind, const SlosArgs& a, int grid, dd inv_in, int 
         slos_bwd<MMAX, false><<<g, 256, smem, s>>>(a);
       break;
     case Kern::Fin:
-      slos_fin<MMAX><<<g, 256, smem, s>>>(a, inv_in, mode, w, out_real, out_c, seed);
+      if (batched) {
+        slos_fin<MMAX><<<g, 256, smem, s>>>(a, inv_in, mode, w, out_real, out_c, seed);
+      } else {
+        const size_t smemf = smem_cn_bytes(a.m, a.cn_stride) + (size_t)256 * 4 * sizeof(uint32_t);
+        slos_fin1<MMAX><<<g, 256, smemf, s>>>(a, mode, w, out_real, out_c, seed);
+      }
       break;
   }
   return (int)cudaGetLastError();
@@ -739,12 +905,33 @@ SlosArgs make_args(const pcvl_slos_plan* p, int k) {
     }
   }
   a.uoff[k + 1] = (uint32_t)u;
+  // unit size: kChunk1 states, smaller (down to 64) when the layer would not give every
+  // resident warp several units
+  uint64_t chunk = kChunk1;
+  const uint64_t want_units = (uint64_t)pcvl::num_sms() * 64;
+  while (chunk > 64 && fock_count(p->m, k) / chunk < want_units) chunk >>= 1;
+  a.chunk1 = (uint32_t)chunk;
+  uint64_t u1 = 0;
+  for (int r = 0; r <= k; ++r) {
+    const uint64_t npf = fock_count(p->tail_p, k - r), S = p->tsize[r];
+    a.uoff1[r] = (uint32_t)u1;
+    if (S >= chunk) {
+      a.cpt1[r] = (uint32_t)((S + chunk - 1) / chunk);
+      a.grp1[r] = 0;
+      u1 += npf * a.cpt1[r];
+    } else {
+      a.cpt1[r] = 0;
+      a.grp1[r] = (uint32_t)std::min<uint64_t>(32, std::max<uint64_t>(1, chunk / S));
+      u1 += (npf + a.grp1[r] - 1) / a.grp1[r];
+    }
+  }
+  a.uoff1[k + 1] = (uint32_t)u1;
   return a;
 }
 
 // CTAs for a layer: one warp per unit, capped at 16 CTAs per SM (grid-stride beyond)
-int grid_for_units(const SlosArgs& a) {
-  const uint64_t units = a.uoff[a.k + 1];
+int grid_for_units(const SlosArgs& a, bool fwd1 = false) {
+  const uint64_t units = fwd1 ? a.uoff1[a.k + 1] : a.uoff[a.k + 1];
   uint64_t g = (units + kWarps - 1) / kWarps;
   g = std::min<uint64_t>(g, (uint64_t)pcvl::num_sms() * 16);
   return (int)std::max<uint64_t>(g, 1);
@@ -926,7 +1113,7 @@ static int forward(pcvl_slos_plan* p, const double* u_d, size_t ustride, cudaStr
     a.out = p->keep ? p->layers[k] : p->layers[k % 2];
     a.ucol = p->ucols_d + (size_t)(k - 1) * m * B;
     a.tail = p->tp_d;
-    const int rc = dispatch(Kern::Fwd, a, grid_for_units(a), s);
+    const int rc = dispatch(Kern::Fwd, a, grid_for_units(a, B == 1), s);
     if (rc != 0) {
       set_error("SLOS layer %d launch failed: %s", k, cudaGetErrorString((cudaError_t)rc));
       return PCVL_ERR_CUDA;
@@ -951,7 +1138,7 @@ static int finalize(pcvl_slos_plan* p, int mode, const double* w, double* out_re
   PCVL_CHECK(p->forwarded, "pcvl_slos_forward has not run on this plan");
   SlosArgs a = make_args(p, p->n);
   a.in = p->final_layer();
-  const int rc = dispatch(Kern::Fin, a, grid_for_units(a), s, dd_from_double(1.0),
+  const int rc = dispatch(Kern::Fin, a, grid_for_units(a, p->B == 1), s, dd_from_double(1.0),
                           mode, w, out_real, out_c, seed);
   if (rc != 0) {
     set_error("SLOS finalize launch failed: %s", cudaGetErrorString((cudaError_t)rc));
