@@ -107,6 +107,24 @@ def dist_setup():
     return ws, rank
 
 
+def max_over_ranks(x: float, device="cpu") -> float:
+    """Max of x over the ranks of the default process group (x itself without one):
+    the job's time is its slowest replica's."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank_step: float, world: int, steps: int, seconds: float) -> float:
+    """Units per second of the whole job: every rank processes units_per_rank_step per step
+    (weak scaling, independent replicas), timed by the slowest rank."""
+    return world * units_per_rank_step * steps / seconds
+
+
 def measured_fp64_peak(torch) -> float:
     """cuBLAS DGEMM 4096^3, best of 5, TFLOP/s (the FP64 roofline denominator)."""
     a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
@@ -240,12 +258,8 @@ def run_ours(args):
             step()
             e.record()
         barrier()
-    ms = sum(s.elapsed_time(e) for s, e in ev)
-    if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t)
-    value = ws * N_MATS * args.steps / (ms * 1e-3)
+    ms = max_over_ranks(sum(s.elapsed_time(e) for s, e in ev), dev)
+    value = whole_job_rate(N_MATS, ws, args.steps, ms * 1e-3)
 
     # e2e through the C ABI from pinned host buffers (copies inside the timed region)
     host_in = torch.from_numpy(flat).pin_memory()
@@ -264,12 +278,9 @@ def run_ours(args):
     for _ in range(args.steps):
         e2e_step()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t)
-    e2e = {"value": ws * N_MATS * args.steps / e2e_s, "unit": "perms/s", "h2d_bytes_per_step": int(flat.nbytes),
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dev)
+    e2e = {"value": whole_job_rate(N_MATS, ws, args.steps, e2e_s), "unit": "perms/s",
+           "h2d_bytes_per_step": int(flat.nbytes),
            "d2h_bytes_per_step": int(N_MATS * 16)}
 
     # dominant kernel alone: the n = 24 bin (its CTAs' share of the step is largest)
@@ -552,7 +563,32 @@ def run_learned(args):
                                  "max_abs_err_E_nn": float(np.abs(refs.T @ refs / len(refs) - E2).max())}}
         row["ess_per_s_ratio"] = row["mis"]["ess_per_s"] / row["exact_sampler"]["ess_per_s"]
         out[f"n{n}_m{m}"] = row
-    print(json.dumps({"learned_proposal": out}), flush=True)
+    # tensor-pipe rate of the network's GEMM kernel (pcvl_gemm_bf16, mma.sync BF16, FP32
+    # accumulation) at the training shapes of n = 30, m = 900 (256 sequences x 30 steps)
+    # and at 8192^3, against the measured cuBLAS BF16 burst peak
+    try:
+        peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"]
+    except (OSError, ValueError, KeyError):
+        peak = 1900.0
+    gemm = {}
+    for (M, N, K) in ((7680, 512, 512), (7680, 900, 512), (7680, 512, 128), (8192, 8192, 8192)):
+        A = torch.randn(M, K, device="cuda").to(torch.bfloat16)
+        B = torch.randn(N, K, device="cuda").to(torch.bfloat16)
+        C = torch.empty(M, N, device="cuda", dtype=torch.float32)
+        f = lambda: _native.gemm_bf16(A, B, M, N, K, K, K, C=C)
+        f()
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(5):
+            s0, e0 = torch.cuda.Event(True), torch.cuda.Event(True)
+            s0.record()
+            f()
+            e0.record()
+            e0.synchronize()
+            best = min(best, s0.elapsed_time(e0))
+        tf = 2.0 * M * N * K / (best * 1e-3) / 1e12
+        gemm[f"{M}x{N}x{K}"] = {"ms": best, "tflops": tf, "frac_of_bf16_peak": tf / peak}
+    print(json.dumps({"learned_proposal": out, "mlp_gemm": gemm, "bf16_peak_tflops": peak}), flush=True)
 
 
 def profile_case(name: str):
@@ -589,6 +625,12 @@ def profile_case(name: str):
         err = torch.empty(1000, dtype=torch.float64, device=dev)
         _native.permanent_estimate_batch(torch.from_numpy(gm.reshape(-1)).to(dev), np.arange(1000) * 400,
                                          np.full(1000, 20), out, err, 10000, 1, 0)
+    elif name == "gemm":
+        M, N, K = 7680, 512, 512
+        A = torch.randn(M, K, device="cuda").to(torch.bfloat16)
+        B = torch.randn(N, K, device="cuda").to(torch.bfloat16)
+        C = torch.empty(M, N, device="cuda", dtype=torch.float32)
+        _native.gemm_bf16(A, B, M, N, K, K, K, C=C)
     elif name == "cc2017":
         U4 = torch.from_numpy(random_unitary(400, seed=0)).to(dev)
         _native.cc2017_sample(U4, [1] * 20 + [0] * 380, 608, seed=1)
@@ -608,7 +650,7 @@ def main():
     ap.add_argument("--learned", action="store_true",
                     help="run the learned-proposal sampler workload (n=30, m=900 and n=8, m=64) and exit")
     ap.add_argument("--learned-train", type=int, default=2048, help="exact training samples at n=30")
-    ap.add_argument("--profile-case", choices=["perm24", "slos20", "slos16b256", "cc2017", "gurvits20"],
+    ap.add_argument("--profile-case", choices=["perm24", "slos20", "slos16b256", "cc2017", "gurvits20", "gemm"],
                     help="run one small untimed case of a single kernel (for ncu) and exit")
     args = ap.parse_args()
     if args.profile_case:
