@@ -8,11 +8,17 @@
 // so Y = X W^T (forward), dX = dY W (transB), dW = dY^T X (transA, transB) are all one
 // kernel with the weight matrices in torch Linear layout (out x in, row-major).
 //
-// Tiling: 128 x 128 x 32 per CTA, 8 warps of 64 x 32, mma.sync m16n8k16 (bf16 in,
-// f32 accumulate) with fragments read from padded shared-memory tiles in the operand
-// layouts of the PTX ISA (A row-major 16x16: rows g / g + 8, columns 2t / 2t + 8;
-// B column-major 16x8: rows 2t / 2t + 8, column g; C: rows g / g + 8, columns 2t,
-// with g = lane / 4 and t = lane % 4).
+// The GEMM runs on the 5th-generation tensor cores: one CTA (4 warps) per 128 x 128
+// tile of C with the FP32 accumulator in tensor memory (128 lanes x 128 columns).  Per
+// 64-wide K step the CTA stages the A and B tiles in shared memory in the canonical
+// K-major layout without swizzle (8 x 16-byte core matrices; 128 B between core
+// matrices along K, 1024 B between 8-row groups), then one thread issues four
+// tcgen05.mma.kind::f16 (M = 128, N = 128, K = 16) with BF16 inputs and commits them to
+// an mbarrier.  Three stages filled by 16-byte cp.async: the tiles of steps k + 1 and
+// k + 2 are in flight while the MMAs of step k run.  The epilogue reads the accumulator with tcgen05.ld (warp w owns TMEM lanes
+// 32w..32w+31 = rows of the tile) and applies alpha, beta, bias and GELU.  Every mbarrier
+// wait is bounded; a CTA whose wait gives up waits (bounded) for its last commit, frees
+// its tensor memory and writes NaN to its tile.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -23,7 +29,12 @@
 
 namespace pcvl {
 
-constexpr int GBM = 128, GBN = 128, GBK = 32, GPAD = 8;
+constexpr int TBM = 128, TBN = 128, TBK = 64;
+constexpr int kTcThreads = 128;
+constexpr uint32_t kTileBytes = TBM * TBK * 2;  // one bf16 operand tile, 16 KB
+constexpr uint32_t kTmemCols = 128;
+constexpr int kStages = 3;                       // operand stages in shared memory (96 KB)
+constexpr uint32_t kWaitLimit = 1u << 22;        // mbarrier polls before giving up
 
 enum Epilogue { EPI_NONE = 0, EPI_BIAS = 1, EPI_BIAS_GELU = 2 };
 
@@ -32,14 +43,6 @@ __device__ __forceinline__ float gelu_grad(float x) {
   const float cdf = 0.5f * (1.f + erff(x * 0.70710678118654752f));
   const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
   return cdf + x * pdf;
-}
-
-__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
 struct GemmArgs {
@@ -55,113 +58,233 @@ struct GemmArgs {
   float* Cpre;                // pre-activation (f32) for EPI_BIAS_GELU (may be null), ldc
 };
 
-// one 128 x 32 operand tile into shared memory as [row][k] (k contiguous)
-__device__ __forceinline__ void load_tile(const __nv_bfloat16* __restrict__ G, int trans, int ld, int rows, int K,
-                                          int row0, int k0, __nv_bfloat16 (*S)[GBK + GPAD]) {
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// byte offset of element (row r, k) of a 128 x 64 tile in the no-swizzle K-major layout
+__device__ __forceinline__ uint32_t tile_off(int r, int k) {
+  return (uint32_t)(((r >> 3) * (TBK / 8) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// shared-memory matrix descriptor: start address, leading-dimension byte offset (next
+// core matrix along K), stride byte offset (next 8-row group), version 1, no swizzle
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+  const uint64_t lbo = 128, sbo = (TBK / 8) * 128;
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((lbo >> 4) << 16) | ((sbo >> 4) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major,
+// N = 128, M = 128
+__device__ __forceinline__ uint32_t umma_idesc() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TBN >> 3) << 17) | ((uint32_t)(TBM >> 4) << 24);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+  for (uint32_t it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t saddr, const void* gptr) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr), "l"(gptr) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+// one 128 x 64 operand tile into shared memory (element (r, k) of rows [row0, row0 + 128),
+// k in [k0, k0 + 64)), zeros outside the matrix.  Rows with k contiguous in memory go by
+// 16-byte cp.async (thread t copies row t); transposed operands are gathered by the
+// threads (eight rows of one k per 16-byte load, scattered into the rows' core matrices).
+__device__ __forceinline__ void stage_tile(const __nv_bfloat16* __restrict__ G, int trans, int ld, int rows, int K,
+                                           int row0, int k0, unsigned char* S) {
   const int tid = threadIdx.x;
+  const bool aligned = (ld & 7) == 0 && ((reinterpret_cast<uintptr_t>(G) & 15) == 0);
   if (!trans) {
-    // 128 rows x 32 k: 512 chunks of 8 contiguous k; 2 per thread
-    for (int c = tid; c < GBM * GBK / 8; c += blockDim.x) {
-      const int r = c >> 2, kk = (c & 3) * 8;
-      const int gr = row0 + r, gk = k0 + kk;
-      __nv_bfloat16 v[8];
-      if (gr < rows && gk + 7 < K && ((ld & 7) == 0)) {
-        const uint4 q = *reinterpret_cast<const uint4*>(&G[(size_t)gr * ld + gk]);
-        *reinterpret_cast<uint4*>(v) = q;
+    const int r = tid, gr = row0 + r;
+    const uint32_t sbase = smem_u32(S);
+#pragma unroll
+    for (int kc = 0; kc < TBK / 8; ++kc) {
+      const int gk = k0 + kc * 8;
+      const uint32_t off = tile_off(r, kc * 8);
+      if (gr < rows && gk + 7 < K && aligned) {
+        cp_async16(sbase + off, &G[(size_t)gr * ld + gk]);
       } else {
+        __nv_bfloat16 v[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e)
           v[e] = (gr < rows && gk + e < K) ? G[(size_t)gr * ld + gk + e] : __float2bfloat16(0.f);
+        *reinterpret_cast<uint4*>(S + off) = *reinterpret_cast<const uint4*>(v);
       }
-#pragma unroll
-      for (int e = 0; e < 8; ++e) S[r][kk + e] = v[e];
     }
   } else {
-    // element (row, k) at G[k * ld + row]: 32 k x 128 rows, rows contiguous
-    for (int c = tid; c < GBM * GBK / 8; c += blockDim.x) {
+    for (int c = tid; c < TBM * TBK / 8; c += kTcThreads) {
       const int kk = c >> 4, r = (c & 15) * 8;
       const int gr = row0 + r, gk = k0 + kk;
       __nv_bfloat16 v[8];
-      if (gk < K && gr + 7 < rows && ((ld & 7) == 0)) {
-        const uint4 q = *reinterpret_cast<const uint4*>(&G[(size_t)gk * ld + gr]);
-        *reinterpret_cast<uint4*>(v) = q;
+      if (gk < K && gr + 7 < rows && aligned) {
+        *reinterpret_cast<uint4*>(v) = *reinterpret_cast<const uint4*>(&G[(size_t)gk * ld + gr]);
       } else {
 #pragma unroll
         for (int e = 0; e < 8; ++e)
           v[e] = (gk < K && gr + e < rows) ? G[(size_t)gk * ld + gr + e] : __float2bfloat16(0.f);
       }
 #pragma unroll
-      for (int e = 0; e < 8; ++e) S[r + e][kk] = v[e];
+      for (int e = 0; e < 8; ++e) *reinterpret_cast<__nv_bfloat16*>(S + tile_off(r + e, kk)) = v[e];
     }
   }
 }
 
-__global__ void __launch_bounds__(256) gemm_bf16_kernel(GemmArgs g) {
-  __shared__ __align__(16) __nv_bfloat16 As[GBM][GBK + GPAD];
-  __shared__ __align__(16) __nv_bfloat16 Bs[GBN][GBK + GPAD];
+__global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(GemmArgs g) {
+  extern __shared__ __align__(1024) unsigned char smem[];  // kStages x (A tile, B tile)
+  __shared__ __align__(8) uint64_t mbar[kStages];
+  __shared__ uint32_t tmem_base_s;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = warp >> 2, wn = warp & 3;  // 2 x 4 warps of 64 x 32
-  const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
-  const int gq = lane >> 2, tq = lane & 3;
-  float acc[4][4][4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.f;
+  const int m0 = blockIdx.y * TBM, n0 = blockIdx.x * TBN;
+  const int nk = (g.K + TBK - 1) / TBK;
 
-  for (int k0 = 0; k0 < g.K; k0 += GBK) {
-    load_tile(g.A, g.transA, g.lda, g.M, g.K, m0, k0, As);
-    load_tile(g.B, g.transB, g.ldb, g.N, g.K, n0, k0, Bs);
-    __syncthreads();
-#pragma unroll
-    for (int ks = 0; ks < GBK; ks += 16) {
-      uint32_t af[4][4], bf[4][2];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const int r = wm * 64 + i * 16 + gq;
-        af[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * tq]);
-        af[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * tq]);
-        af[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * tq + 8]);
-        af[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * tq + 8]);
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int c = wn * 32 + j * 8 + gq;
-        bf[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + 2 * tq]);
-        bf[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + 2 * tq + 8]);
-      }
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bf[j]);
-    }
-    __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  // epilogue
+  if (tid == 0) {
+    for (int i = 0; i < kStages; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[i])));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_base_s;
+  const uint32_t idesc = umma_idesc();
+  bool ok = true;
+  int last = -1;  // last committed K step (uniform over the CTA)
+
+  // step j uses stage j % kStages and completes phase (j / kStages) of mbar[j % kStages]
+  auto issue = [&](int j) {
+    if (j < nk) {
+      unsigned char* As = smem + (j % kStages) * 2 * kTileBytes;
+      stage_tile(g.A, g.transA, g.lda, g.M, g.K, m0, j * TBK, As);
+      stage_tile(g.B, g.transB, g.ldb, g.N, g.K, n0, j * TBK, As + kTileBytes);
+    }
+    cp_async_commit();  // one group per step, empty past the end
+  };
+  for (int j = 0; j < kStages - 1; ++j) issue(j);
+
+  for (int kt = 0; kt < nk && ok; ++kt) {
+    const int st = kt % kStages;
+    asm volatile("cp.async.wait_group %0;" ::"n"(kStages - 2) : "memory");  // step kt has landed
+    // generic-proxy and cp.async writes of the tiles -> visible to the tensor cores
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t a0 = smem_u32(smem + st * 2 * kTileBytes), b0 = a0 + kTileBytes;
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
+      for (int kk = 0; kk < TBK / 16; ++kk) {
+        // K slice kk = core matrices 2kk and 2kk + 1 along K (256 B further per slice)
+        const uint64_t ad = umma_desc(a0 + kk * 256), bd = umma_desc(b0 + kk * 256);
+        const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&mbar[st]))
+                   : "memory");
+    }
+    last = kt;
+    // the next refill reuses the stage of step kt - 1: wait for its MMAs (one pending
+    // phase per barrier at any time; the outcome is uniform over the CTA)
+    if (kt >= 1) {
+      const int j = kt - 1;
+      ok = __syncthreads_and(mbar_wait(smem_u32(&mbar[j % kStages]), (j / kStages) & 1));
+    }
+    if (ok) issue(kt + kStages - 1);
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  // every MMA done: the last commit covers all earlier ones of the issuing thread.  This
+  // wait runs even after a wait gave up, so no MMA is in flight when the tensor memory is
+  // released; a CTA whose waits gave up writes NaN instead of reading the accumulator.
+  if (last >= 0)
+    ok = __syncthreads_and(mbar_wait(smem_u32(&mbar[last % kStages]), (last / kStages) & 1) && ok);
+  asm volatile("tcgen05.fence::after_thread_sync;");
+
+  // epilogue: warp w holds rows 32w..32w+31 of the tile, 32 columns per tcgen05.ld
+  const int row = m0 + warp * 32 + lane;
+  const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+  for (int c0 = 0; c0 < TBN; c0 += 32) {
+    uint32_t r[32];
+    if (nk > 0 && ok) {
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+          "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          : "r"(taddr + (uint32_t)c0));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    } else {
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+      for (int i = 0; i < 32; ++i) r[i] = 0u;
+    }
+    if (row < g.M) {
+      // groups of 4 columns: one 16-byte store per output when the row is aligned
+      const bool vec = (g.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(g.C) & 15) == 0 &&
+                       (reinterpret_cast<uintptr_t>(g.Cpre) & 15) == 0 && (reinterpret_cast<uintptr_t>(g.Cb) & 7) == 0;
 #pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int r = m0 + wm * 64 + i * 16 + gq + (e >= 2 ? 8 : 0);
-        const int c = n0 + wn * 32 + j * 8 + 2 * tq + (e & 1);
-        if (r < g.M && c < g.N) {
-          const size_t o = (size_t)r * g.ldc + c;
-          float v = g.alpha * acc[i][j][e];
-          if (g.beta != 0.f) v += g.beta * g.C[o];
-          if (g.epi != EPI_NONE) v += g.bias[c];
-          if (g.epi == EPI_BIAS_GELU) {
-            if (g.Cpre) g.Cpre[o] = v;
-            v = gelu_f(v);
+      for (int i0 = 0; i0 < 32; i0 += 4) {
+        const int col0 = n0 + c0 + i0;
+        if (col0 >= g.N) break;
+        const size_t o0 = (size_t)row * g.ldc + col0;
+        float v[4], pre[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int col = col0 + e;
+          float x = ok ? g.alpha * __uint_as_float(r[i0 + e]) : __int_as_float(0x7fc00000);
+          if (col < g.N) {
+            if (g.beta != 0.f) x += g.beta * g.C[o0 + e];
+            if (g.epi != EPI_NONE) x += g.bias[col];
           }
-          if (g.C) g.C[o] = v;
-          if (g.Cb) g.Cb[o] = __float2bfloat16(v);
+          pre[e] = x;
+          v[e] = g.epi == EPI_BIAS_GELU ? gelu_f(x) : x;
+        }
+        if (vec && col0 + 3 < g.N) {
+          if (g.C) *reinterpret_cast<float4*>(g.C + o0) = make_float4(v[0], v[1], v[2], v[3]);
+          if (g.Cpre && g.epi == EPI_BIAS_GELU)
+            *reinterpret_cast<float4*>(g.Cpre + o0) = make_float4(pre[0], pre[1], pre[2], pre[3]);
+          if (g.Cb) {
+            __nv_bfloat162 lo = __floats2bfloat162_rn(v[0], v[1]), hi = __floats2bfloat162_rn(v[2], v[3]);
+            uint2 q;
+            q.x = *reinterpret_cast<uint32_t*>(&lo);
+            q.y = *reinterpret_cast<uint32_t*>(&hi);
+            *reinterpret_cast<uint2*>(g.Cb + o0) = q;
+          }
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            if (col0 + e < g.N) {
+              if (g.C) g.C[o0 + e] = v[e];
+              if (g.Cpre && g.epi == EPI_BIAS_GELU) g.Cpre[o0 + e] = pre[e];
+              if (g.Cb) g.Cb[o0 + e] = __float2bfloat16(v[e]);
+            }
+          }
         }
       }
     }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
   }
 }
 
@@ -334,9 +457,11 @@ extern "C" int pcvl_gemm_bf16(const void* A, const void* B, int32_t M, int32_t N
   if (M == 0 || N == 0) return PCVL_OK;
   GemmArgs g{(const __nv_bfloat16*)A, (const __nv_bfloat16*)B, M, N, K, lda, ldb, ldc, transA, transB, alpha, beta,
              bias, epilogue, C, (__nv_bfloat16*)Cb, Cpre};
-  dim3 grid((N + GBN - 1) / GBN, (M + GBM - 1) / GBM);
+  dim3 grid((N + TBN - 1) / TBN, (M + TBM - 1) / TBM);
   PCVL_CHECK(grid.y <= 65535, "M too large for one launch (%d)", M);
-  gemm_bf16_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(g);
+  const int smem = kStages * 2 * (int)kTileBytes;
+  PCVL_CUDA(cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  gemm_tc_kernel<<<grid, kTcThreads, smem, (cudaStream_t)stream>>>(g);
   PCVL_CUDA(cudaGetLastError());
   return PCVL_OK;
 }
