@@ -191,7 +191,9 @@ PCVL_HD uint32_t mulhi32(uint32_t a, uint32_t b) {
 PCVL_HD u4 philox4x32_10(u4 c, uint32_t k0, uint32_t k1) {
   const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
   const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#ifdef __CUDA_ARCH__
 #pragma unroll
+#endif
   for (int r = 0; r < 10; ++r) {
     uint32_t hi0 = mulhi32(M0, c.x), lo0 = M0 * c.x;
     uint32_t hi1 = mulhi32(M1, c.z), lo1 = M1 * c.z;

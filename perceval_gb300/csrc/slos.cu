@@ -80,6 +80,7 @@ struct SlosArgs {
   uint32_t uoff[kSlosMaxN + 2];
   uint32_t npf[kSlosMaxN + 1];
   uint32_t cpt[kSlosMaxN + 1];
+  uint32_t chunkB;        // states per unit of the batched kernels
   // units of the single-circuit forward kernel: tiles of >= chunk1 states in chunks of
   // chunk1 (cpt1 > 0), smaller tiles in groups of grp1 tiles (about chunk1 states)
   uint32_t chunk1;
@@ -89,7 +90,8 @@ struct SlosArgs {
 };
 
 constexpr uint32_t kChunk = 256;   // states per unit of a large tile (single circuit)
-constexpr uint32_t kChunkB = 8;    // states per unit (batched)
+constexpr uint32_t kChunkB = 32;   // states per unit (batched forward and finalisation)
+constexpr uint32_t kChunkBwdB = 8; // states per unit (batched adjoint: more, smaller units)
 constexpr uint32_t kChunk1 = 1024; // largest unit of the single-circuit forward kernel (states)
 
 __device__ __forceinline__ uint32_t cn_at(const uint32_t* cn, int stride, int M, int x) {
@@ -218,9 +220,7 @@ __device__ __forceinline__ cdd fwd_value(const SlosArgs& a, const Desc<MMAX>& d,
   }
   if (r > 0) {
     const uint32_t* row = a.tail + a.tail_off[r] + (size_t)tau * a.t;
-    uint32_t occ = 0;
-    for (int jl = 0; jl < a.t; ++jl)
-      if (__ldg(&row[jl]) != kNone) occ |= 1u << jl;
+    uint32_t occ = __ldg(&a.tocc[a.tstate_off[r] + tau]);  // occupied tail modes
     while (occ) {
       const int jl = __ffs(occ) - 1;
       occ &= occ - 1;
@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(256) slos_fwdb(SlosArgs a) {
     const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
     Desc<MMAX> d;
     describe<MMAX, false, false>(pi, a.k - r, r, a, cn, d, dd{0.f, 0.f}, d.base);
-    const uint32_t t0 = ch * kChunkB, t1 = min(S, t0 + kChunkB);
+    const uint32_t t0 = ch * a.chunkB, t1 = min(S, t0 + a.chunkB);
     if (b < a.B)
       for (uint32_t tau = t0; tau < t1; ++tau)
         a.out[(size_t)(d.A + tau) * a.B + b] = fwd_value<MMAX, true>(a, d, r, tau, a.in, u, 32, b);
@@ -436,7 +436,7 @@ __global__ void __launch_bounds__(256) slos_bwd(SlosArgs a) {
     if (cpt > 0) {
       const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
       describe<MMAX, true, false>(pi, q, r, a, cn, d, dd{0.f, 0.f}, d.base);
-      const uint32_t chunk = BATCHED ? kChunkB : kChunk;
+      const uint32_t chunk = BATCHED ? a.chunkB : kChunk;
       const uint32_t t0 = ch * chunk, t1 = min(S, t0 + chunk);
       if (BATCHED) {
         if (b < a.B)
@@ -539,7 +539,7 @@ __global__ void __launch_bounds__(256) slos_fin(SlosArgs a, dd inv_in, int mode,
     if (cpt > 0) {
       const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
       describe<MMAX, false, true>(pi, q, r, a, cn, d, inv_in, d.base);
-      const uint32_t chunk = batched ? kChunkB : kChunk;
+      const uint32_t chunk = batched ? a.chunkB : kChunk;
       const uint32_t t0 = ch * chunk, t1 = min(S, t0 + chunk);
       if (batched) {
         if (b < a.B) {
@@ -868,8 +868,9 @@ int upload(void* dst, const void* src, size_t bytes) {
   return PCVL_OK;
 }
 
-SlosArgs make_args(const pcvl_slos_plan* p, int k) {
+SlosArgs make_args(const pcvl_slos_plan* p, int k, uint32_t chunkB = kChunkB) {
   SlosArgs a{};
+  a.chunkB = chunkB;
   a.m = p->m;
   a.k = k;
   a.p = p->tail_p;
@@ -886,7 +887,7 @@ SlosArgs make_args(const pcvl_slos_plan* p, int k) {
     a.tstate_off[r] = p->tstate_off[r];
     a.tsize[r] = p->tsize[r];
   }
-  // work units by class r = tail photons: batched -> (tile, kChunkB states); single
+  // work units by class r = tail photons: batched -> (tile, chunkB states); single
   // circuit -> (tile, kChunk states) for tiles of >= 32 states, 32 whole tiles below
   uint64_t u = 0;
   for (int r = 0; r <= k; ++r) {
@@ -894,7 +895,7 @@ SlosArgs make_args(const pcvl_slos_plan* p, int k) {
     a.uoff[r] = (uint32_t)u;
     a.npf[r] = (uint32_t)npf;
     if (p->B > 1) {
-      a.cpt[r] = (uint32_t)((S + kChunkB - 1) / kChunkB);
+      a.cpt[r] = (uint32_t)((S + chunkB - 1) / chunkB);
       u += npf * a.cpt[r];
     } else if (S >= 32) {
       a.cpt[r] = (uint32_t)((S + kChunk - 1) / kChunk);
@@ -1166,7 +1167,7 @@ extern "C" int pcvl_slos_backward(pcvl_slos_plan* p, const double* weights_d, do
   PCVL_CUDA(cudaMemsetAsync(grad_u_d, 0, (size_t)B * m * m * 2 * sizeof(double), s));
   PCVL_TRY(finalize(p, 2, weights_d, nullptr, nullptr, p->adj_d[n % 2], s));
   for (int k = n; k >= 1; --k) {
-    SlosArgs a = make_args(p, k - 1);  // tiles of the parent layer
+    SlosArgs a = make_args(p, k - 1, kChunkBwdB);  // tiles of the parent layer
     a.in = p->adj_d[k % 2];
     a.out = p->adj_d[(k - 1) % 2];
     a.ucol = p->ucols_d + (size_t)(k - 1) * m * B;
