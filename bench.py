@@ -523,7 +523,7 @@ def run_learned(args):
     and n_i n_j against the closed forms."""
     import torch
     from perceval_gb300 import _native
-    from perceval_gb300.learned import ProposalMLP, ess, exact_moments, run_mis
+    from perceval_gb300.learned import ProposalMLP, ess, exact_moments, run_mis, tvd_estimate
     from perceval_gb300.utils.matrix import random_unitary
     _native.load()
     out = {}
@@ -538,7 +538,8 @@ def run_learned(args):
         t_train_samples = time.perf_counter() - t0
         net = ProposalMLP(m, n, D=128, H=512, layers=3, seed=0)
         t0 = time.perf_counter()
-        losses = net.train(train, epochs=epochs, batch=256, lr=1e-3)
+        n_val = max(1, len(train) // 10)  # held-out tenth: early stopping on its NLL
+        losses = net.train(train[n_val:], epochs=epochs, batch=256, lr=1e-3, val=train[:n_val])
         torch.cuda.synchronize()
         t_fit = time.perf_counter() - t0
         # Metropolised independence sampler (proposal sampling + exact permanents + scan)
@@ -554,6 +555,7 @@ def run_learned(args):
         refs = ref.astype(np.float64)
         row = {"m": m, "n": n, "train_samples": n_train, "train_sampling_s": t_train_samples,
                "fit_s": t_fit, "nll_first_last": [losses[0], losses[-1]],
+               "held_out_nll": net.val_nll, "kept_epoch": net.best_epoch,
                "mis": {"chains": chains, "steps": steps, "proposals": res.proposals, "seconds": res.seconds,
                        "accept_rate": res.accept_rate, "ess": ess_mis, "ess_per_s": ess_mis / res.seconds,
                        "max_abs_err_E_n": float(np.abs(st.mean(0) - A).max()),
@@ -562,6 +564,12 @@ def run_learned(args):
                                  "max_abs_err_E_n": float(np.abs(refs.mean(0) - A).max()),
                                  "max_abs_err_E_nn": float(np.abs(refs.T @ refs / len(refs) - E2).max())}}
         row["ess_per_s_ratio"] = row["mis"]["ess_per_s"] / row["exact_sampler"]["ess_per_s"]
+        # TVD(q, pi) on photon sequences from the exact samples: trained vs untrained network
+        untrained = ProposalMLP(m, n, D=128, H=512, layers=3, seed=0)
+        t, te = tvd_estimate(net, U, inp, ref, seed=5)
+        u0, ue = tvd_estimate(untrained, U, inp, ref, seed=5)
+        row["tvd_q_pi_sequences"] = {"samples": int(len(ref)), "trained": t, "trained_stderr": te,
+                                     "untrained": u0, "untrained_stderr": ue}
         out[f"n{n}_m{m}"] = row
     # tensor-pipe rate of the network's GEMM kernel (pcvl_gemm_bf16, mma.sync BF16, FP32
     # accumulation) at the training shapes of n = 30, m = 900 (256 sequences x 30 steps)

@@ -141,13 +141,41 @@ class ProposalMLP:
         for p, g, (m1, m2), wb in zip(self.params, grads, self._adam, bf):
             _native.adam(p, g, m1, m2, lr, b1, b2, eps, self._step, wb)
 
+    def _snapshot(self):
+        return [p.clone() for p in self.params], [w.clone() for w in self.Wb], self.Wob.clone()
+
+    def _restore(self, snap):
+        ps, wbs, wob = snap
+        for p, v in zip(self.params, ps):
+            p.copy_(v)
+        for w, v in zip(self.Wb, wbs):
+            w.copy_(v)
+        self.Wob.copy_(wob)
+
+    def nll(self, samples: np.ndarray, seed: int = 0, batch: int = 1024) -> float:
+        """Mean negative log-likelihood per photon of output samples (counts per mode),
+        each given a uniformly random photon order."""
+        seqs = np.stack(counts_to_sequences(samples, np.random.default_rng(seed))).astype(np.int32)
+        tot = 0.0
+        for i in range(0, len(seqs), batch):
+            tot -= float(self.log_q(torch.from_numpy(seqs[i:i + batch]).cuda()).sum())
+        return tot / (len(seqs) * self.n)
+
     def train(self, samples: np.ndarray, epochs: int = 5, batch: int = 256, lr: float = 1e-3, seed: int = 0,
-              log=None) -> list[float]:
+              log=None, val: np.ndarray | None = None) -> list[float]:
         """Maximum likelihood on sequences made from output samples (counts per mode),
-        each photon order drawn uniformly at random."""
+        each photon order drawn uniformly at random.  With held-out samples ``val`` the
+        parameters of the epoch with the lowest held-out NLL are kept (the starting point
+        counts as epoch 0), so training cannot leave the proposal worse on fresh samples
+        than it found it; ``self.val_nll`` records the held-out NLL per epoch."""
         rng = np.random.default_rng(seed)
         seqs = counts_to_sequences(samples, rng)
         losses = []
+        self.val_nll, self.best_epoch = [], 0
+        best = None
+        if val is not None:
+            self.val_nll.append(self.nll(val, seed=seed + 1))
+            best = self._snapshot()
         for ep in range(epochs):
             order = rng.permutation(len(seqs))
             tot, cnt = 0.0, 0
@@ -160,8 +188,15 @@ class ProposalMLP:
                 tot += loss * len(idx)
                 cnt += len(idx)
             losses.append(tot / cnt)
+            if val is not None:
+                self.val_nll.append(self.nll(val, seed=seed + 1))
+                if self.val_nll[-1] < min(self.val_nll[:-1]):
+                    best, self.best_epoch = self._snapshot(), ep + 1
             if log:
-                log(f"epoch {ep}: nll/photon {losses[-1]:.4f}")
+                log(f"epoch {ep}: nll/photon {losses[-1]:.4f}" +
+                    (f", held-out {self.val_nll[-1]:.4f}" if val is not None else ""))
+        if best is not None:
+            self._restore(best)
         return losses
 
     # ------------------------------------------------------------------ sampling
@@ -266,6 +301,27 @@ def run_mis(proposal: ProposalMLP, U: np.ndarray, input_state, chains: int, step
     secs = time.perf_counter() - t0
     counts = np.stack([sequences_to_counts(states[c], m) for c in range(chains)])
     return MISResult(counts, accepted / (chains * steps), total, secs, state_lp)
+
+
+def tvd_estimate(proposal: "ProposalMLP", U: np.ndarray, input_state, exact_counts: np.ndarray,
+                 seed: int = 0) -> tuple[float, float]:
+    """Total-variation distance between the proposal q and the target pi on photon
+    sequences, TVD = E_{r ~ pi}[max(0, 1 - q(r) / pi(r))], estimated without bias from
+    exact samples (counts) given a uniformly random photon order (a draw from pi); exact
+    pi(r) = |Perm|^2 / n! from the float-float permanents.  Returns (estimate, standard
+    error).  It bounds the distance between the two laws on output multisets from above."""
+    rng = np.random.default_rng(seed)
+    m = U.shape[0]
+    n = int(np.sum(input_state))
+    cols = np.repeat(np.arange(m), np.asarray(input_state))
+    seqs = np.stack(counts_to_sequences(exact_counts, rng)).astype(np.int32)
+    U_dev = torch.from_numpy(np.ascontiguousarray(U)).cuda()
+    seq_d = torch.from_numpy(seqs).cuda()
+    log_pi = log_abs_perm2(U_dev, cols, seq_d) - math.lgamma(n + 1)
+    log_q = proposal.log_q(seq_d).cpu().numpy()
+    with np.errstate(over="ignore"):
+        v = np.maximum(0.0, 1.0 - np.exp(log_q - log_pi))
+    return float(v.mean()), float(v.std(ddof=1) / math.sqrt(len(v)))
 
 
 def ess(x: np.ndarray) -> float:

@@ -119,3 +119,36 @@ def test_exact_moments_match_slos(oracle):
     A, E2 = exact_moments(U, inp)
     assert np.allclose(A, probs @ states, atol=1e-12)
     assert np.allclose(E2, np.einsum("r,ri,rj->ij", probs, states, states), atol=1e-12)
+
+
+def test_tvd_estimate_matches_enumeration(native, oracle):
+    # m = 6, n = 3: all 216 photon sequences enumerated; the Monte-Carlo estimate from exact
+    # samples agrees within 5 standard errors
+    import itertools
+    from perceval_gb300.learned import tvd_estimate
+    m, inp = 6, [1, 0, 1, 0, 1, 0]
+    U = random_unitary(m, seed=12)
+    net = ProposalMLP(m, 3, D=16, H=32, layers=3, seed=2)
+    seqs = np.array(list(itertools.product(range(m), repeat=3)), dtype=np.int32)
+    cols = np.array([0, 2, 4])
+    lp = log_abs_perm2(torch.from_numpy(U).cuda(), cols, torch.from_numpy(seqs).cuda()) - math.log(6)
+    lq = net.log_q(torch.from_numpy(seqs).cuda()).cpu().numpy()
+    exact = 0.5 * np.abs(np.exp(lp) - np.exp(lq)).sum()
+    assert abs(np.exp(lp).sum() - 1) < 1e-12 and abs(np.exp(lq).sum() - 1) < 1e-5
+    samples = oracle.cc2017(U, inp, 20000, seed=4)
+    est, se = tvd_estimate(net, U, inp, samples, seed=1)
+    assert abs(est - exact) < 5 * se + 1e-3, (est, se, exact)
+
+
+def test_early_stopping_keeps_the_best_epoch(native):
+    # 200 samples, 12 epochs: the held-out NLL rises once the network memorises; training
+    # keeps the epoch with the lowest held-out NLL, never worse than the start
+    m, n = 24, 4
+    U = random_unitary(m, seed=30)
+    inp = [1] * n + [0] * (m - n)
+    data = native.cc2017_sample(torch.from_numpy(U).cuda(), inp, 400, seed=31).cpu().numpy()
+    net = ProposalMLP(m, n, D=32, H=256, layers=3, seed=1)
+    net.train(data[:200], epochs=12, batch=32, lr=3e-3, val=data[200:], seed=4)
+    assert len(net.val_nll) == 13
+    assert net.val_nll[net.best_epoch] == min(net.val_nll) <= net.val_nll[0]
+    assert abs(net.nll(data[200:], seed=5) - net.val_nll[net.best_epoch]) < 1e-5
