@@ -95,6 +95,13 @@ def load(require_cuda: bool = True):
             fn.restype = res
             fn.argtypes = args
         _lib = lib
+        if require_cuda:
+            # launch shapes tuned earlier on this GPU and build, if a cached table exists
+            try:
+                from . import autotune
+                autotune.load()
+            except (OSError, ValueError, KeyError, RuntimeError):
+                pass
     return _lib
 
 
