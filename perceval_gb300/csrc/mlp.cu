@@ -19,7 +19,9 @@
 // 32w..32w+31 = rows of the tile) and applies alpha, beta, bias and GELU.  Every mbarrier
 // wait is bounded; a CTA whose wait gives up waits (bounded) for its last commit, frees
 // its tensor memory and writes NaN to its tile.
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -139,6 +141,51 @@ __device__ __forceinline__ void stage_tile(const __nv_bfloat16* __restrict__ G, 
   }
 }
 
+// Epilogue of one thread: 32 accumulator columns of one output row, alpha / beta / bias /
+// GELU applied, in groups of 4 columns (one 16-byte store per output when aligned).
+__device__ __forceinline__ void store_row32(const GemmArgs& g, const uint32_t (&r)[32], int row, int col_base, bool ok,
+                                            bool vec) {
+#pragma unroll
+  for (int i0 = 0; i0 < 32; i0 += 4) {
+    const int col0 = col_base + i0;
+    if (col0 >= g.N) break;
+    const size_t o0 = (size_t)row * g.ldc + col0;
+    float v[4], pre[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int col = col0 + e;
+      float x = ok ? g.alpha * __uint_as_float(r[i0 + e]) : __int_as_float(0x7fc00000);
+      if (col < g.N) {
+        if (g.beta != 0.f) x += g.beta * g.C[o0 + e];
+        if (g.epi != EPI_NONE) x += g.bias[col];
+      }
+      pre[e] = x;
+      v[e] = g.epi == EPI_BIAS_GELU ? gelu_f(x) : x;
+    }
+    if (vec && col0 + 3 < g.N) {
+      if (g.C) *reinterpret_cast<float4*>(g.C + o0) = make_float4(v[0], v[1], v[2], v[3]);
+      if (g.Cpre && g.epi == EPI_BIAS_GELU)
+        *reinterpret_cast<float4*>(g.Cpre + o0) = make_float4(pre[0], pre[1], pre[2], pre[3]);
+      if (g.Cb) {
+        __nv_bfloat162 lo = __floats2bfloat162_rn(v[0], v[1]), hi = __floats2bfloat162_rn(v[2], v[3]);
+        uint2 q;
+        q.x = *reinterpret_cast<uint32_t*>(&lo);
+        q.y = *reinterpret_cast<uint32_t*>(&hi);
+        *reinterpret_cast<uint2*>(g.Cb + o0) = q;
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        if (col0 + e < g.N) {
+          if (g.C) g.C[o0 + e] = v[e];
+          if (g.Cpre && g.epi == EPI_BIAS_GELU) g.Cpre[o0 + e] = pre[e];
+          if (g.Cb) g.Cb[o0 + e] = __float2bfloat16(v[e]);
+        }
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(GemmArgs g) {
   extern __shared__ __align__(1024) unsigned char smem[];  // kStages x (A tile, B tile)
   __shared__ __align__(8) uint64_t mbar[kStages];
@@ -235,50 +282,153 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(GemmArgs g) {
 #pragma unroll
       for (int i = 0; i < 32; ++i) r[i] = 0u;
     }
-    if (row < g.M) {
-      // groups of 4 columns: one 16-byte store per output when the row is aligned
-      const bool vec = (g.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(g.C) & 15) == 0 &&
-                       (reinterpret_cast<uintptr_t>(g.Cpre) & 15) == 0 && (reinterpret_cast<uintptr_t>(g.Cb) & 7) == 0;
-#pragma unroll
-      for (int i0 = 0; i0 < 32; i0 += 4) {
-        const int col0 = n0 + c0 + i0;
-        if (col0 >= g.N) break;
-        const size_t o0 = (size_t)row * g.ldc + col0;
-        float v[4], pre[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int col = col0 + e;
-          float x = ok ? g.alpha * __uint_as_float(r[i0 + e]) : __int_as_float(0x7fc00000);
-          if (col < g.N) {
-            if (g.beta != 0.f) x += g.beta * g.C[o0 + e];
-            if (g.epi != EPI_NONE) x += g.bias[col];
-          }
-          pre[e] = x;
-          v[e] = g.epi == EPI_BIAS_GELU ? gelu_f(x) : x;
-        }
-        if (vec && col0 + 3 < g.N) {
-          if (g.C) *reinterpret_cast<float4*>(g.C + o0) = make_float4(v[0], v[1], v[2], v[3]);
-          if (g.Cpre && g.epi == EPI_BIAS_GELU)
-            *reinterpret_cast<float4*>(g.Cpre + o0) = make_float4(pre[0], pre[1], pre[2], pre[3]);
-          if (g.Cb) {
-            __nv_bfloat162 lo = __floats2bfloat162_rn(v[0], v[1]), hi = __floats2bfloat162_rn(v[2], v[3]);
-            uint2 q;
-            q.x = *reinterpret_cast<uint32_t*>(&lo);
-            q.y = *reinterpret_cast<uint32_t*>(&hi);
-            *reinterpret_cast<uint2*>(g.Cb + o0) = q;
-          }
-        } else {
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            if (col0 + e < g.N) {
-              if (g.C) g.C[o0 + e] = v[e];
-              if (g.Cpre && g.epi == EPI_BIAS_GELU) g.Cpre[o0 + e] = pre[e];
-              if (g.Cb) g.Cb[o0 + e] = __float2bfloat16(v[e]);
-            }
-          }
-        }
-      }
+    const bool vec = (g.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(g.C) & 15) == 0 &&
+                     (reinterpret_cast<uintptr_t>(g.Cpre) & 15) == 0 && (reinterpret_cast<uintptr_t>(g.Cb) & 7) == 0;
+    if (row < g.M) store_row32(g, r, row, n0 + c0, ok, vec);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+  }
+}
+
+// ---------------------------------------------------------------- TMA-fed variant
+// For A and B in the plain layout (k contiguous, 16-byte aligned rows) the tiles come by
+// TMA (cp.async.bulk.tensor, 128-byte swizzle) into a ring of kTmaStages stages; one
+// thread issues the loads (mbarrier transaction counts), one thread issues the MMAs and
+// releases each stage through tcgen05.commit, and all four warps run the epilogue.  The
+// shared-memory descriptors use the 128-byte swizzled K-major layout (8 rows x 128 B per
+// swizzle atom, 1024 B between 8-row groups); a K slice of 16 elements is 32 B further.
+constexpr int kTmaStages = 3;
+constexpr uint32_t kStageBytes = 2 * kTileBytes;  // A and B tiles of one stage
+
+__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr) {
+  const uint64_t lbo = 16, sbo = 1024;
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((lbo >> 4) << 16) | ((sbo >> 4) << 32) | (1ull << 46) |
+         (2ull << 61);
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(mbar)
+      : "memory");
+}
+
+__global__ void __launch_bounds__(kTcThreads) gemm_tma_kernel(const __grid_constant__ CUtensorMap mapA,
+                                                              const __grid_constant__ CUtensorMap mapB, GemmArgs g) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full[kTmaStages], empty[kTmaStages], done;
+  __shared__ uint32_t tmem_base_s;
+  __shared__ int fail;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int m0 = blockIdx.y * TBM, n0 = blockIdx.x * TBN;
+  const int nk = (g.K + TBK - 1) / TBK;
+  // stages start on a 1024-byte boundary (the swizzle atom)
+  const uint32_t sbase = (smem_u32(smem_raw) + 1023u) & ~1023u;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int i = 0; i < kTmaStages; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[i])));
     }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done)));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    fail = 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_base_s;
+
+  if (warp == 0 && lane == 0 && nk > 0) {
+    // producer: step kt -> stage kt % S, phase kt / S of full[] and empty[]
+    int issued = 0;
+    for (int kt = 0; kt < nk; ++kt) {
+      const int st = kt % kTmaStages, round = kt / kTmaStages;
+      if (kt >= kTmaStages && !mbar_wait(smem_u32(&empty[st]), (round - 1) & 1)) {
+        fail = 1;
+        break;
+      }
+      const uint32_t fb = smem_u32(&full[st]);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kStageBytes) : "memory");
+      const uint32_t a_dst = sbase + st * kStageBytes;
+      tma_load_2d(a_dst, &mapA, kt * TBK, m0, fb);
+      tma_load_2d(a_dst + kTileBytes, &mapB, kt * TBK, n0, fb);
+      issued = kt + 1;
+    }
+    // every load issued has landed before the CTA moves on
+    for (int kt = (issued > kTmaStages ? issued - kTmaStages : 0); kt < issued; ++kt)
+      if (!mbar_wait(smem_u32(&full[kt % kTmaStages]), (kt / kTmaStages) & 1)) fail = 1;
+  } else if (warp == 1 && lane == 0 && nk > 0) {
+    // MMA issuer
+    const uint32_t idesc = umma_idesc();
+    int used = 0;
+    for (int kt = 0; kt < nk; ++kt) {
+      const int st = kt % kTmaStages;
+      if (!mbar_wait(smem_u32(&full[st]), (kt / kTmaStages) & 1)) {
+        fail = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t a0 = sbase + st * kStageBytes, b0 = a0 + kTileBytes;
+#pragma unroll
+      for (int kk = 0; kk < TBK / 16; ++kk) {
+        const uint64_t ad = umma_desc_sw128(a0 + kk * 32), bd = umma_desc_sw128(b0 + kk * 32);
+        const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&empty[st]))
+                   : "memory");
+      used = kt + 1;
+    }
+    // completion of every MMA issued (a commit covers all earlier ones of this thread)
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(&done))
+                 : "memory");
+    (void)used;
+  }
+  __syncwarp();
+  bool ok = true;
+  if (nk > 0) ok = mbar_wait(smem_u32(&done), 0);
+  __syncthreads();
+  ok = __syncthreads_and(ok && fail == 0);
+  asm volatile("tcgen05.fence::after_thread_sync;");
+
+  const int row = m0 + warp * 32 + lane;
+  const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+  const bool vec = (g.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(g.C) & 15) == 0 &&
+                   (reinterpret_cast<uintptr_t>(g.Cpre) & 15) == 0 && (reinterpret_cast<uintptr_t>(g.Cb) & 7) == 0;
+#pragma unroll 1
+  for (int c0 = 0; c0 < TBN; c0 += 32) {
+    uint32_t r[32];
+    if (nk > 0 && ok) {
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+          "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          : "r"(taddr + (uint32_t)c0));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    } else {
+#pragma unroll
+      for (int i = 0; i < 32; ++i) r[i] = 0u;
+    }
+    if (row < g.M) store_row32(g, r, row, n0 + c0, ok, vec);
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -439,6 +589,28 @@ __global__ void k_sample_step(const float* __restrict__ logits, int S, int N, in
   }
 }
 
+// Tensor map of a row-major bf16 matrix (rows x k, row stride ld elements) for 128-row x
+// 64-element boxes with the 128-byte swizzle; out-of-range elements read as zero.
+static int make_tile_map(CUtensorMap* map, const void* base, int k, int rows, int ld) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    PCVL_CHECK(e == cudaSuccess && q == cudaDriverEntryPointSuccess && fn, "cuTensorMapEncodeTiled is unavailable");
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  const cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)TBK, (cuuint32_t)TBM};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  PCVL_CHECK(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return PCVL_OK;
+}
+
 static int grid1(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 65536)); }
 
 }  // namespace pcvl
@@ -459,9 +631,21 @@ extern "C" int pcvl_gemm_bf16(const void* A, const void* B, int32_t M, int32_t N
              bias, epilogue, C, (__nv_bfloat16*)Cb, Cpre};
   dim3 grid((N + TBN - 1) / TBN, (M + TBM - 1) / TBM);
   PCVL_CHECK(grid.y <= 65535, "M too large for one launch (%d)", M);
-  const int smem = kStages * 2 * (int)kTileBytes;
-  PCVL_CUDA(cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  gemm_tc_kernel<<<grid, kTcThreads, smem, (cudaStream_t)stream>>>(g);
+  // plain layouts with 16-byte aligned rows: TMA-fed kernel; anything else: cp.async
+  const bool tma = !transA && !transB && K > 0 && (lda % 8) == 0 && (ldb % 8) == 0 &&
+                   (reinterpret_cast<uintptr_t>(A) & 15) == 0 && (reinterpret_cast<uintptr_t>(B) & 15) == 0;
+  if (tma) {
+    CUtensorMap mapA, mapB;
+    PCVL_TRY(make_tile_map(&mapA, A, K, M, lda));
+    PCVL_TRY(make_tile_map(&mapB, B, K, N, ldb));
+    const int smem = kTmaStages * (int)kStageBytes + 1024;
+    PCVL_CUDA(cudaFuncSetAttribute(gemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    gemm_tma_kernel<<<grid, kTcThreads, smem, (cudaStream_t)stream>>>(mapA, mapB, g);
+  } else {
+    const int smem = kStages * 2 * (int)kTileBytes;
+    PCVL_CUDA(cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    gemm_tc_kernel<<<grid, kTcThreads, smem, (cudaStream_t)stream>>>(g);
+  }
   PCVL_CUDA(cudaGetLastError());
   return PCVL_OK;
 }
