@@ -48,26 +48,38 @@ class NaiveBackend(AStrongSimulationBackend):
         return complex(self.prob_amplitudes([output_state])[0])
 
     def prob_amplitudes(self, output_states) -> np.ndarray:
-        """Amplitudes of many outputs in one batched permanent launch."""
+        """Amplitudes of many outputs in one batched permanent launch.  The submatrices
+        of all outputs are gathered at once: output s contributes the rows of its modes
+        repeated by their counts (the same row selection as _compute_submatrix)."""
         outs = [FockState(s) for s in output_states]
         res = np.zeros(len(outs), dtype=np.complex128)
-        mats, sizes, offs, where, norms = [], [], [], [], []
-        off = 0
-        pin = self._input_state.prodnfact()
-        for i, s in enumerate(outs):
-            M = self._compute_submatrix(s)
-            if M.size == 1:
-                res[i] = M[0, 0]
-                continue
-            mats.append(M.reshape(-1))
-            sizes.append(M.shape[0])
-            offs.append(off)
-            off += M.size
-            where.append(i)
-            norms.append(math.sqrt(s.prodnfact() * pin))
-        if where:
-            perms = self._permanents(np.concatenate(mats), np.array(offs), np.array(sizes))
-            res[np.array(where)] = perms / np.array(norms)
+        if not outs:
+            return res
+        inp = self._input_state
+        n, m = inp.n, inp.m
+        counts = np.array([list(s) for s in outs], dtype=np.int64)
+        assert counts.shape[1] == m, "output state size mismatch"
+        nout = counts.sum(axis=1)
+        ok = nout == n
+        res[~ok] = 0.0
+        if n == 0:
+            res[ok] = 1.0
+            return res
+        idx = np.nonzero(ok)[0]
+        if n == 1:  # 1 x 1 submatrix: the element itself (_naive.py:46-49)
+            col = int(np.nonzero(np.asarray(list(inp)))[0][0])
+            res[idx] = self._umat[np.argmax(counts[idx] > 0, axis=1), col]
+            return res
+        # row modes of every output (sorted, repeated by count) and the input's columns
+        rows = np.repeat(np.tile(np.arange(m), len(idx)), counts[idx].reshape(-1)).reshape(len(idx), n)
+        cols = _expand(inp)
+        mats = np.ascontiguousarray(self._umat[rows[:, :, None], cols[None, None, :]])  # N x n x n
+        lfact = np.array([math.lgamma(v + 1) for v in range(n + 1)])
+        log_pout = lfact[counts[idx]].sum(axis=1)
+        norms = np.exp(0.5 * (log_pout + math.log(inp.prodnfact())))
+        offs = np.arange(len(idx), dtype=np.int64) * n * n
+        perms = self._permanents(mats.reshape(-1), offs, np.full(len(idx), n, dtype=np.int32))
+        res[idx] = perms / norms
         return res
 
     def _permanents(self, flat: np.ndarray, offs: np.ndarray, sizes: np.ndarray) -> np.ndarray:
