@@ -181,6 +181,39 @@ def cpu_perm_baseline(budget_s: float = 15.0) -> dict:
                       f"from the per-size times and the size counts"}
 
 
+def cpu_context() -> dict:
+    """The oracle (C; SLOS and permanents with OpenMP on all host threads, the samplers on
+    one thread) on bounded samples of the secondary workloads, for context beside the GPU
+    lines: about 20 s of host time."""
+    from oracle import oracle
+    from perceval_gb300.utils.matrix import random_unitary
+    out = {"threads_openmp": oracle.num_threads()}
+
+    def t(fn):
+        t0 = time.perf_counter()
+        fn()
+        return time.perf_counter() - t0
+    U12 = random_unitary(12, seed=0)
+    out["slos_m12_n6_ms"] = 1e3 * t(lambda: oracle.slos(U12, [1] * 6 + [0] * 6))
+    U20 = random_unitary(20, seed=0)
+    out["slos_m20_n10_ms"] = 1e3 * t(lambda: oracle.slos(U20, [1] * 10 + [0] * 10))
+    U16 = random_unitary(16, seed=0)
+    inp16 = [1] * 8 + [0] * 8
+    out["slos_m16_n8_one_circuit_ms"] = 1e3 * t(lambda: oracle.slos(U16, inp16))
+    w = np.random.default_rng(1).normal(size=math.comb(23, 8))
+    out["slos_grad_m16_n8_one_circuit_ms"] = 1e3 * t(lambda: oracle.slos_grad(U16, inp16, w))
+    U400 = random_unitary(400, seed=0)
+    ns = 4
+    out["cc2017_n20_m400_samples_per_s_1thread"] = ns / t(lambda: oracle.cc2017(U400, [1] * 20 + [0] * 380, ns, seed=1))
+    Ubig = random_unitary(1024, seed=0)
+    rng = np.random.default_rng(11)
+    gm = [Ubig[np.ix_(rng.choice(1024, 20, False), rng.choice(1024, 20, False))] for _ in range(20)]
+    draws = 2000
+    dt = t(lambda: [oracle.gurvits(a, draws, seed=1, first=i * draws) for i, a in enumerate(gm)])
+    out["gurvits_n20_draws_per_s_1thread"] = 20 * draws / dt
+    return out
+
+
 def run_reference(args):
     ws, rank = dist_setup()
     if rank != 0:
@@ -341,6 +374,8 @@ def run_ours(args):
         line["secondary"] = sec
     if rank == 0 and ws == 1 and not args.skip_cpu:
         line["cpu_baseline"] = cpu_perm_baseline()
+        if "secondary" in line:
+            line["secondary"]["cpu_context"] = cpu_context()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -384,6 +419,13 @@ def secondary(torch, _native, random_unitary, dev, flush):
                            "sum_p": float(probs.sum())}
     del plan, probs
     torch.cuda.empty_cache()
+    plan = _native.SlosPlan(20, [1] * 10 + [0] * 10)
+    U20 = torch.from_numpy(random_unitary(20, seed=0)).to(dev)
+    t_f20 = timed(lambda: plan.forward(U20), reps=3)
+    p20 = plan.probabilities()
+    t_p20 = timed(lambda: plan.probabilities(p20), reps=3)
+    res["slos_m20_n10"] = {"forward_ms": t_f20, "probabilities_ms": t_p20, "outputs": plan.count}
+    del plan, p20
     # batched forward + adjoint, 256 Clements meshes m=16, n=8
     from perceval_gb300.components.mesh import clements_mesh_unitary
     ph = torch.from_numpy(np.random.default_rng(0).uniform(0, 2 * math.pi, (256, 240)))
