@@ -419,6 +419,25 @@ def secondary(torch, _native, random_unitary, dev, flush):
                            "sum_p": float(probs.sum())}
     del plan, probs
     torch.cuda.empty_cache()
+    # the same circuit heralded: modes 20..23 detected as 1, 1, 0, 0 (a masked plan keeps only
+    # the states that can still end with that pattern)
+    from perceval_gb300.utils import FSMask
+    herald = "*" * 20 + "1100"
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plan = _native.SlosPlan(m, [1] * n + [0] * (m - n), mask=FSMask(m, n, [herald]))
+    torch.cuda.synchronize()
+    t_build = 1e3 * (time.perf_counter() - t0)
+    t_fm = timed(lambda: plan.forward(Ud), reps=3)
+    pm = plan.probabilities()
+    t_pm = timed(lambda: plan.probabilities(pm), reps=3)
+    res["slos_masked_m24_n12_heralded"] = {
+        "mask": herald, "kept_outputs": plan.count, "full_outputs": Ls[n], "plan_build_ms": t_build,
+        "forward_ms": t_fm, "probabilities_ms": t_pm, "full_forward_ms": t_fwd, "speedup_vs_full": t_fwd / t_fm,
+        "kept_amps_per_s": plan.count / (t_fm * 1e-3), "device_gb": plan.device_bytes / 1e9,
+        "heralded_probability": float(pm.sum())}
+    del plan, pm
+    torch.cuda.empty_cache()
     plan = _native.SlosPlan(20, [1] * 10 + [0] * 10)
     U20 = torch.from_numpy(random_unitary(20, seed=0)).to(dev)
     t_f20 = timed(lambda: plan.forward(U20), reps=3)
@@ -686,6 +705,14 @@ def profile_case(name: str):
         plan = _native.SlosPlan(20, [1] * 10 + [0] * 10)
         plan.forward(torch.from_numpy(random_unitary(20, seed=0)).to(dev))
         plan.probabilities()
+    elif name == "slosmask22":
+        # heralded SLOS m = 22, n = 11 (modes 18..21 detected as 1, 1, 0, 0): the largest kept
+        # layer (k = 10) holds 7,330,675 states, 117 MB of amplitudes plus 0.3 GB of parent
+        # tables (above L2); about 1 GB on the device
+        from perceval_gb300.utils import FSMask
+        plan = _native.SlosPlan(22, [1] * 11 + [0] * 11, mask=FSMask(22, 11, ["*" * 18 + "1100"]))
+        plan.forward(torch.from_numpy(random_unitary(22, seed=0)).to(dev))
+        plan.probabilities()
     elif name == "slos16b256":
         from perceval_gb300.components.mesh import clements_mesh_unitary
         ph = torch.from_numpy(np.random.default_rng(0).uniform(0, 2 * math.pi, (256, 240)))
@@ -726,7 +753,8 @@ def main():
                     help="run the learned-proposal sampler workload (n=30, m=900 and n=8, m=64) and exit")
     ap.add_argument("--learned-train", type=int, default=2048, help="exact training samples at n=30")
     ap.add_argument("--large-perm", action="store_true", help="one n = 40 permanent (about a minute)")
-    ap.add_argument("--profile-case", choices=["perm24", "slos20", "slos16b256", "cc2017", "gurvits20", "gemm"],
+    ap.add_argument("--profile-case", choices=["perm24", "slos20", "slosmask22", "slos16b256", "cc2017", "gurvits20",
+                                               "gemm"],
                     help="run one small untimed case of a single kernel (for ncu) and exit")
     args = ap.parse_args()
     if args.profile_case:

@@ -135,8 +135,27 @@ int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int32_t* input
  * prod(in_b!). */
 int pcvl_slos_plan_create_multi(pcvl_slos_plan** plan, int32_t m, const int32_t* input_states_h,
                                 int32_t batch, int32_t keep_layers);
+/* Plan restricted by a mask: replaces xq.FSMask + xq.FSArray(m, k, mask) /
+ * xq.FSMap(cur, prev, True) of a masked SLOSBackend (perceval/backends/_abstract_backends.py:
+ * 103-137 set_mask / _init_mask; perceval/backends/_slos.py:152-166 _deploy).  Mask q is
+ * digits_h[q * m .. q * m + m - 1]: a count >= 0 fixes mode i, -1 accepts any count; bit i
+ * of at_least_modes makes mode i's digit a lower bound.  A state is accepted when it
+ * matches one of the n_masks masks.  Layer k keeps only the k-photon states that can still
+ * be completed to an accepted state of mask_n photons, so the plan's outputs are the
+ * accepted n-photon states (when mask_n == n) in descending lexicographic order; their
+ * count is pcvl_slos_output_count and their ranks in the full space
+ * pcvl_slos_output_ranks.  Input states as pcvl_slos_plan_create_multi (batch x m, host;
+ * one photon count).  Forward, probabilities, amplitudes and backward take the same
+ * arguments as for a full plan, indexed by kept output. */
+int pcvl_slos_plan_create_masked(pcvl_slos_plan** plan, int32_t m, const int32_t* input_states_h,
+                                 int32_t batch, int32_t keep_layers, int32_t n_masks,
+                                 const int8_t* digits_h, uint32_t at_least_modes, int32_t mask_n);
+/* Ranks of the plan's outputs in the full n-photon space (descending lexicographic order,
+ * rank 0 = |n,0,..,0>), ascending: ranks_h receives pcvl_slos_output_count entries (host).
+ * For a plan without mask this is 0, 1, 2, ... */
+int pcvl_slos_output_ranks(const pcvl_slos_plan* plan, uint64_t* ranks_h);
 int pcvl_slos_plan_destroy(pcvl_slos_plan* plan);
-/* Number of output states C(m+n-1, n) of the plan. */
+/* Number of output states of the plan: C(m+n-1, n), or the kept outputs of a masked plan. */
 int pcvl_slos_output_count(const pcvl_slos_plan* plan, int64_t* count);
 /* Device bytes the plan holds. */
 int pcvl_slos_plan_bytes(const pcvl_slos_plan* plan, int64_t* bytes);

@@ -41,6 +41,11 @@ SYMBOLS = {
                                              ctypes.c_int32, ctypes.c_int32]),
     "pcvl_slos_plan_create_multi": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
                                                    ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
+    "pcvl_slos_plan_create_masked": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
+                                                     ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                                     ctypes.c_int32, ctypes.c_void_p, ctypes.c_uint32,
+                                                     ctypes.c_int32]),
+    "pcvl_slos_output_ranks": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "pcvl_slos_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "pcvl_slos_forward_shared": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "pcvl_slos_output_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
@@ -262,13 +267,35 @@ class SlosPlan:
 
     ``input_state`` is one state shared by the ``batch`` entries, or a (batch x m)
     array of per-entry states with one photon count (``pcvl_slos_plan_create_multi``).
+    ``mask`` (an ``FSMask``) restricts every layer to the states the mask can still
+    accept (``pcvl_slos_plan_create_masked``): the outputs are then the accepted states,
+    ``output_ranks()`` gives their ranks in the full n-photon space.
     """
 
-    def __init__(self, m: int, input_state, batch: int = 1, keep_layers: bool = False):
+    def __init__(self, m: int, input_state, batch: int = 1, keep_layers: bool = False, mask=None):
         self._lib = load()
         inp = np.ascontiguousarray(input_state, dtype=np.int32)
         h = ctypes.c_void_p()
-        if inp.ndim == 2:
+        self.masked = mask is not None
+        if mask is not None:
+            if inp.ndim == 1:
+                if inp.shape != (m,):
+                    raise ValueError("input_state must have m entries")
+                self.input_state = tuple(int(v) for v in inp)
+                inp = np.ascontiguousarray(np.tile(inp, (int(batch), 1)))
+            elif inp.ndim != 2 or inp.shape[1] != m or inp.shape[0] < 1:
+                raise ValueError("input states must form a (batch x m) array")
+            else:
+                self.input_state = [tuple(int(v) for v in row) for row in inp]
+            batch = inp.shape[0]
+            digits, at_least, mask_n = mask.device_spec()
+            if digits.shape[1] != m:
+                raise ValueError("mask and input state lengths differ")
+            check(self._lib.pcvl_slos_plan_create_masked(ctypes.byref(h), int(m), inp.ctypes.data, int(batch),
+                                                         1 if keep_layers else 0, int(digits.shape[0]),
+                                                         digits.ctypes.data, int(at_least), int(mask_n)),
+                  "pcvl_slos_plan_create_masked")
+        elif inp.ndim == 2:
             if inp.shape[1] != m or inp.shape[0] < 1:
                 raise ValueError("input states must form a (batch x m) array")
             batch = inp.shape[0]
@@ -286,6 +313,13 @@ class SlosPlan:
         c = ctypes.c_int64()
         check(self._lib.pcvl_slos_output_count(h, ctypes.byref(c)), "pcvl_slos_output_count")
         self.count = int(c.value)
+
+    def output_ranks(self) -> np.ndarray:
+        """Ranks of the plan's outputs in the full n-photon space (descending
+        lexicographic order), ascending; 0 .. count-1 without a mask."""
+        out = np.empty(self.count, dtype=np.uint64)
+        check(self._lib.pcvl_slos_output_ranks(self._h, out.ctypes.data), "pcvl_slos_output_ranks")
+        return out
 
     @property
     def device_bytes(self) -> int:
@@ -308,6 +342,8 @@ class SlosPlan:
     def probabilities(self, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
         if out is None:
             out = torch.empty(self.count * self.batch, dtype=torch.float64, device="cuda")
+        if self.count == 0:  # a mask that accepts no output
+            return out
         _dev_tensor(out, torch.float64, "out")
         check(self._lib.pcvl_slos_probabilities(self._h, out.data_ptr(), _stream_ptr(stream)),
               "pcvl_slos_probabilities")
@@ -316,6 +352,8 @@ class SlosPlan:
     def amplitudes(self, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
         if out is None:
             out = torch.empty(self.count * self.batch, dtype=torch.complex128, device="cuda")
+        if self.count == 0:
+            return out
         _dev_tensor(out, torch.complex128, "out")
         check(self._lib.pcvl_slos_amplitudes(self._h, out.data_ptr(), _stream_ptr(stream)),
               "pcvl_slos_amplitudes")
@@ -327,6 +365,8 @@ class SlosPlan:
             raise ValueError("weights must hold count x batch elements (state-major)")
         if grad_u is None:
             grad_u = torch.empty(self.batch * self.m * self.m, dtype=torch.complex128, device="cuda")
+        if self.count == 0:  # L is identically zero
+            return grad_u.zero_()
         _dev_tensor(grad_u, torch.complex128, "grad_u")
         check(self._lib.pcvl_slos_backward(self._h, weights.data_ptr(), grad_u.data_ptr(), _stream_ptr(stream)),
               "pcvl_slos_backward")

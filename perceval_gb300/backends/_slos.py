@@ -7,7 +7,9 @@ reference, changing the circuit to another one of the same size keeps the plans 
 recomputes their coefficients (_slos.py:130-141); a different size resets them.
 
 Outputs come back in descending-lexicographic order (the reference's
-``allstate_iterator`` order).  ``all_prob`` returns a list up to 2^22 outputs and a
+``allstate_iterator`` order).  With a mask (``set_mask``) the plans are masked plans:
+every layer holds only the states the mask can still accept (xq.FSArray(m, k, mask),
+_slos.py:161-164), and the outputs are the accepted states in the same order.  ``all_prob`` returns a list up to 2^22 outputs and a
 numpy array above; ``all_prob_tensor`` leaves the probabilities on the device.
 
 ``all_probs_many`` / ``prob_distributions`` evaluate many input states of the circuit
@@ -24,7 +26,7 @@ import numpy as np
 import torch
 
 from .. import _native
-from ..utils.states import BSDistribution, FockState, StateVector, fock_rank, fock_space_array
+from ..utils.states import BSDistribution, FSMask, FockState, StateVector, fock_rank, fock_unrank_array
 from ._abstract_backends import AStrongSimulationBackend, _as_circuit
 
 _LIST_LIMIT = 1 << 22
@@ -39,6 +41,7 @@ class _Entry:
         self.probs = None            # device tensor
         self.amps = None             # device tensor
         self.amps_host = None        # numpy copy (small spaces)
+        self.ranks = None            # masked plan: full-space ranks of the accepted outputs
 
 
 class SLOSBackend(AStrongSimulationBackend):
@@ -74,6 +77,7 @@ class SLOSBackend(AStrongSimulationBackend):
 
     def clear_mask(self):
         super().clear_mask()
+        self._reset()  # plans are built for a mask (_slos.py:147-149)
 
     def _unitary_device(self) -> torch.Tensor:
         if self._u_dev is None:
@@ -89,7 +93,9 @@ class SLOSBackend(AStrongSimulationBackend):
         st = self._input_state
         e = self._entries.get(st)
         if e is None:
-            e = _Entry(_native.SlosPlan(st.m, list(st), batch=1, keep_layers=False))
+            e = _Entry(_native.SlosPlan(st.m, list(st), batch=1, keep_layers=False, mask=self._mask))
+            if self._mask is not None:
+                e.ranks = e.plan.output_ranks()
             self._entries[st] = e
         if not e.fresh:
             e.plan.forward(self._unitary_device())
@@ -99,7 +105,8 @@ class SLOSBackend(AStrongSimulationBackend):
 
     # -------------------------------------------------------------- results
     def all_prob_tensor(self, input_state=None) -> torch.Tensor:
-        """Probabilities of every output (no mask) as a float64 CUDA tensor, rank order."""
+        """Probabilities of every output (the accepted ones under a mask) as a float64
+        CUDA tensor, in descending-lexicographic order."""
         if input_state is not None:
             self.set_input_state(input_state)
         e = self._entry()
@@ -108,19 +115,27 @@ class SLOSBackend(AStrongSimulationBackend):
         return e.probs
 
     def amplitudes_tensor(self) -> torch.Tensor:
-        """Amplitudes of every output as a complex128 CUDA tensor, rank order."""
+        """Amplitudes of every output (the accepted ones under a mask) as a complex128
+        CUDA tensor, in descending-lexicographic order."""
         e = self._entry()
         if e.amps is None:
             e.amps = e.plan.amplitudes()
         return e.amps
 
-    def _mask_indices(self, m: int | None = None, n: int | None = None) -> np.ndarray | None:
-        if self._mask is None:
+    def _get_iterator(self, input_state):
+        # under a mask, the accepted outputs are the plan's own (no full-space enumeration)
+        if self._mask is not None and isinstance(input_state, FockState) and input_state.n not in self._cache_iterator:
+            e = self._entries.get(input_state)
+            if e is not None and e.ranks is not None:
+                arr = fock_unrank_array(input_state.m, input_state.n, e.ranks)
+                self._cache_iterator[input_state.n] = tuple(FockState(row) for row in arr)
+        return super()._get_iterator(input_state)
+
+    def _group_mask(self, m: int, n: int) -> FSMask | None:
+        """The mask of an input state of n photons (_abstract_backends.py:126-137)."""
+        if self._masks_str is None:
             return None
-        if m is None:
-            m, n = self._input_state.m, self._input_state.n
-        arr = fock_space_array(m, n)
-        return np.nonzero(self._mask.match_array(arr))[0]
+        return FSMask(m, self._mask_n or n, self._masks_str, self._no_limit_modes)
 
     def all_probs_many(self, input_states, max_device_bytes: int = 1 << 31) -> list[np.ndarray]:
         """Probabilities of every output (descending-lexicographic order, mask applied)
@@ -139,19 +154,18 @@ class SLOSBackend(AStrongSimulationBackend):
             # two float-float layers per entry dominate a plan's memory
             per_entry = 2 * 16 * max(count, 1)
             step = max(1, min(len(idxs), max_device_bytes // per_entry))
-            sel = self._mask_indices(m, n)
+            mask = self._group_mask(m, n)
             for c0 in range(0, len(idxs), step):
                 chunk = idxs[c0:c0 + step]
                 arr = np.array([list(states[i]) for i in chunk], dtype=np.int32)
-                plan = _native.SlosPlan(m, arr, keep_layers=False)
+                plan = _native.SlosPlan(m, arr, keep_layers=False, mask=mask)
                 try:
                     plan.forward(U)
                     host = plan.probabilities().view(plan.count, len(chunk)).cpu().numpy()
                 finally:
                     plan.close()
                 for col, i in enumerate(chunk):
-                    p = np.ascontiguousarray(host[:, col])
-                    res[i] = p if sel is None else p[sel]
+                    res[i] = np.ascontiguousarray(host[:, col])
         return res
 
     def prob_distributions(self, input_states) -> list[BSDistribution]:
@@ -169,9 +183,6 @@ class SLOSBackend(AStrongSimulationBackend):
         if input_state is not None:
             self.set_input_state(input_state)
         probs = self.all_prob_tensor().cpu().numpy()
-        idx = self._mask_indices()
-        if idx is not None:
-            probs = probs[idx]
         return probs.tolist() if probs.size <= _LIST_LIMIT else probs
 
     def prob_distribution(self) -> BSDistribution:
@@ -188,6 +199,10 @@ class SLOSBackend(AStrongSimulationBackend):
         assert output_state.m == self._input_state.m, "output state size mismatch"
         e = self._entry()
         r = fock_rank(output_state)
+        if e.ranks is not None:  # index among the accepted outputs (_slos.py:190-191)
+            pos = int(np.searchsorted(e.ranks, np.uint64(r)))
+            assert pos < len(e.ranks) and int(e.ranks[pos]) == r, "output state is not accepted by the mask"
+            r = pos
         if e.plan.count <= _LIST_LIMIT:
             if e.amps_host is None:
                 e.amps_host = self.amplitudes_tensor().cpu().numpy()
@@ -196,10 +211,8 @@ class SLOSBackend(AStrongSimulationBackend):
 
     def evolve(self) -> StateVector:
         amps = self.amplitudes_tensor().cpu().numpy()
-        idx = self._mask_indices()
         res = StateVector()
         states = self._get_iterator(self._input_state)
-        sel = amps if idx is None else amps[idx]
-        for s, a in zip(states, sel):
+        for s, a in zip(states, amps):
             res[s] = complex(a)
         return res

@@ -49,6 +49,7 @@
 
 #include "common.cuh"
 #include "runtime.cuh"
+#include "slos_plan.cuh"
 
 namespace pcvl {
 
@@ -722,32 +723,6 @@ static int dispatch(Kern kind, const SlosArgs& a, int grid, cudaStream_t s, dd i
 
 using namespace pcvl;
 
-struct pcvl_slos_plan {
-  int m = 0, n = 0, B = 0;
-  bool keep = false;
-  std::vector<int> inputs;        // B x m input states (same photon count)
-  std::vector<int32_t> col;       // n x B: input mode of photon k of entry b -> col[(k-1) * B + b]
-  std::vector<uint64_t> sizes;    // layer sizes, k = 0..n
-  int cn_stride = 0;
-  uint32_t* cn_d = nullptr;
-  int32_t* col_d = nullptr;
-  dd* inv_in_d = nullptr;         // 1 / prod(in_b!) per entry
-  cdd* ucols_d = nullptr;         // [k][j][b]
-  std::vector<cdd*> layers;       // keep: every layer; else layers[k % 2] ping-pong
-  cdd* adj_d[2] = {nullptr, nullptr};
-  cdd* gpart_d = nullptr;
-  int gpart_blocks = 0;
-  int64_t bytes = 0;
-  bool forwarded = false;
-  int tail_t = 0, tail_p = 0;
-  uint32_t* tp_d = nullptr;       // rank_t(tau - e_j) per tail state and tail mode
-  uint32_t* tc_d = nullptr;       // rank_t(tau + e_j)
-  uint8_t* tocc_d = nullptr;      // occupied tail modes per tail state
-  dd* ftail_d = nullptr;          // prod tau_j! per tail state
-  std::vector<uint32_t> tail_off, tstate_off, tsize;
-  cdd* final_layer() const { return keep ? layers[n] : layers[n % 2]; }
-};
-
 namespace {
 
 void free_plan(pcvl_slos_plan* p) {
@@ -764,6 +739,7 @@ void free_plan(pcvl_slos_plan* p) {
   cudaFree(p->tc_d);
   cudaFree(p->tocc_d);
   cudaFree(p->ftail_d);
+  slos_masked_free(p);
   delete p;
 }
 
@@ -940,6 +916,11 @@ int grid_for_units(const SlosArgs& a, bool fwd1 = false) {
 
 }  // namespace
 
+int pcvl::slos_alloc(void** p, size_t bytes, int64_t& total) { return alloc(p, bytes, total); }
+int pcvl::slos_upload(void* dst, const void* src, size_t bytes) { return upload(dst, src, bytes); }
+std::vector<int> pcvl::slos_path_order(const std::vector<int>& input) { return path_order(input); }
+void pcvl::slos_free_plan(pcvl_slos_plan* p) { free_plan(p); }
+
 // Plan for `batch` entries with input states inputs[b * m .. b * m + m - 1].
 static int create_plan(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, int32_t batch, int32_t keep_layers) {
   PCVL_CHECK(plan && inputs, "null pointer argument");
@@ -1108,6 +1089,11 @@ static int forward(pcvl_slos_plan* p, const double* u_d, size_t ustride, cudaStr
   PCVL_CUDA(cudaGetLastError());
   slos_fill_vacuum<<<(B + 255) / 256, 256, 0, s>>>(p->layers[0], B);
   PCVL_CUDA(cudaGetLastError());
+  if (p->masked) {
+    PCVL_TRY(slos_masked_forward(p, s));
+    p->forwarded = true;
+    return PCVL_OK;
+  }
   for (int k = 1; k <= p->n; ++k) {
     SlosArgs a = make_args(p, k);
     a.in = p->keep ? p->layers[k - 1] : p->layers[(k - 1) % 2];
@@ -1137,6 +1123,7 @@ extern "C" int pcvl_slos_forward_shared(pcvl_slos_plan* p, const double* u_d, vo
 static int finalize(pcvl_slos_plan* p, int mode, const double* w, double* out_real, double2* out_c, cdd* seed,
                     cudaStream_t s) {
   PCVL_CHECK(p->forwarded, "pcvl_slos_forward has not run on this plan");
+  if (p->masked) return slos_masked_finalize(p, mode, w, out_real, out_c, seed, s);
   SlosArgs a = make_args(p, p->n);
   a.in = p->final_layer();
   const int rc = dispatch(Kern::Fin, a, grid_for_units(a, p->B == 1), s, dd_from_double(1.0),
@@ -1163,6 +1150,7 @@ extern "C" int pcvl_slos_backward(pcvl_slos_plan* p, const double* weights_d, do
   PCVL_CHECK(p->keep, "pcvl_slos_backward needs a plan created with keep_layers != 0");
   PCVL_CHECK(p->forwarded, "pcvl_slos_forward has not run on this plan");
   cudaStream_t s = (cudaStream_t)stream_;
+  if (p->masked) return slos_masked_backward(p, weights_d, grad_u_d, s);
   const int m = p->m, B = p->B, n = p->n;
   PCVL_CUDA(cudaMemsetAsync(grad_u_d, 0, (size_t)B * m * m * 2 * sizeof(double), s));
   PCVL_TRY(finalize(p, 2, weights_d, nullptr, nullptr, p->adj_d[n % 2], s));

@@ -272,6 +272,27 @@ def fock_unrank(m: int, n: int, rank: int) -> FockState:
     return FockState(out)
 
 
+def fock_unrank_array(m: int, n: int, ranks) -> np.ndarray:
+    """Occupation vectors (rows) of the states with the given ranks in the n-photon
+    space on m modes; vectorised ``fock_unrank``."""
+    r = np.asarray(ranks, dtype=np.int64).copy()
+    out = np.zeros((len(r), m), dtype=np.int32)
+    rest = np.full(len(r), n, dtype=np.int64)
+    for i in range(m - 1):
+        # photons after mode i: smallest x with rank < count(m - i, x); offset count(m - i, x - 1)
+        after = np.zeros(len(r), dtype=np.int64)
+        for x in range(n + 1):
+            cum = fock_space_size(m - i, x)
+            after += (r >= cum) & (after == x) & (x < rest)
+        prev = np.array([fock_space_size(m - i, int(x) - 1) if x > 0 else 0 for x in range(n + 1)],
+                        dtype=np.int64)
+        r = r - prev[after]
+        out[:, i] = rest - after
+        rest = after
+    out[:, m - 1] = rest
+    return out
+
+
 def allstate_iterator(input_state, mask=None) -> Iterator[FockState]:
     """Iterate all output states with the input's photon number(s), respecting a mask.
 
@@ -285,7 +306,7 @@ def allstate_iterator(input_state, mask=None) -> Iterator[FockState]:
     for n in ns:
         arr = fock_space_array(m, n)
         if mask is not None:
-            arr = arr[mask.match_array(arr)]
+            arr = arr[mask.accepts_space(arr)]
         for row in arr:
             yield FockState(row)
 
@@ -315,6 +336,7 @@ class FSMask:
         self.n = n
         self._conds = []
         at_least = set(at_least_modes or [])
+        self._at_least = at_least
         for s in masks:
             s = s.replace("*", " ")
             assert len(s) == m, "Mask and state lengths have to be the same"
@@ -351,12 +373,42 @@ class FSMask:
             return missing <= self.n - state.n
         return True
 
-    def match_array(self, arr: np.ndarray) -> np.ndarray:
-        """Vectorised ``match`` over rows of an occupation array (full match only)."""
+    def match_array(self, arr: np.ndarray, partial: bool = False) -> np.ndarray:
+        """Vectorised ``match`` over rows of an occupation array."""
         ok = np.zeros(arr.shape[0], dtype=bool)
+        spare = self.n - arr.sum(axis=1)
         for cond in self._conds:
             cur = np.ones(arr.shape[0], dtype=bool)
+            missing = np.zeros(arr.shape[0], dtype=np.int64)
             for i, d, at_least in cond:
-                cur &= (arr[:, i] >= d) if at_least else (arr[:, i] == d)
+                v = arr[:, i]
+                if not partial:
+                    cur &= (v >= d) if at_least else (v == d)
+                elif at_least:
+                    missing += np.maximum(d - v, 0)
+                else:
+                    cur &= v <= d
+                    missing += d - v
+            if partial:
+                cur &= missing <= spare
             ok |= cur
         return ok
+
+    def accepts_space(self, arr: np.ndarray) -> np.ndarray:
+        """The states of one layer that ``xq.FSArray(m, k, mask)`` keeps: those that can
+        still be completed to a match with ``n`` photons (a full match when they hold
+        ``n`` photons)."""
+        return self.match_array(arr, partial=True)
+
+    def device_spec(self):
+        """(digits, at_least bits, n) for ``pcvl_slos_plan_create_masked``: digits is an
+        int8 (masks x m) array with -1 where a mask accepts any count."""
+        digits = np.full((len(self._conds), self.m), -1, dtype=np.int8)
+        for q, cond in enumerate(self._conds):
+            for i, d, _ in cond:
+                digits[q, i] = d
+        bits = 0
+        for i in self._at_least:
+            if 0 <= i < self.m:
+                bits |= 1 << i
+        return np.ascontiguousarray(digits), bits, self.n

@@ -51,6 +51,32 @@ def test_mask_reference():
     assert not mask.match(BasicState("|0,0,1,1,1,1>"))
 
 
+def test_mask_layers_and_device_spec():
+    """The vectorised partial / full matches agree with ``match`` on every layer; the
+    kept layers are closed under removing a photon (what a masked SLOS plan relies on);
+    the device encoding carries the digits, the at-least modes and the photon count."""
+    from perceval_gb300.utils.states import fock_rank, fock_space_array, fock_unrank_array
+    mask = FSMask(7, 4, ["   01 1", " 2   0 "], at_least_modes=[6])
+    for k in range(6):
+        arr = fock_space_array(7, k)
+        part = mask.match_array(arr, partial=True)
+        assert np.array_equal(part, [mask.match(BasicState(list(s)), True) for s in arr])
+        assert np.array_equal(mask.match_array(arr), [mask.match(BasicState(list(s))) for s in arr])
+        for s in arr[part]:
+            for j in np.nonzero(s)[0]:
+                p = s.copy()
+                p[j] -= 1
+                assert mask.match(BasicState(list(p)), True)
+    assert np.array_equal(mask.accepts_space(fock_space_array(7, 4)), mask.match_array(fock_space_array(7, 4)))
+    digits, bits, n = mask.device_spec()
+    assert digits.tolist() == [[-1, -1, -1, 0, 1, -1, 1], [-1, 2, -1, -1, -1, 0, -1]]
+    assert bits == 1 << 6 and n == 4
+    ranks = np.array([0, 5, 17, 83, 209])
+    arr = fock_unrank_array(7, 4, ranks)
+    assert [fock_rank(list(s)) for s in arr] == ranks.tolist()
+    assert np.array_equal(fock_unrank_array(7, 4, np.arange(210)), fock_space_array(7, 4))
+
+
 def test_bsdistribution_and_counts():
     d = BSDistribution()
     d.add(BasicState([1, 0]), 0.25)
