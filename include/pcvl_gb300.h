@@ -175,6 +175,33 @@ int pcvl_slos_amplitudes(pcvl_slos_plan* plan, double* amps_d, void* stream);
 int pcvl_slos_backward(pcvl_slos_plan* plan, const double* weights_d, double* grad_u_d,
                        void* stream);
 
+/* ------------------------------------------------------------------ SLAP
+ * Replaces xq.SLAP for circuits without feed-forward (perceval/backends/_slap.py:38-80:
+ * set_unitary, all_prob_ampli, all_prob, prob_distribution).  Every output of one input
+ * state (m <= 4096 modes, n <= 12 photons, at most 2^36 outputs) in descending
+ * lexicographic order, computed by a depth-first walk over the outputs that keeps one
+ * table of 2^n photon-subset values per walker: no intermediate Fock layers.  u_d is the
+ * m x m complex128 unitary (device), input_state_h the input occupation (host). */
+int pcvl_slap_output_count(int32_t m, const int32_t* input_state_h, int64_t* count);
+/* probs_d[r] = |Perm(U_{s_r,t})|^2 / (prod s_r! prod t!)   (count float64) */
+int pcvl_slap_probabilities(const double* u_d, int32_t m, const int32_t* input_state_h, double* probs_d,
+                            void* stream);
+/* amps_d[r] = Perm(U_{s_r,t}) / sqrt(prod s_r! prod t!)   (count complex128) */
+int pcvl_slap_amplitudes(const double* u_d, int32_t m, const int32_t* input_state_h, double* amps_d,
+                         void* stream);
+
+/* The outputs a mask keeps among the n-photon states on m modes (m <= 4096): replaces
+ * iterating xq.FSArray(m, n, mask) (perceval/utils/states.py:255-290, with the mask of
+ * perceval/backends/_abstract_backends.py:126-137) for any number of modes.  Mask q is
+ * digits_h[q * m .. q * m + m - 1] (count >= 0, or -1 for any); at_least_h (m flags, host,
+ * may be NULL) marks modes whose digit is a lower bound; mask_n is the mask's photon
+ * count.  *kept receives the number of kept states; with ranks_d non-NULL (device,
+ * capacity entries) their ranks in descending lexicographic order are written
+ * ascending.  Synchronous. */
+int pcvl_fock_mask_ranks(int32_t m, int32_t n, int32_t n_masks, const int8_t* digits_h,
+                         const uint8_t* at_least_h, int32_t mask_n, uint64_t* ranks_d, int64_t capacity,
+                         int64_t* kept);
+
 /* ------------------------------------------------------------------ sampling
  * Replaces xq.Clifford2017 (perceval/backends/_clifford2017.py:36-57:
  * set_unitary / set_input_state / sample / samples).

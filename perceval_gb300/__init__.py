@@ -5,7 +5,7 @@ CUDA kernels through the C ABI of ``lib/libpcvl_gb300.so`` (declared in
 ``include/pcvl_gb300.h``); there is no CPU fallback.
 """
 from .backends import (BACKEND_LIST, ABackend, ASamplingBackend, AStrongSimulationBackend, BackendFactory,
-                       Clifford2017Backend, NaiveApproxBackend, NaiveBackend, SLOSBackend)
+                       Clifford2017Backend, NaiveApproxBackend, NaiveBackend, SLAPBackend, SLOSBackend)
 from .components import BS, PERM, PS, Circuit, GenericInterferometer, Unitary, catalog
 from .utils import (BasicState, BSCount, BSDistribution, BSSamples, FockState, StateVector, Matrix,
                     allstate_iterator, random_seed)

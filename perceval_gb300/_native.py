@@ -47,6 +47,14 @@ SYMBOLS = {
                                                      ctypes.c_int32]),
     "pcvl_slos_output_ranks": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "pcvl_slos_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "pcvl_fock_mask_ranks": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64,
+                                             ctypes.POINTER(ctypes.c_int64)]),
+    "pcvl_slap_output_count": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
+    "pcvl_slap_probabilities": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                                ctypes.c_void_p]),
+    "pcvl_slap_amplitudes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                             ctypes.c_void_p]),
     "pcvl_slos_forward_shared": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "pcvl_slos_output_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     "pcvl_slos_plan_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
@@ -382,6 +390,60 @@ class SlosPlan:
             self.close()
         except Exception:
             pass
+
+
+# ------------------------------------------------------------------ SLAP
+def slap_output_count(m: int, input_state) -> int:
+    lib = load()
+    inp = np.ascontiguousarray(input_state, dtype=np.int32)
+    if inp.shape != (m,):
+        raise ValueError("input_state must have m entries")
+    c = ctypes.c_int64()
+    check(lib.pcvl_slap_output_count(int(m), inp.ctypes.data, ctypes.byref(c)), "pcvl_slap_output_count")
+    return int(c.value)
+
+
+def slap_all(u: torch.Tensor, input_state, amplitudes: bool = False, out: torch.Tensor | None = None,
+             stream=None) -> torch.Tensor:
+    """Every output probability (float64) or amplitude (complex128) of one input state,
+    in descending-lexicographic order, by the SLAP walk (``pcvl_slap_probabilities`` /
+    ``pcvl_slap_amplitudes``)."""
+    lib = load()
+    _dev_tensor(u, torch.complex128, "u")
+    m = u.shape[-1]
+    inp = np.ascontiguousarray(input_state, dtype=np.int32)
+    count = slap_output_count(m, inp)
+    dt = torch.complex128 if amplitudes else torch.float64
+    if out is None:
+        out = torch.empty(count, dtype=dt, device="cuda")
+    _dev_tensor(out, dt, "out")
+    if out.numel() < count:
+        raise ValueError("out holds fewer than the output count")
+    fn = lib.pcvl_slap_amplitudes if amplitudes else lib.pcvl_slap_probabilities
+    check(fn(u.data_ptr(), int(m), inp.ctypes.data, out.data_ptr(), _stream_ptr(stream)),
+          "pcvl_slap_amplitudes" if amplitudes else "pcvl_slap_probabilities")
+    return out
+
+
+def fock_mask_ranks(m: int, n: int, mask) -> torch.Tensor:
+    """Ranks (int64 CUDA tensor, ascending) of the n-photon states on m modes that the
+    ``FSMask`` keeps (``pcvl_fock_mask_ranks``)."""
+    lib = load()
+    digits, _, mask_n = mask.device_spec()
+    if digits.shape[1] != m:
+        raise ValueError("mask and state lengths differ")
+    atl = np.zeros(m, dtype=np.uint8)
+    for i in mask.at_least_modes:
+        if 0 <= i < m:
+            atl[i] = 1
+    kept = ctypes.c_int64()
+    args = (int(m), int(n), int(digits.shape[0]), digits.ctypes.data, atl.ctypes.data, int(mask_n))
+    check(lib.pcvl_fock_mask_ranks(*args, None, 0, ctypes.byref(kept)), "pcvl_fock_mask_ranks")
+    out = torch.empty(max(kept.value, 1), dtype=torch.int64, device="cuda")
+    if kept.value:
+        check(lib.pcvl_fock_mask_ranks(*args, out.data_ptr(), int(kept.value), ctypes.byref(kept)),
+              "pcvl_fock_mask_ranks")
+    return out[:kept.value]
 
 
 # ------------------------------------------------------------------ sampling

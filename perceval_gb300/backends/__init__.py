@@ -1,7 +1,7 @@
 """Backend registry and factory (perceval/backends/__init__.py:39-62).
 
 ``BackendFactory.get_backend(name)`` returns a GPU backend for the names of the hot
-path ("SLOS", "Naive", "NaiveApprox", "CliffordClifford2017"); an unknown name logs a
+path ("SLOS", "SLAP", "Naive", "NaiveApprox", "CliffordClifford2017"); an unknown name logs a
 warning and falls back to SLOS, as in the reference.
 """
 import logging
@@ -10,12 +10,14 @@ from ._abstract_backends import ABackend, ASamplingBackend, AStrongSimulationBac
 from ._clifford2017 import Clifford2017Backend
 from ._naive import NaiveBackend
 from ._naive_approx import NaiveApproxBackend
+from ._slap import SLAPBackend
 from ._slos import SLOSBackend
 
 BACKEND_LIST = {
     "CliffordClifford2017": Clifford2017Backend,
     "Naive": NaiveBackend,
     "NaiveApprox": NaiveApproxBackend,
+    "SLAP": SLAPBackend,
     "SLOS": SLOSBackend,
 }
 
@@ -35,4 +37,4 @@ class BackendFactory:
 
 
 __all__ = ["ABackend", "ASamplingBackend", "AStrongSimulationBackend", "BACKEND_LIST", "BackendFactory",
-           "Clifford2017Backend", "NaiveApproxBackend", "NaiveBackend", "SLOSBackend"]
+           "Clifford2017Backend", "NaiveApproxBackend", "NaiveBackend", "SLAPBackend", "SLOSBackend"]

@@ -400,6 +400,10 @@ class FSMask:
         ``n`` photons)."""
         return self.match_array(arr, partial=True)
 
+    @property
+    def at_least_modes(self) -> list[int]:
+        return sorted(self._at_least)
+
     def device_spec(self):
         """(digits, at_least bits, n) for ``pcvl_slos_plan_create_masked``: digits is an
         int8 (masks x m) array with -1 where a mask accepts any count."""

@@ -11,7 +11,7 @@ from perceval_gb300.components import BS, catalog
 from perceval_gb300.utils.matrix import random_unitary
 
 pytestmark = pytest.mark.gpu
-STRONG = ["SLOS", "Naive"]
+STRONG = ["SLOS", "SLAP", "Naive"]
 
 
 def check_output_distribution(backend, input_state, expected):

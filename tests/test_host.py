@@ -147,10 +147,10 @@ def test_random_unitary_matches_reference_recipe():
 
 
 def test_factory_and_errors():
-    assert set(BackendFactory.list()) == {"SLOS", "Naive", "NaiveApprox", "CliffordClifford2017"}
+    assert set(BackendFactory.list()) == {"SLOS", "SLAP", "Naive", "NaiveApprox", "CliffordClifford2017"}
     assert BackendFactory.get_backend("nope").name == "SLOS"
     assert BackendFactory.get_backend().name == "SLOS"
-    for name in ("SLOS", "Naive", "NaiveApprox", "CliffordClifford2017"):
+    for name in ("SLOS", "SLAP", "Naive", "NaiveApprox", "CliffordClifford2017"):
         b = BackendFactory.get_backend(name)
         assert b.name == name
         # tests/backends/test_backends.py:106-113
