@@ -78,6 +78,19 @@ __device__ __forceinline__ cdd ld_cdd(const cdd* p) {
   const float4 v = __ldg(reinterpret_cast<const float4*>(p));
   return {{v.x, v.y}, {v.z, v.w}};
 }
+// double from a float by exponent re-bias on the integer pipe (GB300 issues FP64 at a
+// small fraction of its FP32 rate); zero, subnormals, infinities and NaN take the
+// conversion instruction
+__device__ __forceinline__ double f2d_int(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)f;
+  const uint64_t bits = ((uint64_t)(u & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
+                        ((uint64_t)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+// hi + lo as a double: two integer-pipe conversions and one FP64 add
+__device__ __forceinline__ double dd_to_double_fast(dd a) { return f2d_int(a.hi) + f2d_int(a.lo); }
 #endif
 PCVL_HD cdd cdd_zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
 PCVL_HD cdd cdd_one() { return {{1.f, 0.f}, {0.f, 0.f}}; }

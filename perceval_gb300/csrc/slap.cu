@@ -73,7 +73,8 @@ struct SlapArgs {
   const uint32_t* moff;
   const uint64_t* cn;                // cn[M * cs + x] = C(M + x - 1, x)
   int cs;
-  double inv_tfact;                  // 1 / prod t!
+  dd inv_t;                          // 1 / prod t! (probabilities) or 1 / sqrt(prod t!) (amplitudes)
+  const dd* invf;                    // invf[k] = 1 / k! or 1 / sqrt(k!), k = 0..n+1
   int mode;                          // 0: probabilities, 1: amplitudes
   double* out_p;
   double2* out_a;
@@ -104,101 +105,123 @@ __device__ __forceinline__ void slap_level(const SlapArgs& a, cdd* F, int k, int
 __device__ __forceinline__ void slap_leaves(const SlapArgs& a, const cdd* F, const int* elem, int lo, uint64_t pos,
                                             int lane) {
   const int n = a.n;
-  // prod s! of the prefix and the multiplicity of its last element
-  double pf = 1.0;
+  // 1 / (prod s! prod t!) (its square root for amplitudes) from float-float tables on the
+  // FP32 pipe: every run of equal prefix elements but the last contributes invf[length];
+  // the last run contributes invf[run] when x is past it and invf[run + 1] when x extends it
+  dd base = a.inv_t;
   int run = 0;
   for (int e = 0; e < n - 1; ++e) {
-    run = (e > 0 && elem[e] == elem[e - 1]) ? run + 1 : 1;
-    pf *= (double)run;
+    if (e > 0 && elem[e] == elem[e - 1]) {
+      ++run;
+    } else {
+      if (run > 0) base = dd_mul(base, a.invf[run]);
+      run = 1;
+    }
   }
+  const int xr = n > 1 ? elem[n - 2] : -1;
+  const dd f0 = run > 0 ? dd_mul(base, a.invf[run]) : base;
+  const dd f1 = dd_mul(base, a.invf[run + 1]);
   const uint32_t full = (1u << n) - 1u;
   for (int x = lo + lane; x < a.m; x += 32) {
     const cdd* ux = a.uc + (size_t)x * n;
     cacc acc = cacc_zero();
     for (int p = 0; p < n; ++p) cacc_fma(acc, F[full ^ (1u << p)], ux[p]);
     const cdd c = cacc_finish(acc);
-    const double sf = (n > 1 && x == elem[n - 2]) ? pf * (double)(run + 1) : pf;
+    const dd f = x == xr ? f1 : f0;
     const uint64_t o = pos + (uint64_t)(x - lo);
     if (a.mode == 0) {
       const dd c2 = dd_add(dd_mul(c.re, c.re), dd_mul(c.im, c.im));
-      a.out_p[o] = dd_to_double(c2) * (a.inv_tfact / sf);
+      a.out_p[o] = dd_to_double_fast(dd_mul(c2, f));
     } else {
-      const double s = sqrt(a.inv_tfact / sf);
-      a.out_a[o] = make_double2(dd_to_double(c.re) * s, dd_to_double(c.im) * s);
+      a.out_a[o] = make_double2(dd_to_double_fast(dd_mul(c.re, f)), dd_to_double_fast(dd_mul(c.im, f)));
     }
   }
 }
+
+// Sorted mode list el[0..k-1] of rank r among the k-element lists on modes lo..m-1.  The
+// lists with first element below i number Cn(m - lo, k) - Cn(m - i, k), so the first
+// element is the largest i with that count <= r (binary search), and so on.
+__device__ __forceinline__ void slap_unrank(const SlapArgs& a, uint64_t r, int k, int* el) {
+  int lo = 0;
+  for (int e = 0; e < k; ++e) {
+    const int kk = k - e;
+    const uint64_t tot = slap_cn(a, a.m - lo, kk);
+    int L = lo, R = a.m - 1;
+    while (L < R) {
+      const int mid = (L + R + 1) >> 1;
+      if (tot - slap_cn(a, a.m - mid, kk) <= r)
+        L = mid;
+      else
+        R = mid - 1;
+    }
+    r -= tot - slap_cn(a, a.m - L, kk);
+    el[e] = L;
+    lo = L;
+  }
+}
+
+constexpr int kSlapChunk = 16;  // consecutive units per grab: they share most of their prefix
 
 __global__ void __launch_bounds__(256) slap_walk(SlapArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int n = a.n, m = a.m, k0 = a.k0;
   cdd* F = reinterpret_cast<cdd*>(smem_raw) + ((size_t)w << n);
-  int elem[kSlapMaxN];
+  int elem[kSlapMaxN], pre[kSlapMaxN];
   while (true) {
-    unsigned long long u = 0;
-    if (lane == 0) u = atomicAdd(a.next, 1ull);
-    u = __shfl_sync(0xffffffffu, u, 0);
-    if (u >= a.units) break;
-    // prefix: the k0-photon state of rank u, as a sorted mode list
-    {
-      uint64_t r = u;
-      int rem = k0, e = 0;
-      for (int i = 0; i < m - 1 && rem > 0; ++i) {
-        int x = 0;
-        while (x < rem && r >= slap_cn(a, m - i, x)) ++x;
-        r -= slap_cn(a, m - i, x - 1);
-        for (int v = rem - x; v > 0; --v) elem[e++] = i;
-        rem = x;
-      }
-      for (; rem > 0; --rem) elem[e++] = m - 1;
-    }
-    // first output of the unit: the prefix followed by n - k0 copies of its last element;
-    // rank(s) = sum_{i <= m-2} Cn(m - i, R_{i+1} - 1), R_{i+1} = photons after mode i
-    uint64_t pos = 0;
-    {
-      const int last = k0 > 0 ? elem[k0 - 1] : 0;
-      int after = n, e = 0;
-      for (int i = 0; i < m - 1 && after > 0; ++i) {
-        int v = 0;
-        while (e < k0 && elem[e] == i) {
-          ++v;
-          ++e;
-        }
-        if (i == last) v += n - k0;
-        after -= v;
-        pos += slap_cn(a, m - i, after - 1);
-      }
-    }
-    // F for the prefix
-    if (lane == 0) F[0] = cdd_one();
-    __syncwarp();
-    for (int k = 0; k < k0; ++k) slap_level(a, F, k, elem[k], lane);
-    if (k0 == n - 1) {
-      const int lo = k0 > 0 ? elem[k0 - 1] : 0;
-      slap_leaves(a, F, elem, lo, pos, lane);
+    unsigned long long c = 0;
+    if (lane == 0) c = atomicAdd(a.next, 1ull);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    const uint64_t u0 = (uint64_t)c * kSlapChunk;
+    if (u0 >= a.units) break;
+    const uint64_t u1 = min(a.units, u0 + kSlapChunk);
+    for (uint64_t u = u0; u < u1; ++u) {
+      // the prefix (k0 elements); F levels 0..d stay valid when the first change is at d
+      slap_unrank(a, u, k0, pre);
+      int d = 0;
+      if (u != u0)
+        while (d < k0 && pre[d] == elem[d]) ++d;
+      else if (lane == 0)
+        F[0] = cdd_one();
+      for (int e = 0; e < k0; ++e) elem[e] = pre[e];
       __syncwarp();
-      continue;
-    }
-    int k = k0;
-    elem[k] = k > 0 ? elem[k - 1] : 0;
-    while (true) {
-      slap_level(a, F, k, elem[k], lane);
-      if (k + 1 == n - 1) {
-        slap_leaves(a, F, elem, elem[k], pos, lane);
-        pos += (uint64_t)(m - elem[k]);
-        while (true) {
-          if (++elem[k] < m) break;
-          if (--k < k0) break;
+      for (int k = d; k < k0; ++k) slap_level(a, F, k, elem[k], lane);
+      // first output: the prefix followed by n - k0 copies of its last element; in list
+      // order, rank = sum_j [Cn(m - a_{j-1}, n - j + 1) - Cn(m - a_j, n - j + 1)], a_0 = 0
+      uint64_t pos = 0;
+      {
+        int prev = 0;
+        for (int j = 0; j < n; ++j) {
+          const int aj = j < k0 ? elem[j] : (k0 > 0 ? elem[k0 - 1] : 0);
+          pos += slap_cn(a, m - prev, n - j) - slap_cn(a, m - aj, n - j);
+          prev = aj;
         }
-        if (k < k0) break;
-        __syncwarp();  // the leaves read level n - 1 before it is rewritten
-      } else {
-        ++k;
-        elem[k] = elem[k - 1];
       }
+      if (k0 == n - 1) {
+        slap_leaves(a, F, elem, k0 > 0 ? elem[k0 - 1] : 0, pos, lane);
+        __syncwarp();  // the next unit rewrites level n - 1
+        continue;
+      }
+      int k = k0;
+      elem[k] = k > 0 ? elem[k - 1] : 0;
+      while (true) {
+        slap_level(a, F, k, elem[k], lane);
+        if (k + 1 == n - 1) {
+          slap_leaves(a, F, elem, elem[k], pos, lane);
+          pos += (uint64_t)(m - elem[k]);
+          while (true) {
+            if (++elem[k] < m) break;
+            if (--k < k0) break;
+          }
+          if (k < k0) break;
+          __syncwarp();  // the leaves read level n - 1 before it is rewritten
+        } else {
+          ++k;
+          elem[k] = elem[k - 1];
+        }
+      }
+      __syncwarp();
     }
-    __syncwarp();
   }
 }
 
@@ -248,16 +271,26 @@ int slap_run(const double* u_d, int32_t m, const int32_t* input_state_h, int32_t
       if (__builtin_popcount(M) == k) masks.push_back((uint16_t)M);
   }
   moff[n + 1] = (uint32_t)masks.size();
-  // work units: the smallest prefix length giving every resident warp several units
+  // work units: the smallest prefix length giving every resident warp several chunks
   const int W = std::max(1, std::min(8, kSlapSmemBudget / (int)(sizeof(cdd) << n)));
-  const uint64_t want = (uint64_t)num_sms() * W * 8;
+  const uint64_t want = (uint64_t)num_sms() * W * 8 * kSlapChunk;
   int k0 = 0;
   while (k0 < n - 1 && cn[(size_t)m * cs + k0] < want) ++k0;
-  // one staged upload: cols | cn | moff | masks | counter
+  // 1 / k! (probabilities) or 1 / sqrt(k!) (amplitudes), k = 0..n+1, as float-float
+  std::vector<dd> invf(n + 2);
+  {
+    double f = 1.0;
+    for (int k = 0; k <= n + 1; ++k) {
+      if (k > 1) f *= k;
+      invf[k] = dd_from_double(mode == 0 ? 1.0 / f : 1.0 / std::sqrt(f));
+    }
+  }
+  // one staged upload: cols | cn | moff | masks | invf | counter
   const size_t o_cols = 0, o_cn = align_up(cols.size() * 4, 16);
   const size_t o_moff = o_cn + align_up(cn.size() * 8, 16);
   const size_t o_masks = o_moff + align_up(moff.size() * 4, 16);
-  const size_t o_next = o_masks + align_up(masks.size() * 2, 16);
+  const size_t o_invf = o_masks + align_up(masks.size() * 2, 16);
+  const size_t o_next = o_invf + align_up(invf.size() * sizeof(dd), 16);
   const size_t o_uc = o_next + 16;
   const size_t total = o_uc + (size_t)m * n * sizeof(cdd);
   std::vector<unsigned char> host(o_uc, 0);
@@ -265,6 +298,7 @@ int slap_run(const double* u_d, int32_t m, const int32_t* input_state_h, int32_t
   std::memcpy(host.data() + o_cn, cn.data(), cn.size() * 8);
   std::memcpy(host.data() + o_moff, moff.data(), moff.size() * 4);
   std::memcpy(host.data() + o_masks, masks.data(), masks.size() * 2);
+  std::memcpy(host.data() + o_invf, invf.data(), invf.size() * sizeof(dd));
   void* ws = nullptr;
   PCVL_TRY(workspace(WS_SLAP, total, &ws));
   unsigned char* base = static_cast<unsigned char*>(ws);
@@ -282,7 +316,8 @@ int slap_run(const double* u_d, int32_t m, const int32_t* input_state_h, int32_t
   a.moff = (const uint32_t*)(base + o_moff);
   a.cn = (const uint64_t*)(base + o_cn);
   a.cs = cs;
-  a.inv_tfact = 1.0 / tfact;
+  a.inv_t = dd_from_double(mode == 0 ? 1.0 / tfact : 1.0 / std::sqrt(tfact));
+  a.invf = (const dd*)(base + o_invf);
   a.mode = mode;
   a.out_p = out_d;
   a.out_a = (double2*)out_d;
@@ -291,7 +326,7 @@ int slap_run(const double* u_d, int32_t m, const int32_t* input_state_h, int32_t
   PCVL_CUDA(cudaFuncSetAttribute(slap_walk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   PCVL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, slap_walk, W * 32, smem));
-  const uint64_t blocks_needed = (a.units + W - 1) / W;
+  const uint64_t blocks_needed = ((a.units + kSlapChunk - 1) / kSlapChunk + W - 1) / W;
   const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)num_sms() * std::max(per_sm, 1)));
   slap_walk<<<grid, W * 32, smem, s>>>(a);
   PCVL_CUDA(cudaGetLastError());

@@ -487,17 +487,6 @@ __global__ void __launch_bounds__(256) slos_bwd(SlosArgs a) {
   }
 }
 
-// double from a float by exponent re-bias (integer pipe); zero and subnormals take the
-// conversion instruction
-__device__ __forceinline__ double f2d_int(float f) {
-  const uint32_t u = __float_as_uint(f);
-  const uint32_t e = (u >> 23) & 0xffu;
-  if (e == 0u || e == 0xffu) return (double)f;
-  const uint64_t bits = ((uint64_t)(u & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
-                        ((uint64_t)(u & 0x7fffffu) << 29);
-  return __longlong_as_double((long long)bits);
-}
-__device__ __forceinline__ double dd_to_double_fast(dd a) { return f2d_int(a.hi) + f2d_int(a.lo); }
 
 // Last layer -> probabilities (mode 0), amplitudes (mode 1) or the adjoint seed
 // a_n = 2 w F c_n (mode 2), with F = prod(out!) / prod(in!) = f(tile) x ftail[tau].

@@ -306,10 +306,10 @@ __global__ void __launch_bounds__(256) slos_mfin(const cdd* __restrict__ c, cons
     const cdd v = ld_cdd(&c[idx]);
     if (mode == 0) {
       const dd c2 = dd_add(dd_mul(v.re, v.re), dd_mul(v.im, v.im));
-      out_real[idx] = dd_to_double(dd_mul(c2, F));
+      out_real[idx] = dd_to_double_fast(dd_mul(c2, F));
     } else if (mode == 1) {
-      const double sF = sqrt(dd_to_double(F));
-      out_c[idx] = make_double2(dd_to_double(v.re) * sF, dd_to_double(v.im) * sF);
+      const double sF = sqrt(dd_to_double_fast(F));
+      out_c[idx] = make_double2(dd_to_double_fast(v.re) * sF, dd_to_double_fast(v.im) * sF);
     } else {
       const dd f2 = dd_mul(dd_from_double(2.0 * w[idx]), F);
       seed[idx] = {dd_mul(v.re, f2), dd_mul(v.im, f2)};
