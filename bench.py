@@ -202,6 +202,8 @@ def cpu_context() -> dict:
     out["slos_m16_n8_one_circuit_ms"] = 1e3 * t(lambda: oracle.slos(U16, inp16))
     w = np.random.default_rng(1).normal(size=math.comb(23, 8))
     out["slos_grad_m16_n8_one_circuit_ms"] = 1e3 * t(lambda: oracle.slos_grad(U16, inp16, w))
+    U64 = random_unitary(64, seed=0)
+    out["all_outputs_m64_n4_ms"] = 1e3 * t(lambda: oracle.slos(U64, [1] * 4 + [0] * 60))
     U400 = random_unitary(400, seed=0)
     ns = 4
     out["cc2017_n20_m400_samples_per_s_1thread"] = ns / t(lambda: oracle.cc2017(U400, [1] * 20 + [0] * 380, ns, seed=1))
@@ -445,6 +447,32 @@ def secondary(torch, _native, random_unitary, dev, flush):
     t_p20 = timed(lambda: plan.probabilities(p20), reps=3)
     res["slos_m20_n10"] = {"forward_ms": t_f20, "probabilities_ms": t_p20, "outputs": plan.count}
     del plan, p20
+    # SLAP: every output of one input without intermediate layers, many modes and few photons
+    # (SLOS plans stop at 32 modes); one line where both run
+    for (ms, ns) in [(1024, 3), (256, 4), (64, 6), (64, 4)]:
+        inp = [1] * ns + [0] * (ms - ns)
+        Us = torch.from_numpy(random_unitary(ms, seed=0)).to(dev)
+        cnt = _native.slap_output_count(ms, inp)
+        ps = torch.empty(cnt, dtype=torch.float64, device=dev)
+        t_s = timed(lambda: _native.slap_all(Us, inp, out=ps), reps=3)
+        res[f"slap_m{ms}_n{ns}"] = {"outputs": cnt, "ms": t_s, "outputs_per_s": cnt / (t_s * 1e-3),
+                                    "written_gbs": 8 * cnt / (t_s * 1e-3) / 1e9, "sum_p": float(ps.sum())}
+        del ps
+    torch.cuda.empty_cache()
+    inp = [1] * 6 + [0] * 26
+    U32 = torch.from_numpy(random_unitary(32, seed=0)).to(dev)
+    plan = _native.SlosPlan(32, inp)
+    p32 = torch.empty(plan.count, dtype=torch.float64, device=dev)
+
+    def slos32():
+        plan.forward(U32)
+        plan.probabilities(p32)
+    t_slos32 = timed(slos32, reps=3)
+    ps = torch.empty_like(p32)
+    t_slap32 = timed(lambda: _native.slap_all(U32, inp, out=ps), reps=3)
+    res["slap_vs_slos_m32_n6"] = {"outputs": plan.count, "slos_ms": t_slos32, "slap_ms": t_slap32,
+                                  "max_abs_diff": float((ps - p32).abs().max())}
+    del plan, p32, ps
     # batched forward + adjoint, 256 Clements meshes m=16, n=8
     from perceval_gb300.components.mesh import clements_mesh_unitary
     ph = torch.from_numpy(np.random.default_rng(0).uniform(0, 2 * math.pi, (256, 240)))
@@ -713,6 +741,10 @@ def profile_case(name: str):
         plan = _native.SlosPlan(22, [1] * 11 + [0] * 11, mask=FSMask(22, 11, ["*" * 18 + "1100"]))
         plan.forward(torch.from_numpy(random_unitary(22, seed=0)).to(dev))
         plan.probabilities()
+    elif name == "slap1024":
+        # SLAP m = 1024, n = 3: 179,481,600 outputs (1.4 GB of probabilities), one slap_walk launch
+        inp = [1] * 3 + [0] * 1021
+        _native.slap_all(torch.from_numpy(random_unitary(1024, seed=0)).to(dev), inp)
     elif name == "slos16b256":
         from perceval_gb300.components.mesh import clements_mesh_unitary
         ph = torch.from_numpy(np.random.default_rng(0).uniform(0, 2 * math.pi, (256, 240)))
@@ -753,8 +785,8 @@ def main():
                     help="run the learned-proposal sampler workload (n=30, m=900 and n=8, m=64) and exit")
     ap.add_argument("--learned-train", type=int, default=2048, help="exact training samples at n=30")
     ap.add_argument("--large-perm", action="store_true", help="one n = 40 permanent (about a minute)")
-    ap.add_argument("--profile-case", choices=["perm24", "slos20", "slosmask22", "slos16b256", "cc2017", "gurvits20",
-                                               "gemm"],
+    ap.add_argument("--profile-case", choices=["perm24", "slos20", "slosmask22", "slap1024", "slos16b256", "cc2017",
+                                               "gurvits20", "gemm"],
                     help="run one small untimed case of a single kernel (for ncu) and exit")
     args = ap.parse_args()
     if args.profile_case:
