@@ -285,13 +285,14 @@ __host__ __device__ constexpr int fwd1_slot() {
 //    over the set bits of its state's occupation (prefix bits from its tile's slot, tail
 //    bits from the table), so a warp runs as many multiply-adds as its busiest lane.
 template <int MMAX>
-__global__ void __launch_bounds__(256) slos_fwd1(SlosArgs a) {
+__global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int SL = fwd1_slot<MMAX>();
   uint32_t* cn;
   const cdd* u = load_shared<MMAX, false, false>(a, smem_raw, cn);
+  // one circuit: u holds MMAX entries; the slots follow
   uint32_t* slots = reinterpret_cast<uint32_t*>(smem_raw + smem_cn_bytes(a.m, a.cn_stride) +
-                                                (size_t)MMAX * 32 * sizeof(cdd));
+                                                (size_t)MMAX * sizeof(cdd));
   const int lane = threadIdx.x & 31, p = a.p;
   uint32_t* myslot = slots + (size_t)threadIdx.x * SL;
   const uint32_t* wslots = slots + (size_t)(threadIdx.x - lane) * SL;  // the warp's 32 slots
@@ -676,7 +677,8 @@ static int launch_kernel(Kern kind, const SlosArgs& a, int grid, dd inv_in, int 
       if (batched) {
         slos_fwdb<MMAX><<<g, 256, smem, s>>>(a);
       } else {
-        const size_t smem1 = smem + (size_t)256 * fwd1_slot<MMAX>() * sizeof(uint32_t);
+        const size_t smem1 = smem_cn_bytes(a.m, a.cn_stride) + (size_t)MMAX * sizeof(cdd) +
+                             (size_t)256 * fwd1_slot<MMAX>() * sizeof(uint32_t);
         cudaFuncSetAttribute(slos_fwd1<MMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
         slos_fwd1<MMAX><<<g, 256, smem1, s>>>(a);
       }
