@@ -235,7 +235,7 @@ __device__ __forceinline__ cdd fwd_value(const SlosArgs& a, const Desc<MMAX>& d,
 // Batched forward layer: a warp takes a unit (one tile, up to kChunkB states) and its
 // lanes 32 circuits; the parent offsets are warp-uniform, the loads coalesced.
 template <int MMAX>
-__global__ void __launch_bounds__(256) slos_fwdb(SlosArgs a) {
+__global__ void __launch_bounds__(256, 4) slos_fwdb(SlosArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t* cn;
   const cdd* us_base = load_shared<MMAX, true, false>(a, smem_raw, cn);
