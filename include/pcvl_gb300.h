@@ -164,6 +164,13 @@ int pcvl_slos_plan_bytes(const pcvl_slos_plan* plan, int64_t* bytes);
 int pcvl_slos_forward(pcvl_slos_plan* plan, const double* u_d, void* stream);
 /* Same, with one m x m unitary u_d shared by every entry of the plan. */
 int pcvl_slos_forward_shared(pcvl_slos_plan* plan, const double* u_d, void* stream);
+/* pcvl_slos_forward + pcvl_slos_probabilities in one call, for callers that want only the
+ * probabilities (SLOSBackend.all_prob / prob_distribution, perceval/backends/_slos.py:195-214).
+ * For one circuit the last layer writes each probability directly and its coefficients are
+ * not stored (no write and read-back of the largest layer); pcvl_slos_amplitudes /
+ * pcvl_slos_probabilities / pcvl_slos_backward then need a pcvl_slos_forward first.
+ * Results are identical to the two calls. */
+int pcvl_slos_forward_probabilities(pcvl_slos_plan* plan, const double* u_d, double* probs_d, void* stream);
 /* probs_d[r * batch + b] = |c|^2 * prod(out!) / prod(in!)   (float64; state-major,
  * circuit innermost) */
 int pcvl_slos_probabilities(pcvl_slos_plan* plan, double* probs_d, void* stream);

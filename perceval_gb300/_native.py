@@ -60,6 +60,8 @@ SYMBOLS = {
     "pcvl_slos_plan_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     "pcvl_slos_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "pcvl_slos_probabilities": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "pcvl_slos_forward_probabilities": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                        ctypes.c_void_p]),
     "pcvl_slos_amplitudes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "pcvl_slos_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "pcvl_cc2017_sample": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64,
@@ -346,6 +348,22 @@ class SlosPlan:
                   "pcvl_slos_forward_shared")
         else:
             raise ValueError("u must hold batch x m x m or m x m elements")
+
+    def forward_probabilities(self, u: torch.Tensor, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        """``forward`` then ``probabilities`` in one call; with one circuit the last layer
+        writes the probabilities directly (its coefficients are not kept: ``amplitudes``
+        and ``backward`` need a ``forward`` first).  ``u``: batch x m x m unitaries."""
+        _dev_tensor(u, torch.complex128, "u")
+        if u.numel() != self.batch * self.m * self.m:
+            raise ValueError("u must hold batch x m x m elements")
+        if out is None:
+            out = torch.empty(self.count * self.batch, dtype=torch.float64, device="cuda")
+        if self.count == 0:
+            return out
+        _dev_tensor(out, torch.float64, "out")
+        check(self._lib.pcvl_slos_forward_probabilities(self._h, u.data_ptr(), out.data_ptr(), _stream_ptr(stream)),
+              "pcvl_slos_forward_probabilities")
+        return out
 
     def probabilities(self, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
         if out is None:

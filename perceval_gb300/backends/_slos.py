@@ -37,7 +37,8 @@ class _Entry:
 
     def __init__(self, plan: _native.SlosPlan):
         self.plan = plan
-        self.fresh = False           # coefficients match the current unitary
+        self.fresh = False           # cached results belong to the current unitary
+        self.layer_ok = False        # the plan's last layer holds this unitary's coefficients
         self.probs = None            # device tensor
         self.amps = None             # device tensor
         self.amps_host = None        # numpy copy (small spaces)
@@ -98,8 +99,8 @@ class SLOSBackend(AStrongSimulationBackend):
                 e.ranks = e.plan.output_ranks()
             self._entries[st] = e
         if not e.fresh:
-            e.plan.forward(self._unitary_device())
             e.probs = e.amps = e.amps_host = None
+            e.layer_ok = False
             e.fresh = True
         return e
 
@@ -111,7 +112,8 @@ class SLOSBackend(AStrongSimulationBackend):
             self.set_input_state(input_state)
         e = self._entry()
         if e.probs is None:
-            e.probs = e.plan.probabilities()
+            # probabilities alone: the last layer writes them directly (not stored)
+            e.probs = e.plan.probabilities() if e.layer_ok else e.plan.forward_probabilities(self._unitary_device())
         return e.probs
 
     def amplitudes_tensor(self) -> torch.Tensor:
@@ -119,6 +121,9 @@ class SLOSBackend(AStrongSimulationBackend):
         CUDA tensor, in descending-lexicographic order."""
         e = self._entry()
         if e.amps is None:
+            if not e.layer_ok:
+                e.plan.forward(self._unitary_device())
+                e.layer_ok = True
             e.amps = e.plan.amplitudes()
         return e.amps
 

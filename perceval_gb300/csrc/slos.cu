@@ -265,10 +265,18 @@ __device__ __forceinline__ int unit_class1(const SlosArgs& a, uint32_t u) {
 }
 
 // Words per thread of the single-circuit forward kernel's shared slots: the parent
-// offsets of one tile (MMAX) and its A, tb and prefix mask.
-template <int MMAX>
+// offsets of one tile (MMAX), its A, tb and prefix mask, and (probability output) its
+// normalisation prod pi! / prod in! as two floats.
+template <int MMAX, bool PROB>
 __host__ __device__ constexpr int fwd1_slot() {
-  return MMAX + 4;
+  return PROB ? MMAX + 5 : MMAX + 4;
+}
+
+// Probability of a last-layer state from its coefficient and F = prod(out!) / prod(in!)
+// (the arithmetic of fin_state, so the fused and the two-pass results are identical).
+__device__ __forceinline__ double fwd_prob(const cdd& c, const dd& F) {
+  const dd c2 = dd_add(dd_mul(c.re, c.re), dd_mul(c.im, c.im));
+  return dd_to_double_fast(dd_mul(c2, F));
 }
 
 // Single-circuit forward layer.
@@ -284,10 +292,13 @@ __host__ __device__ constexpr int fwd1_slot() {
 //    warp sweeps the group's states in rank order, one state per lane; each lane loops
 //    over the set bits of its state's occupation (prefix bits from its tile's slot, tail
 //    bits from the table), so a warp runs as many multiply-adds as its busiest lane.
-template <int MMAX>
-__global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a) {
+//  * PROB (the last layer, when only probabilities are wanted): each state's probability
+//    |c|^2 prod(out!) / prod(in!) goes to probs instead of its coefficient to a.out, so the
+//    last layer is never stored nor read back.
+template <int MMAX, bool PROB>
+__global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a, double* __restrict__ probs) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int SL = fwd1_slot<MMAX>();
+  constexpr int SL = fwd1_slot<MMAX, PROB>();
   uint32_t* cn;
   const cdd* u = load_shared<MMAX, false, false>(a, smem_raw, cn);
   // one circuit: u holds MMAX entries; the slots follow
@@ -309,17 +320,28 @@ __global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a) {
       const uint32_t c0 = (lu - pi * cpt) * a.chunk1;
       const uint32_t c1 = min(S, c0 + a.chunk1);
       uint32_t A = 0, tb = 0, mask = 0;
+      float fh = 0.f, fl = 0.f;
       if (lane == 0) {
         Desc<MMAX> d;
-        describe<MMAX, false, false>(pi, q, r, a, cn, d, dd{0.f, 0.f}, myslot);
+        describe<MMAX, false, PROB>(pi, q, r, a, cn, d, PROB ? a.inv_in[0] : dd{0.f, 0.f}, myslot);
         A = d.A;
         tb = d.tb;
         mask = d.mask;
+        if (PROB) {
+          fh = d.f.hi;
+          fl = d.f.lo;
+        }
       }
       __syncwarp();
       A = __shfl_sync(0xffffffffu, A, 0);
       tb = __shfl_sync(0xffffffffu, tb, 0);
       mask = __shfl_sync(0xffffffffu, mask, 0);
+      if (PROB) {
+        fh = __shfl_sync(0xffffffffu, fh, 0);
+        fl = __shfl_sync(0xffffffffu, fl, 0);
+      }
+      const dd ft = {fh, fl};
+      const dd* ftail = a.ftail + a.tstate_off[r];
       for (uint32_t t0 = c0 + lane; t0 < c1; t0 += 64) {
         const uint32_t t1 = t0 + 32;
         const bool two = t1 < c1;
@@ -337,7 +359,10 @@ __global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a) {
             const int jl = __ffs(o) - 1;
             cacc_fma(acc0, ld_cdd(&a.in[tb + __ldg(&row[jl])]), u[p + jl]);
           }
-          a.out[A + t0] = cacc_finish(acc0);
+          if (PROB)
+            probs[A + t0] = fwd_prob(cacc_finish(acc0), dd_mul(ft, ftail[t0]));
+          else
+            a.out[A + t0] = cacc_finish(acc0);
         }
         if (two) {
           const uint32_t* row = rows + (size_t)t1 * a.t;
@@ -345,7 +370,10 @@ __global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a) {
             const int jl = __ffs(o) - 1;
             cacc_fma(acc1, ld_cdd(&a.in[tb + __ldg(&row[jl])]), u[p + jl]);
           }
-          a.out[A + t1] = cacc_finish(acc1);
+          if (PROB)
+            probs[A + t1] = fwd_prob(cacc_finish(acc1), dd_mul(ft, ftail[t1]));
+          else
+            a.out[A + t1] = cacc_finish(acc1);
         }
       }
       __syncwarp();  // lane 0's slot is rewritten by the next unit
@@ -357,10 +385,14 @@ __global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a) {
     const uint32_t ng = min(G, a.npf[r] - g0);
     if ((uint32_t)lane < ng) {
       Desc<MMAX> d;
-      describe<MMAX, false, false>(g0 + lane, q, r, a, cn, d, dd{0.f, 0.f}, myslot);
+      describe<MMAX, false, PROB>(g0 + lane, q, r, a, cn, d, PROB ? a.inv_in[0] : dd{0.f, 0.f}, myslot);
       myslot[MMAX] = d.A;
       myslot[MMAX + 1] = d.tb;
       myslot[MMAX + 2] = d.mask;
+      if (PROB) {
+        myslot[MMAX + 3] = __float_as_uint(d.f.hi);
+        myslot[MMAX + 4] = __float_as_uint(d.f.lo);
+      }
     }
     __syncwarp();
     // state f = g * S + tau of the group, f = lane, lane + 32, ...
@@ -378,7 +410,12 @@ __global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a) {
         const uint32_t ad = j < p ? ws[j] + tau : tb + __ldg(&row[j]);
         cacc_fma(acc, ld_cdd(&a.in[ad]), u[j]);
       }
-      a.out[ws[MMAX] + tau] = cacc_finish(acc);
+      if (PROB) {
+        const dd fg = {__uint_as_float(ws[MMAX + 3]), __uint_as_float(ws[MMAX + 4])};
+        probs[ws[MMAX] + tau] = fwd_prob(cacc_finish(acc), dd_mul(fg, a.ftail[a.tstate_off[r] + tau]));
+      } else {
+        a.out[ws[MMAX] + tau] = cacc_finish(acc);
+      }
       g += q32;
       tau += r32;
       if (tau >= S) {
@@ -659,7 +696,7 @@ __global__ void slos_fill_vacuum(cdd* layer0, int B) {
   if (b < B) layer0[b] = cdd_one();
 }
 
-enum class Kern { Fwd, Bwd, Fin };
+enum class Kern { Fwd, FwdProb, Bwd, Fin };
 
 template <int MMAX>
 static int launch_kernel(Kern kind, const SlosArgs& a, int grid, dd inv_in, int mode, const double* w,
@@ -678,11 +715,18 @@ static int launch_kernel(Kern kind, const SlosArgs& a, int grid, dd inv_in, int 
         slos_fwdb<MMAX><<<g, 256, smem, s>>>(a);
       } else {
         const size_t smem1 = smem_cn_bytes(a.m, a.cn_stride) + (size_t)MMAX * sizeof(cdd) +
-                             (size_t)256 * fwd1_slot<MMAX>() * sizeof(uint32_t);
-        cudaFuncSetAttribute(slos_fwd1<MMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
-        slos_fwd1<MMAX><<<g, 256, smem1, s>>>(a);
+                             (size_t)256 * fwd1_slot<MMAX, false>() * sizeof(uint32_t);
+        cudaFuncSetAttribute(slos_fwd1<MMAX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+        slos_fwd1<MMAX, false><<<g, 256, smem1, s>>>(a, nullptr);
       }
       break;
+    case Kern::FwdProb: {  // single circuit only
+      const size_t smem1 = smem_cn_bytes(a.m, a.cn_stride) + (size_t)MMAX * sizeof(cdd) +
+                           (size_t)256 * fwd1_slot<MMAX, true>() * sizeof(uint32_t);
+      cudaFuncSetAttribute(slos_fwd1<MMAX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+      slos_fwd1<MMAX, true><<<g, 256, smem1, s>>>(a, out_real);
+      break;
+    }
     case Kern::Bwd:
       if (batched)
         slos_bwd<MMAX, true><<<g, 256, smem, s>>>(a);
@@ -1070,7 +1114,9 @@ extern "C" int pcvl_slos_plan_bytes(const pcvl_slos_plan* plan, int64_t* bytes) 
   return PCVL_OK;
 }
 
-static int forward(pcvl_slos_plan* p, const double* u_d, size_t ustride, cudaStream_t s) {
+// probs != nullptr (one circuit, full space, n >= 1): the last layer writes probabilities
+// instead of coefficients and the plan's last layer is left unwritten.
+static int forward(pcvl_slos_plan* p, const double* u_d, size_t ustride, cudaStream_t s, double* probs = nullptr) {
   const int m = p->m, B = p->B;
   if (p->n > 0) {
     const uint64_t tot = (uint64_t)p->n * m * B;
@@ -1091,13 +1137,15 @@ static int forward(pcvl_slos_plan* p, const double* u_d, size_t ustride, cudaStr
     a.out = p->keep ? p->layers[k] : p->layers[k % 2];
     a.ucol = p->ucols_d + (size_t)(k - 1) * m * B;
     a.tail = p->tp_d;
-    const int rc = dispatch(Kern::Fwd, a, grid_for_units(a, B == 1), s);
+    const bool fuse = probs && k == p->n;
+    const int rc = fuse ? dispatch(Kern::FwdProb, a, grid_for_units(a, true), s, dd{0.f, 0.f}, 0, nullptr, probs)
+                        : dispatch(Kern::Fwd, a, grid_for_units(a, B == 1), s);
     if (rc != 0) {
       set_error("SLOS layer %d launch failed: %s", k, cudaGetErrorString((cudaError_t)rc));
       return PCVL_ERR_CUDA;
     }
   }
-  p->forwarded = true;
+  p->forwarded = probs == nullptr;
   return PCVL_OK;
 }
 
@@ -1109,6 +1157,20 @@ extern "C" int pcvl_slos_forward(pcvl_slos_plan* p, const double* u_d, void* str
 extern "C" int pcvl_slos_forward_shared(pcvl_slos_plan* p, const double* u_d, void* stream) {
   PCVL_CHECK(p && u_d, "null pointer argument");
   return forward(p, u_d, 0, (cudaStream_t)stream);
+}
+
+static int finalize(pcvl_slos_plan* p, int mode, const double* w, double* out_real, double2* out_c, cdd* seed,
+                    cudaStream_t s);
+
+extern "C" int pcvl_slos_forward_probabilities(pcvl_slos_plan* p, const double* u_d, double* probs_d, void* stream) {
+  PCVL_CHECK(p && u_d && probs_d, "null pointer argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t ustride = (size_t)p->m * p->m;
+  if (p->masked || p->B > 1 || p->n == 0) {  // forward, then the probabilities of the stored last layer
+    PCVL_TRY(forward(p, u_d, ustride, s));
+    return finalize(p, 0, nullptr, probs_d, nullptr, nullptr, s);
+  }
+  return forward(p, u_d, ustride, s, probs_d);
 }
 
 static int finalize(pcvl_slos_plan* p, int mode, const double* w, double* out_real, double2* out_c, cdd* seed,

@@ -127,3 +127,36 @@ def test_plan_errors(native):
     with pytest.raises(RuntimeError, match="keep_layers"):
         plan.forward(torch.from_numpy(random_unitary(3, seed=1)).cuda())
         plan.backward(torch.zeros(plan.count, dtype=torch.float64, device="cuda"))
+
+
+@pytest.mark.parametrize("m,n", [(6, 3), (12, 6), (16, 8), (20, 10), (24, 8), (9, 0)])
+def test_fused_probabilities_equal_two_pass(native, m, n):
+    """forward_probabilities (the last layer writes probabilities, one circuit) gives
+    exactly the forward + probabilities results, over the large-tile and the grouped
+    small-tile paths; afterwards the plan refuses amplitudes until a plain forward."""
+    inp = [1] * n + [0] * (m - n)
+    U = torch.from_numpy(random_unitary(m, seed=m + n)).cuda()
+    plan = native.SlosPlan(m, inp)
+    plan.forward(U)
+    ref = plan.probabilities().clone()
+    got = plan.forward_probabilities(U)
+    assert torch.equal(got, ref)
+    if n > 0:
+        with pytest.raises(RuntimeError):
+            plan.amplitudes()
+    plan.forward(U)
+    assert torch.equal(plan.probabilities(), ref)
+
+
+def test_fused_probabilities_batched_and_masked(native):
+    from perceval_gb300.utils import FSMask
+    m, inp = 8, [1, 1, 0, 1, 0, 0, 1, 0]
+    Us = torch.from_numpy(np.stack([random_unitary(m, seed=40 + b) for b in range(5)])).cuda()
+    plan = native.SlosPlan(m, inp, batch=5)
+    plan.forward(Us)
+    ref = plan.probabilities().clone()
+    assert torch.equal(plan.forward_probabilities(Us), ref)
+    mplan = native.SlosPlan(m, inp, mask=FSMask(m, 4, ["******00"]))
+    mplan.forward(Us[0])
+    mref = mplan.probabilities().clone()
+    assert torch.equal(mplan.forward_probabilities(Us[0].contiguous()), mref)
