@@ -57,6 +57,7 @@ constexpr int kSlosMaxM = 32;
 constexpr int kSlosMaxN = 32;
 constexpr uint32_t kNone = 0xffffffffu;
 constexpr int kWarps = 8;  // warps per CTA (256 threads)
+constexpr int kBwdGroups = 2;  // mode groups per warp of the batched adjoint (measured: 2 beats 1 and 4)
 
 struct SlosArgs {
   int m, k, p, t, B;      // k: photons of the layer whose states are the tiles
@@ -427,13 +428,13 @@ __global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a, double* __restri
   }
 }
 
-// Adjoint value of parent state (d, tau): a_{k-1} = sum_j conj(u_j) a_k[child_j], and
-// g_j += conj(c_{k-1}) a_k[child_j] (every child exists).
-template <int MMAX, bool BATCHED>
+// Adjoint value of parent state (d, tau) of one circuit: a_{k-1} = sum_j conj(u_j)
+// a_k[child_j], and g_j += conj(c_{k-1}) a_k[child_j] (every child exists).
+template <int MMAX>
 __device__ __forceinline__ void bwd_state(const SlosArgs& a, const Desc<MMAX>& d, int r, uint32_t tau,
-                                          const cdd* uc, int us, int b, cacc (&g)[MMAX]) {
+                                          const cdd* uc, cacc (&g)[MMAX]) {
   const int p = a.p, m = a.m;
-  const size_t pidx = BATCHED ? (size_t)(d.A + tau) * a.B + b : (size_t)(d.A + tau);
+  const size_t pidx = (size_t)(d.A + tau);
   const cdd cp = cdd_conj(ld_cdd(&a.cpar[pidx]));
   const uint32_t* row = a.tail + a.tail_off[r] + (size_t)tau * a.t;
   cacc acc = cacc_zero();
@@ -441,27 +442,24 @@ __device__ __forceinline__ void bwd_state(const SlosArgs& a, const Desc<MMAX>& d
   for (int j = 0; j < MMAX; ++j) {
     if (j < m) {
       const uint32_t ad = j < p ? d.base[j] + tau : d.tb + __ldg(&row[j - p]);
-      const cdd v = ld_cdd(&a.in[BATCHED ? (size_t)ad * a.B + b : (size_t)ad]);
-      cacc_fma(acc, v, uc[j * us]);
+      const cdd v = ld_cdd(&a.in[ad]);
+      cacc_fma(acc, v, uc[j]);
       cacc_fma(g[j], v, cp);
     }
   }
   a.out[pidx] = cacc_finish(acc);
 }
 
-// Adjoint step over the parent layer (its states are the units' states); per-CTA
-// partials of dL/du_j go to gpart.
-template <int MMAX, bool BATCHED>
+// Single-circuit adjoint step over the parent layer (its states are the units' states);
+// per-CTA partials of dL/du_j go to gpart.  Batches use slos_bwd_g.
+template <int MMAX>
 __global__ void __launch_bounds__(256) slos_bwd(SlosArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ cdd red[kWarps][32];
   uint32_t* cn;
-  const cdd* us_base = load_shared<MMAX, BATCHED, true>(a, smem_raw, cn);
+  const cdd* uc = load_shared<MMAX, false, true>(a, smem_raw, cn);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int b = BATCHED ? blockIdx.y * 32 + lane : 0;
   const int m = a.m;
-  const cdd* uc = BATCHED ? us_base + lane : us_base;
-  const int us = BATCHED ? 32 : 1;
   cacc g[MMAX];
 #pragma unroll
   for (int j = 0; j < MMAX; ++j) g[j] = cacc_zero();
@@ -475,56 +473,123 @@ __global__ void __launch_bounds__(256) slos_bwd(SlosArgs a) {
     if (cpt > 0) {
       const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
       describe<MMAX, true, false>(pi, q, r, a, cn, d, dd{0.f, 0.f}, d.base);
-      const uint32_t chunk = BATCHED ? a.chunkB : kChunk;
-      const uint32_t t0 = ch * chunk, t1 = min(S, t0 + chunk);
-      if (BATCHED) {
-        if (b < a.B)
-          for (uint32_t tau = t0; tau < t1; ++tau) bwd_state<MMAX, true>(a, d, r, tau, uc, us, b, g);
-      } else {
-        for (uint32_t tau = t0 + lane; tau < t1; tau += 32) bwd_state<MMAX, false>(a, d, r, tau, uc, us, 0, g);
-      }
+      const uint32_t t0 = ch * kChunk, t1 = min(S, t0 + kChunk);
+      for (uint32_t tau = t0 + lane; tau < t1; tau += 32) bwd_state<MMAX>(a, d, r, tau, uc, g);
     } else {
       // small tiles: one tile per lane
       const uint32_t pi = lu * 32 + lane;
       if (pi < a.npf[r]) {
         describe<MMAX, true, false>(pi, q, r, a, cn, d, dd{0.f, 0.f}, d.base);
-        for (uint32_t tau = 0; tau < S; ++tau) bwd_state<MMAX, false>(a, d, r, tau, uc, us, 0, g);
+        for (uint32_t tau = 0; tau < S; ++tau) bwd_state<MMAX>(a, d, r, tau, uc, g);
       }
     }
   }
-  // reduce g over the CTA: over all threads (one circuit) or over warps per lane
+  // reduce g over the CTA's threads
 #pragma unroll
   for (int j = 0; j < MMAX; ++j) {
     if (j >= m) break;
     cdd v = cacc_finish(g[j]);
-    if (!BATCHED) {
 #pragma unroll
-      for (int dlt = 16; dlt > 0; dlt >>= 1) {
-        cdd o;
-        o.re.hi = __shfl_down_sync(0xffffffffu, v.re.hi, dlt);
-        o.re.lo = __shfl_down_sync(0xffffffffu, v.re.lo, dlt);
-        o.im.hi = __shfl_down_sync(0xffffffffu, v.im.hi, dlt);
-        o.im.lo = __shfl_down_sync(0xffffffffu, v.im.lo, dlt);
-        v = cdd_add(v, o);
-      }
+    for (int dlt = 16; dlt > 0; dlt >>= 1) {
+      cdd o;
+      o.re.hi = __shfl_down_sync(0xffffffffu, v.re.hi, dlt);
+      o.re.lo = __shfl_down_sync(0xffffffffu, v.re.lo, dlt);
+      o.im.hi = __shfl_down_sync(0xffffffffu, v.im.hi, dlt);
+      o.im.lo = __shfl_down_sync(0xffffffffu, v.im.lo, dlt);
+      v = cdd_add(v, o);
     }
     red[wid][lane] = v;
     __syncthreads();
-    if (wid == 0) {
-      if (BATCHED) {
-        cdd s2 = red[0][lane];
-        for (int w = 1; w < kWarps; ++w) s2 = cdd_add(s2, red[w][lane]);
-        if (b < a.B) a.gpart[((size_t)blockIdx.x * m + j) * a.B + b] = s2;
-      } else if (lane == 0) {
-        cdd s2 = red[0][0];
-        for (int w = 1; w < kWarps; ++w) s2 = cdd_add(s2, red[w][0]);
-        a.gpart[(size_t)blockIdx.x * m + j] = s2;
-      }
+    if (wid == 0 && lane == 0) {
+      cdd s2 = red[0][0];
+      for (int w = 1; w < kWarps; ++w) s2 = cdd_add(s2, red[w][0]);
+      a.gpart[(size_t)blockIdx.x * m + j] = s2;
     }
     __syncthreads();
   }
 }
 
+
+// Batched adjoint with a fraction of the accumulator registers: the lanes of a warp are
+// G mode groups x 32/G circuits.  Lane l serves circuit blockIdx.y * 32/G + l % (32/G) for
+// the modes j = (l / (32/G)) * MMAX/G + jj, so it keeps the float-float partials of
+// dL/du_j for MMAX/G modes; the G group parts of a parent's
+// a_{k-1} = sum_j conj(u_j) a_k[child_j] meet by log2(G) shuffles.  Every (parent, mode,
+// circuit) child value is loaded once, as in slos_bwd.
+template <int MMAX, int G>
+__global__ void __launch_bounds__(256, MMAX <= 16 ? 4 : 2) slos_bwd_g(SlosArgs a) {
+  constexpr int NC = 32 / G, MG = MMAX / G;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ cdd red[kWarps][32];
+  uint32_t* cn = reinterpret_cast<uint32_t*>(smem_raw);
+  cdd* us = reinterpret_cast<cdd*>(smem_raw + smem_cn_bytes(a.m, a.cn_stride));  // [j][NC circuits], conjugated
+  const int ncn = (a.m + 1) * a.cn_stride;
+  for (int i = threadIdx.x; i < ncn; i += blockDim.x) cn[i] = a.cn[i];
+  for (int i = threadIdx.x; i < MMAX * NC; i += blockDim.x) {
+    const int j = i / NC, b = blockIdx.y * NC + (i % NC);
+    us[i] = (j < a.m && b < a.B) ? cdd_conj(a.ucol[(size_t)j * a.B + b]) : cdd_zero();
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int cl = lane % NC, grp = lane / NC;
+  const int b = blockIdx.y * NC + cl;
+  const bool live = b < a.B;
+  const int m = a.m, p = a.p;
+  cacc g[MG];
+#pragma unroll
+  for (int jj = 0; jj < MG; ++jj) g[jj] = cacc_zero();
+  const uint32_t total = a.uoff[a.k + 1];
+  const uint32_t nw = gridDim.x * kWarps;
+  for (uint32_t unit = blockIdx.x * kWarps + wid; unit < total; unit += nw) {
+    const int r = unit_class(a, unit);
+    const int q = a.k - r;
+    const uint32_t S = a.tsize[r], lu = unit - a.uoff[r], cpt = a.cpt[r];
+    Desc<MMAX> d;
+    const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
+    describe<MMAX, true, false>(pi, q, r, a, cn, d, dd{0.f, 0.f}, d.base);
+    const uint32_t t0 = ch * a.chunkB, t1 = min(S, t0 + a.chunkB);
+    for (uint32_t tau = t0; tau < t1; ++tau) {
+      const size_t pidx = (size_t)(d.A + tau) * a.B + b;
+      const cdd cp = live ? cdd_conj(ld_cdd(&a.cpar[pidx])) : cdd_zero();
+      const uint32_t* row = a.tail + a.tail_off[r] + (size_t)tau * a.t;
+      cacc acc = cacc_zero();
+#pragma unroll
+      for (int jj = 0; jj < MG; ++jj) {
+        const int j = grp * MG + jj;
+        if (j < m && live) {
+          const uint32_t ad = j < p ? d.base[j] + tau : d.tb + __ldg(&row[j - p]);
+          const cdd v = ld_cdd(&a.in[(size_t)ad * a.B + b]);
+          cacc_fma(acc, v, us[j * NC + cl]);
+          cacc_fma(g[jj], v, cp);
+        }
+      }
+      cdd part = cacc_finish(acc);
+#pragma unroll
+      for (int dl = NC; dl < 32; dl <<= 1) {
+        cdd other;
+        other.re.hi = __shfl_xor_sync(0xffffffffu, part.re.hi, dl);
+        other.re.lo = __shfl_xor_sync(0xffffffffu, part.re.lo, dl);
+        other.im.hi = __shfl_xor_sync(0xffffffffu, part.im.hi, dl);
+        other.im.lo = __shfl_xor_sync(0xffffffffu, part.im.lo, dl);
+        part = cdd_add(part, other);
+      }
+      if (grp == 0 && live) a.out[pidx] = part;
+    }
+  }
+  // per-CTA partials: lane l holds mode (l / NC) * MG + jj of circuit l % NC
+#pragma unroll
+  for (int jj = 0; jj < MG; ++jj) {
+    red[wid][lane] = cacc_finish(g[jj]);
+    __syncthreads();
+    if (wid == 0) {
+      cdd s2 = red[0][lane];
+      for (int w = 1; w < kWarps; ++w) s2 = cdd_add(s2, red[w][lane]);
+      const int j = grp * MG + jj;
+      if (j < m && live) a.gpart[((size_t)blockIdx.x * m + j) * a.B + b] = s2;
+    }
+    __syncthreads();
+  }
+}
 
 // Last layer -> probabilities (mode 0), amplitudes (mode 1) or the adjoint seed
 // a_n = 2 w F c_n (mode 2), with F = prod(out!) / prod(in!) = f(tile) x ftail[tau].
@@ -706,8 +771,7 @@ static int launch_kernel(Kern kind, const SlosArgs& a, int grid, dd inv_in, int 
   dim3 g(grid, batched ? (a.B + 31) / 32 : 1);
   // the descriptors of 8 warps, u and the rank table may pass 48 KB: allow it
   cudaFuncSetAttribute(slos_fwdb<MMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaFuncSetAttribute(slos_bwd<MMAX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaFuncSetAttribute(slos_bwd<MMAX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(slos_bwd<MMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaFuncSetAttribute(slos_fin<MMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   switch (kind) {
     case Kern::Fwd:
@@ -728,10 +792,14 @@ static int launch_kernel(Kern kind, const SlosArgs& a, int grid, dd inv_in, int 
       break;
     }
     case Kern::Bwd:
-      if (batched)
-        slos_bwd<MMAX, true><<<g, 256, smem, s>>>(a);
-      else
-        slos_bwd<MMAX, false><<<g, 256, smem, s>>>(a);
+      if (batched) {
+        constexpr int G = kBwdGroups;
+        const dim3 gh(grid, (a.B + 32 / G - 1) / (32 / G));
+        const size_t smemh = smem_cn_bytes(a.m, a.cn_stride) + (size_t)MMAX * (32 / G) * sizeof(cdd);
+        slos_bwd_g<MMAX, G><<<gh, 256, smemh, s>>>(a);
+      } else {
+        slos_bwd<MMAX><<<g, 256, smem, s>>>(a);
+      }
       break;
     case Kern::Fin:
       if (batched) {

@@ -36,6 +36,19 @@ def test_grad_vs_oracle(native, oracle, B):
         assert np.abs(g[b] - ref).max() <= 1e-10 * np.abs(ref).max()
 
 
+def test_grad_batched_m20_partial_chunk(native, oracle):
+    """m = 20 (the 24-mode kernels), 17 circuits: a full and a partial chunk of 16."""
+    m, inp = 20, (1, 0, 1, 0, 0, 2) + (0,) * 14
+    B = 17
+    Us = np.stack([random_unitary(m, seed=80 + b) for b in range(B)])
+    count = math.comb(m + 4 - 1, 4)
+    w = np.random.default_rng(3).normal(size=(count, B))
+    p, g = gpu_grad(native, Us, inp, w)
+    for b in (0, 8, 15, 16):
+        ref = oracle.slos_grad(Us[b], inp, w[:, b])
+        assert np.abs(g[b] - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
 def perm_torch(a):
     n = a.shape[0]
     tot = torch.zeros((), dtype=a.dtype)
