@@ -740,6 +740,10 @@ def profile_case(name: str):
         plan = _native.SlosPlan(20, [1] * 10 + [0] * 10)
         plan.forward(torch.from_numpy(random_unitary(20, seed=0)).to(dev))
         plan.probabilities()
+    elif name == "slos20p":
+        # SLOS m = 20, n = 10, every probability with the last layer writing them directly
+        plan = _native.SlosPlan(20, [1] * 10 + [0] * 10)
+        plan.forward_probabilities(torch.from_numpy(random_unitary(20, seed=0)).to(dev))
     elif name == "slosmask22":
         # heralded SLOS m = 22, n = 11 (modes 18..21 detected as 1, 1, 0, 0): the largest kept
         # layer (k = 10) holds 7,330,675 states, 117 MB of amplitudes plus 0.3 GB of parent
@@ -792,8 +796,8 @@ def main():
                     help="run the learned-proposal sampler workload (n=30, m=900 and n=8, m=64) and exit")
     ap.add_argument("--learned-train", type=int, default=2048, help="exact training samples at n=30")
     ap.add_argument("--large-perm", action="store_true", help="one n = 40 permanent (about a minute)")
-    ap.add_argument("--profile-case", choices=["perm24", "slos20", "slosmask22", "slap1024", "slos16b256", "cc2017",
-                                               "gurvits20", "gemm"],
+    ap.add_argument("--profile-case", choices=["perm24", "slos20", "slos20p", "slosmask22", "slap1024", "slos16b256",
+                                               "cc2017", "gurvits20", "gemm"],
                     help="run one small untimed case of a single kernel (for ncu) and exit")
     args = ap.parse_args()
     if args.profile_case:
