@@ -39,7 +39,9 @@ void set_error(const char* fmt, ...);
 
 // Workspace cached per (device, slot); grown on demand, freed by
 // pcvl_release_workspace().  Slots let independent kernels keep their buffers.
-enum WorkspaceSlot { WS_PERM = 0, WS_PERM_ITEMS = 1, WS_CC2017 = 2, WS_GURVITS = 3, WS_SLAP = 4, WS_SLOTS = 5 };
+enum WorkspaceSlot {
+  WS_PERM = 0, WS_PERM_ITEMS = 1, WS_CC2017 = 2, WS_GURVITS = 3, WS_SLAP = 4, WS_MASK = 5, WS_SLOTS = 6
+};
 int workspace(int slot, size_t bytes, void** ptr);
 
 // Copies `bytes` of host memory to device memory on `stream` through a pinned

@@ -440,7 +440,8 @@ int mask_ranks(int32_t m, int32_t n, int32_t n_masks, const int8_t* digits_h, co
   const size_t o_suf = o_atl + align_up(m, 16), o_bsum = o_suf + align_up(suf.size() * 4, 16);
   const size_t o_boff = o_bsum + align_up(nb * 4, 16), total = o_boff + nb * 8;
   void* ws = nullptr;
-  PCVL_TRY(workspace(WS_SLAP, total, &ws));
+  // its own slot: a SLAP walk still running on another stream keeps its tables
+  PCVL_TRY(workspace(WS_MASK, total, &ws));
   unsigned char* base = static_cast<unsigned char*>(ws);
   PCVL_CUDA(cudaMemcpy(base, cn.data(), cn.size() * 8, cudaMemcpyHostToDevice));
   PCVL_CUDA(cudaMemcpy(base + o_dg, digits_h, (size_t)n_masks * m, cudaMemcpyHostToDevice));
