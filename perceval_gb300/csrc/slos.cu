@@ -205,10 +205,10 @@ __device__ __forceinline__ cdd* load_shared(const SlosArgs& a, unsigned char* ra
   return u;
 }
 
-// Forward value of state (d, tau) with r tail photons: sum over its occupied modes of
-// u_j x[parent_j].  Prefix modes follow the tile mask (uniform over a tile); tail
-// modes loop over the set bits of the state's own tail occupation.
-template <int MMAX, bool BATCHED>
+// Forward value of state (d, tau) with r tail photons for circuit b of a batch: sum over
+// its occupied modes of u_j x[parent_j].  Prefix modes follow the tile mask (uniform over
+// a tile); tail modes loop over the set bits of the state's own tail occupation.
+template <int MMAX>
 __device__ __forceinline__ cdd fwd_value(const SlosArgs& a, const Desc<MMAX>& d, int r, uint32_t tau,
                                          const cdd* __restrict__ x, const cdd* u, int us, int b) {
   const int p = a.p;
@@ -217,7 +217,7 @@ __device__ __forceinline__ cdd fwd_value(const SlosArgs& a, const Desc<MMAX>& d,
   for (int j = 0; j < MMAX; ++j) {
     if (j < p && ((d.mask >> j) & 1u)) {
       const uint32_t ad = d.base[j] + tau;
-      cacc_fma(acc, ld_cdd(&x[BATCHED ? (size_t)ad * a.B + b : (size_t)ad]), u[j * us]);
+      cacc_fma(acc, ld_cdd(&x[(size_t)ad * a.B + b]), u[j * us]);
     }
   }
   if (r > 0) {
@@ -227,7 +227,7 @@ __device__ __forceinline__ cdd fwd_value(const SlosArgs& a, const Desc<MMAX>& d,
       const int jl = __ffs(occ) - 1;
       occ &= occ - 1;
       const uint32_t ad = d.tb + __ldg(&row[jl]);
-      cacc_fma(acc, ld_cdd(&x[BATCHED ? (size_t)ad * a.B + b : (size_t)ad]), u[(p + jl) * us]);
+      cacc_fma(acc, ld_cdd(&x[(size_t)ad * a.B + b]), u[(p + jl) * us]);
     }
   }
   return cacc_finish(acc);
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(256, 4) slos_fwdb(SlosArgs a) {
     const uint32_t t0 = ch * a.chunkB, t1 = min(S, t0 + a.chunkB);
     if (b < a.B)
       for (uint32_t tau = t0; tau < t1; ++tau)
-        a.out[(size_t)(d.A + tau) * a.B + b] = fwd_value<MMAX, true>(a, d, r, tau, a.in, u, 32, b);
+        a.out[(size_t)(d.A + tau) * a.B + b] = fwd_value<MMAX>(a, d, r, tau, a.in, u, 32, b);
   }
 }
 
