@@ -60,6 +60,40 @@ def test_argument_errors_are_reported_without_device_work(lib):
     assert rc == 1 and "outside" in _native.last_error()
 
 
+def test_masked_slap_and_mask_ranks_refuse_bad_arguments(lib):
+    """New entry points check their arguments on the host, before any device work; the
+    SLAP output count is host-only: C(m + n - 1, n)."""
+    import math
+
+    import numpy as np
+    from perceval_gb300 import _native
+    L = _native.load(require_cuda=False)
+    h = ctypes.c_void_p()
+    inp = np.array([1, 1, 0, 0], dtype=np.int32)
+    digits = np.array([[-1, -1, 0, 0]], dtype=np.int8)
+    assert L.pcvl_slos_plan_create_masked(ctypes.byref(h), 4, inp.ctypes.data, 1, 0, 0, digits.ctypes.data, 0, 2) == 1
+    assert "n_masks" in _native.last_error()
+    bad = np.array([[-1, -2, 0, 0]], dtype=np.int8)
+    assert L.pcvl_slos_plan_create_masked(ctypes.byref(h), 4, inp.ctypes.data, 1, 0, 1, bad.ctypes.data, 0, 2) == 1
+    assert "digit" in _native.last_error()
+    two = np.array([1, 1, 0, 0, 1, 0, 0, 0], dtype=np.int32)
+    assert L.pcvl_slos_plan_create_masked(ctypes.byref(h), 4, two.ctypes.data, 2, 0, 1, digits.ctypes.data, 0, 2) == 1
+    assert "photon count" in _native.last_error()
+    kept = ctypes.c_int64()
+    assert L.pcvl_fock_mask_ranks(0, 2, 1, digits.ctypes.data, None, 2, None, 0, ctypes.byref(kept)) == 1
+    assert L.pcvl_fock_mask_ranks(4, 2, 1, bad.ctypes.data, None, 2, None, 0, ctypes.byref(kept)) == 1
+    c = ctypes.c_int64()
+    for m, n in [(4, 2), (64, 6), (1024, 3), (3, 12)]:
+        state = np.zeros(m, dtype=np.int32)
+        state[0] = n
+        assert L.pcvl_slap_output_count(m, state.ctypes.data, ctypes.byref(c)) == 0
+        assert c.value == math.comb(m + n - 1, n)
+    state = np.zeros(4, dtype=np.int32)
+    state[0] = 13
+    assert L.pcvl_slap_output_count(4, state.ctypes.data, ctypes.byref(c)) == 1
+    assert "photons" in _native.last_error()
+
+
 def test_product_path_has_no_cpu_fallback():
     import torch
     from perceval_gb300 import _native
