@@ -101,13 +101,19 @@ __device__ __forceinline__ void slap_level(const SlapArgs& a, cdd* F, int k, int
   __syncwarp();
 }
 
-// outputs (prefix elem[0..n-2], a_n) for a_n = lo .. m-1 at positions pos ..
-__device__ __forceinline__ void slap_leaves(const SlapArgs& a, const cdd* F, const int* elem, int lo, uint64_t pos,
-                                            int lane) {
-  const int n = a.n;
-  // 1 / (prod s! prod t!) (its square root for amplitudes) from float-float tables on the
-  // FP32 pipe: every run of equal prefix elements but the last contributes invf[length];
-  // the last run contributes invf[run] when x is past it and invf[run + 1] when x extends it
+__device__ __forceinline__ void slap_store(const SlapArgs& a, uint64_t o, const cdd& c, const dd& f) {
+  if (a.mode == 0) {
+    const dd c2 = dd_add(dd_mul(c.re, c.re), dd_mul(c.im, c.im));
+    a.out_p[o] = dd_to_double_fast(dd_mul(c2, f));
+  } else {
+    a.out_a[o] = make_double2(dd_to_double_fast(dd_mul(c.re, f)), dd_to_double_fast(dd_mul(c.im, f)));
+  }
+}
+
+// The outputs of the node elem[0..n-2] (F valid up to level n - 1): (..., y) for
+// y = elem[n-2] .. m-1, one per lane, at positions pos ..  (units that fix n - 1 elements)
+__device__ void slap_leaves(const SlapArgs& a, const cdd* F, const int* elem, uint64_t pos, int lane) {
+  const int n = a.n, m = a.m;
   dd base = a.inv_t;
   int run = 0;
   for (int e = 0; e < n - 1; ++e) {
@@ -118,24 +124,87 @@ __device__ __forceinline__ void slap_leaves(const SlapArgs& a, const cdd* F, con
       run = 1;
     }
   }
-  const int xr = n > 1 ? elem[n - 2] : -1;
-  const dd f0 = run > 0 ? dd_mul(base, a.invf[run]) : base;
-  const dd f1 = dd_mul(base, a.invf[run + 1]);
+  const int lo = elem[n - 2];
+  const dd f0 = dd_mul(base, a.invf[run]), f1 = dd_mul(base, a.invf[run + 1]);
   const uint32_t full = (1u << n) - 1u;
-  for (int x = lo + lane; x < a.m; x += 32) {
-    const cdd* ux = a.uc + (size_t)x * n;
+  for (int y = lo + lane; y < m; y += 32) {
+    const cdd* uy = a.uc + (size_t)y * n;
     cacc acc = cacc_zero();
-    for (int p = 0; p < n; ++p) cacc_fma(acc, F[full ^ (1u << p)], ux[p]);
-    const cdd c = cacc_finish(acc);
-    const dd f = x == xr ? f1 : f0;
-    const uint64_t o = pos + (uint64_t)(x - lo);
-    if (a.mode == 0) {
-      const dd c2 = dd_add(dd_mul(c.re, c.re), dd_mul(c.im, c.im));
-      a.out_p[o] = dd_to_double_fast(dd_mul(c2, f));
+    for (int p = 0; p < n; ++p) cacc_fma(acc, F[full ^ (1u << p)], uy[p]);
+    slap_store(a, pos + (uint64_t)(y - lo), cacc_finish(acc), y == lo ? f1 : f0);
+  }
+}
+
+// The last two levels of the node elem[0..n-3] (F valid up to level n - 2; n >= 2): for the
+// siblings x = v0 .. m-1 (v0 = elem[n-3], or 0 for n = 2), in chunks of 32,
+//   level n-1: Fs[x][p] = F_{n-1}(x)[all \ {p}] = sum_{q != p} F[all \ {p, q}] U[x, c_q]
+// with the lanes over (x, p) pairs, then every output (..., x, y), y >= x:
+//   F_n = sum_p Fs[x][p] U[y, c_p],
+// with the lanes over the chunk's outputs in order (rows x, columns y: a contiguous range
+// of the output order).  Normalisation 1 / (prod s! prod t!) (its square root for
+// amplitudes) from float-float tables on the FP32 pipe: the prefix's closed runs give
+// base, its last run (length r0, value v0) is closed by x > v0 or extended by x = v0, and
+// y = x adds one more to the run of x.  Returns the position after the node's outputs.
+__device__ uint64_t slap_batch(const SlapArgs& a, const cdd* F, cdd* Fs, const int* elem, uint64_t pos, int lane) {
+  const int n = a.n, m = a.m;
+  dd base = a.inv_t;
+  int run = 0;
+  for (int e = 0; e < n - 2; ++e) {
+    if (e > 0 && elem[e] == elem[e - 1]) {
+      ++run;
     } else {
-      a.out_a[o] = make_double2(dd_to_double_fast(dd_mul(c.re, f)), dd_to_double_fast(dd_mul(c.im, f)));
+      if (run > 0) base = dd_mul(base, a.invf[run]);
+      run = 1;
     }
   }
+  const int v0 = n >= 3 ? elem[n - 3] : 0;
+  const dd A0 = run > 0 ? dd_mul(base, a.invf[run]) : base;
+  const dd A1 = dd_mul(base, a.invf[run + 1]), A2 = dd_mul(base, a.invf[run + 2]);
+  const dd A0y = dd_mul(A0, a.invf[2]);
+  const uint32_t full = (1u << n) - 1u;
+  for (int x0 = v0; x0 < m; x0 += 32) {
+    const int nx = min(32, m - x0);
+    for (int t = lane; t < nx * n; t += 32) {
+      const int xi = t / n, p = t - xi * n;
+      const uint32_t M = full ^ (1u << p);
+      const cdd* ux = a.uc + (size_t)(x0 + xi) * n;
+      cacc acc = cacc_zero();
+      for (uint32_t r = M; r; r &= r - 1) {
+        const int q = __ffs(r) - 1;
+        cacc_fma(acc, F[M ^ (1u << q)], ux[q]);
+      }
+      Fs[t] = cacc_finish(acc);
+    }
+    __syncwarp();
+    // rows xi = 0 .. nx-1 hold y = x0 + xi .. m-1 (lengths m - x0 - xi)
+    const uint64_t total = (uint64_t)nx * (m - x0) - (uint64_t)nx * (nx - 1) / 2;
+    uint64_t t = lane;
+    int xi = 0, y = x0 + lane;
+    while (xi < nx && y >= m) {
+      const int over = y - m;
+      ++xi;
+      y = x0 + xi + over;
+    }
+    while (xi < nx) {
+      const int x = x0 + xi;
+      const cdd* uy = a.uc + (size_t)y * n;
+      const cdd* fx = Fs + xi * n;
+      cacc acc = cacc_zero();
+      for (int p = 0; p < n; ++p) cacc_fma(acc, fx[p], uy[p]);
+      const dd f = (n >= 3 && x == v0) ? (y == x ? A2 : A1) : (y == x ? A0y : A0);
+      slap_store(a, pos + t, cacc_finish(acc), f);
+      t += 32;
+      y += 32;
+      while (xi < nx && y >= m) {
+        const int over = y - m;
+        ++xi;
+        y = x0 + xi + over;
+      }
+    }
+    __syncwarp();  // Fs is rewritten by the next chunk
+    pos += total;
+  }
+  return pos;
 }
 
 // Sorted mode list el[0..k-1] of rank r among the k-element lists on modes lo..m-1.  The
@@ -167,6 +236,7 @@ __global__ void __launch_bounds__(256) slap_walk(SlapArgs a) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int n = a.n, m = a.m, k0 = a.k0;
   cdd* F = reinterpret_cast<cdd*>(smem_raw) + ((size_t)w << n);
+  cdd* Fs = reinterpret_cast<cdd*>(smem_raw) + ((size_t)blockDim.x / 32 << n) + (size_t)w * 32 * n;
   int elem[kSlapMaxN], pre[kSlapMaxN];
   while (true) {
     unsigned long long c = 0;
@@ -197,24 +267,30 @@ __global__ void __launch_bounds__(256) slap_walk(SlapArgs a) {
           prev = aj;
         }
       }
-      if (k0 == n - 1) {
-        slap_leaves(a, F, elem, k0 > 0 ? elem[k0 - 1] : 0, pos, lane);
+      if (n == 1) {  // every output is one element: U[x, c_0] / sqrt(prod t!)
+        for (int x = lane; x < m; x += 32) slap_store(a, pos + x, cdd{a.uc[x].re, a.uc[x].im}, a.inv_t);
+        continue;
+      }
+      if (k0 == n - 1) {  // the prefix fixes level n - 1: its outputs only
+        slap_leaves(a, F, elem, pos, lane);
         __syncwarp();  // the next unit rewrites level n - 1
+        continue;
+      }
+      if (k0 == n - 2) {
+        slap_batch(a, F, Fs, elem, pos, lane);
         continue;
       }
       int k = k0;
       elem[k] = k > 0 ? elem[k - 1] : 0;
       while (true) {
         slap_level(a, F, k, elem[k], lane);
-        if (k + 1 == n - 1) {
-          slap_leaves(a, F, elem, elem[k], pos, lane);
-          pos += (uint64_t)(m - elem[k]);
+        if (k + 1 == n - 2) {
+          pos = slap_batch(a, F, Fs, elem, pos, lane);
           while (true) {
             if (++elem[k] < m) break;
             if (--k < k0) break;
           }
           if (k < k0) break;
-          __syncwarp();  // the leaves read level n - 1 before it is rewritten
         } else {
           ++k;
           elem[k] = elem[k - 1];
@@ -271,11 +347,30 @@ int slap_run(const double* u_d, int32_t m, const int32_t* input_state_h, int32_t
       if (__builtin_popcount(M) == k) masks.push_back((uint16_t)M);
   }
   moff[n + 1] = (uint32_t)masks.size();
-  // work units: the smallest prefix length giving every resident warp several chunks
-  const int W = std::max(1, std::min(8, kSlapSmemBudget / (int)(sizeof(cdd) << n)));
-  const uint64_t want = (uint64_t)num_sms() * W * 8 * kSlapChunk;
-  int k0 = 0;
-  while (k0 < n - 1 && cn[(size_t)m * cs + k0] < want) ++k0;
+  const int warp_bytes = (int)(sizeof(cdd) * ((1 << n) + 32 * n));  // subset table + sibling level
+  const int W = std::max(1, std::min(8, kSlapSmemBudget / warp_bytes));
+  const size_t smem = (size_t)W * warp_bytes;
+  PCVL_CUDA(cudaFuncSetAttribute(slap_walk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  PCVL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, slap_walk, W * 32, smem));
+  per_sm = std::max(per_sm, 1);
+  // Work units: prefixes of k0 elements.  A node of level n - 1 has about m / n outputs.
+  // From m >= 16 n on they keep at least half the lanes busy: units fix n - 1 elements and
+  // write their outputs (k0 = n - 1).  Below that the walk ends with the sibling batches of
+  // level n - 2 (k0 <= n - 2): the smallest k0 giving every resident warp eight chunks (the
+  // first units have the largest subtrees), or n - 2.  (Measured: m = 1024, n = 3 and
+  // m = 256, n = 4 run 2-60x faster on the first form; m = 64, n = 6, m = 32, n = 8 and
+  // m = 24, n = 10 run 3-6x faster on the second.)
+  const uint64_t warps = (uint64_t)num_sms() * per_sm * W;
+  int k0 = n - 1;
+  if (n >= 2 && m < 16 * n) {
+    k0 = n - 2;
+    for (int k = 0; k < n - 2; ++k)
+      if (cn[(size_t)m * cs + k] >= warps * 8 * kSlapChunk) {
+        k0 = k;
+        break;
+      }
+  }
   // 1 / k! (probabilities) or 1 / sqrt(k!) (amplitudes), k = 0..n+1, as float-float
   std::vector<dd> invf(n + 2);
   {
@@ -322,12 +417,8 @@ int slap_run(const double* u_d, int32_t m, const int32_t* input_state_h, int32_t
   a.out_p = out_d;
   a.out_a = (double2*)out_d;
   a.next = (unsigned long long*)(base + o_next);
-  const size_t smem = (size_t)W * (sizeof(cdd) << n);
-  PCVL_CUDA(cudaFuncSetAttribute(slap_walk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 0;
-  PCVL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, slap_walk, W * 32, smem));
   const uint64_t blocks_needed = ((a.units + kSlapChunk - 1) / kSlapChunk + W - 1) / W;
-  const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)num_sms() * std::max(per_sm, 1)));
+  const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)num_sms() * per_sm));
   slap_walk<<<grid, W * 32, smem, s>>>(a);
   PCVL_CUDA(cudaGetLastError());
   return PCVL_OK;
