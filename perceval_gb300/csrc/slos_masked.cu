@@ -62,7 +62,19 @@ struct MaskSpace {
 };
 
 __device__ __forceinline__ uint64_t cnv(const MaskSpace& s, int M, int x) {
-  return x < 0 ? 0ull : __ldg(&s.cn[M * s.cs + x]);
+  return x < 0 ? 0ull : s.cn[M * s.cs + x];
+}
+
+// The table Cn in shared memory for the kernels that unrank every state: returns the
+// space with cn pointing to the shared copy.
+constexpr int kCnWords = (kMaskMaxM + 1) * (kMaskMaxN + 2);
+__device__ __forceinline__ MaskSpace shared_cn(const MaskSpace& s, uint64_t* buf) {
+  const int words = (s.m + 1) * s.cs;
+  for (int i = threadIdx.x; i < words; i += blockDim.x) buf[i] = s.cn[i];
+  __syncthreads();
+  MaskSpace t = s;
+  t.cn = buf;
+  return t;
 }
 
 // Occupation of the state of rank r among the k-photon states.  On modes i..m-1 with
@@ -134,10 +146,12 @@ __device__ uint32_t accepted_children(const MaskSpace& s, int k, const uint8_t* 
 // parents b * 256 ..).  Count pass (out == nullptr): the block's number of kept
 // children to bsum[b].  Write pass: their full-space ranks, in parent order then mode
 // order, from position boff[b].
-__global__ void __launch_bounds__(kGenThreads) mask_gen(MaskSpace s, int k, const uint64_t* __restrict__ prev,
+__global__ void __launch_bounds__(kGenThreads) mask_gen(MaskSpace sg, int k, const uint64_t* __restrict__ prev,
                                                        uint64_t nprev, const uint64_t* __restrict__ boff,
                                                        uint32_t* __restrict__ bsum, uint64_t* __restrict__ out) {
   __shared__ uint32_t wsum[kGenThreads / 32];
+  __shared__ uint64_t cn_s[kCnWords];
+  const MaskSpace s = shared_cn(sg, cn_s);
   const uint64_t i = (uint64_t)blockIdx.x * kGenThreads + threadIdx.x;
   uint8_t v[kMaskMaxM];
   uint32_t ok = 0;
@@ -183,45 +197,82 @@ __global__ void __launch_bounds__(kGenThreads) mask_gen(MaskSpace s, int k, cons
   }
 }
 
+// Smallest index >= start of a value >= r in the ascending prev[0..n) (n if none):
+// exponential probing from start, then a binary search in the bracket.
+__device__ __forceinline__ uint64_t gallop(const uint64_t* __restrict__ prev, uint64_t n, uint64_t start,
+                                           uint64_t r) {
+  uint64_t lo = start, hi = n, step = 1;
+  while (true) {
+    const uint64_t probe = lo + step - 1;
+    if (probe >= n) break;
+    if (prev[probe] >= r) {
+      hi = probe;
+      break;
+    }
+    lo = probe + 1;
+    step <<= 1;
+  }
+  while (lo < hi) {
+    const uint64_t mid = (lo + hi) >> 1;
+    if (prev[mid] < r)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+constexpr int kParentRun = 16;  // most consecutive kept states per thread of mask_parents
+
 // Per kept state i of layer k: occupied-mode bits, the index in layer k-1 of each parent
 // (par[e * ncur + i] for its e-th occupied mode) and, on the last layer, prod(out!).
-__global__ void __launch_bounds__(256) mask_parents(MaskSpace s, int k, const uint64_t* __restrict__ cur,
+// rank(c - e_j) = rank(c) - sum_{i<j} Cn(m - i - 1, R_{i+1}(c) - 1).  For a fixed mode j,
+// c -> c - e_j keeps the order, so a thread takes `run` consecutive states (1 .. kParentRun,
+// fewer on small layers to keep every SM busy) and finds each parent by galloping forward
+// from the previous state's parent through the same mode.
+__global__ void __launch_bounds__(256) mask_parents(MaskSpace sg, int k, const uint64_t* __restrict__ cur,
                                                     uint64_t ncur, const uint64_t* __restrict__ prev,
                                                     uint64_t nprev, uint32_t* __restrict__ occ,
                                                     uint32_t* __restrict__ par, dd* __restrict__ fact,
-                                                    int* __restrict__ err) {
+                                                    int* __restrict__ err, int run_len) {
+  __shared__ uint64_t cn_s[kCnWords];
+  const MaskSpace s = shared_cn(sg, cn_s);
+  const uint64_t runs = (ncur + run_len - 1) / run_len;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ncur; i += stride) {
-    uint8_t v[kMaskMaxM];
-    unrank_state(s, k, cur[i], v);
-    uint32_t om = 0;
-    uint64_t e = 0;
-    double f = 1.0;
-    for (int j = 0; j < s.m; ++j) {
-      if (!v[j]) continue;
-      om |= 1u << j;
-      for (int t = 2; t <= v[j]; ++t) f *= (double)t;
-      --v[j];
-      const uint64_t r = rank_state(s, k - 1, v);
-      ++v[j];
-      uint64_t lo = 0, hi = nprev;
-      while (lo < hi) {
-        const uint64_t mid = (lo + hi) >> 1;
-        if (prev[mid] < r)
-          lo = mid + 1;
-        else
-          hi = mid;
+  for (uint64_t run = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; run < runs; run += stride) {
+    uint64_t next[kMaskMaxM];  // per mode: where the next parent search starts
+    for (int j = 0; j < s.m; ++j) next[j] = 0;
+    const uint64_t i1 = min(ncur, (run + 1) * run_len);
+    for (uint64_t i = run * run_len; i < i1; ++i) {
+      uint8_t v[kMaskMaxM];
+      const uint64_t rc = cur[i];
+      unrank_state(s, k, rc, v);
+      uint32_t om = 0;
+      uint64_t e = 0, sub = 0;
+      int after = k;
+      double f = 1.0;
+      for (int j = 0; j < s.m; ++j) {
+        if (v[j]) {
+          om |= 1u << j;
+          for (int t = 2; t <= v[j]; ++t) f *= (double)t;
+          const uint64_t r = rc - sub;
+          const uint64_t lo = gallop(prev, nprev, next[j], r);
+          uint32_t idx = (uint32_t)lo;
+          if (lo >= nprev || prev[lo] != r) {
+            atomicExch(err, 1);
+            idx = 0;
+          } else {
+            next[j] = lo + 1;
+          }
+          par[e * ncur + i] = idx;
+          ++e;
+        }
+        after -= v[j];
+        sub += cnv(s, s.m - j - 1, after - 1);
       }
-      uint32_t idx = (uint32_t)lo;
-      if (lo >= nprev || prev[lo] != r) {
-        atomicExch(err, 1);
-        idx = 0;
-      }
-      par[e * ncur + i] = idx;
-      ++e;
+      occ[i] = om;
+      if (fact) fact[i] = dd_from_double(f);
     }
-    occ[i] = om;
-    if (fact) fact[i] = dd_from_double(f);
   }
 }
 
@@ -575,9 +626,11 @@ int slos_masked_create(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, 
     if ((rc = slos_alloc((void**)&p->mpar_d[k], width * total * 4, p->bytes)) != PCVL_OK) goto fail;
     if (k == n && (rc = slos_alloc((void**)&p->mfact_d, total * sizeof(dd), p->bytes)) != PCVL_OK) goto fail;
     if (total > 0) {
-      mask_parents<<<grid_for(total, 8), 256>>>(sp, k, (const uint64_t*)cur.p, total, (const uint64_t*)prev_d.p,
-                                                nprev, p->mocc_d[k], p->mpar_d[k], k == n ? p->mfact_d : nullptr,
-                                                (int*)err_d.p);
+      const int run_len = (int)std::max<uint64_t>(
+          1, std::min<uint64_t>(kParentRun, total / ((uint64_t)num_sms() * 4096)));
+      mask_parents<<<grid_for((total + run_len - 1) / run_len, 8), 256>>>(
+          sp, k, (const uint64_t*)cur.p, total, (const uint64_t*)prev_d.p, nprev, p->mocc_d[k], p->mpar_d[k],
+          k == n ? p->mfact_d : nullptr, (int*)err_d.p, run_len);
       if (cudaGetLastError() != cudaSuccess) goto cuda_fail;
     }
     if (p->keep) {
