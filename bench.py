@@ -417,8 +417,15 @@ def secondary(torch, _native, random_unitary, dev, flush):
     t_fused = timed(lambda: plan.forward_probabilities(Ud, probs), reps=2)
     Ls = [math.comb(m + k - 1, k) for k in range(n + 1)]
     alg_bytes = 16 * sum(Ls[k - 1] + Ls[k] for k in range(1, n + 1))
+    # the arithmetic floor: layer k has m L_{k-1} (state, occupied mode) terms (the states with
+    # mode 0 occupied number L_{k-1}); a float-float complex multiply-add is 48 FP32 operations,
+    # at the 36.8 T FP32 operations/s measured on this part
+    terms = m * sum(Ls[k - 1] for k in range(1, n + 1))
+    fp32_floor_ms = terms * 48 / 36.8e12 * 1e3
     res["slos_m24_n12"] = {"amps_per_s": Ls[n] / (t_fwd * 1e-3), "forward_ms": t_fwd, "probabilities_ms": t_prob,
-                           "forward_probabilities_ms": t_fused, "algorithmic_gb": alg_bytes / 1e9,
+                           "forward_probabilities_ms": t_fused, "multiply_add_terms": terms,
+                           "fp32_floor_ms": fp32_floor_ms, "fp32_frac": fp32_floor_ms / t_fwd,
+                           "algorithmic_gb": alg_bytes / 1e9,
                            "hbm_frac": alg_bytes / (t_fwd * 1e-3) / 1e9 / hbm, "hbm_peak_gbs": hbm,
                            "sum_p": float(probs.sum())}
     del plan, probs
