@@ -134,15 +134,20 @@ struct GvArgs {
 
 template <int NMAX>
 __global__ void __launch_bounds__(kGvThreads) gv_sample(GvArgs a) {
-  __shared__ float2 As[NMAX * NMAX];
+  // rows padded to an even length (a zero column for odd n): two adjacent columns are one
+  // 16-byte load, so each load of the matrix feeds four multiply-adds
+  constexpr int NS = (NMAX + 1) & ~1;
+  __shared__ __align__(16) float2 As[NMAX * NS];
   __shared__ double2 red[kGvThreads / 32];
   const int mi = a.cta_mat[blockIdx.x];
   const GvDesc d = a.descs[mi];
   const int n = d.n, tid = threadIdx.x;
   const int c = (int)((int64_t)blockIdx.x - d.part);  // CTA index = partial index
   const int e = a.scale_exp[mi];
-  for (int x = tid; x < n * n; x += blockDim.x) {
-    const double2 v = a.mats[d.off + x];
+  const int ns = (n + 1) & ~1;
+  for (int x = tid; x < n * ns; x += blockDim.x) {
+    const int i = x / ns, j = x - i * ns;
+    const double2 v = j < n ? a.mats[d.off + (int64_t)i * n + j] : make_double2(0.0, 0.0);
     As[x] = make_float2((float)ldexp(v.x, -e), (float)ldexp(v.y, -e));
   }
   __syncthreads();
@@ -164,19 +169,26 @@ __global__ void __launch_bounds__(kGvThreads) gv_sample(GvArgs a) {
       if (i < n) par ^= bit;
     }
     float pr = 1.f, pi = 0.f;
-    for (int j = 0; j < n; ++j) {
-      float yr = 0.f, yi = 0.f;
+    for (int j = 0; j < n; j += 2) {
+      float yr = 0.f, yi = 0.f, zr = 0.f, zi = 0.f;  // columns j and j + 1
 #pragma unroll
       for (int i = 0; i < NMAX; ++i) {
         if (i < n) {
-          const float2 v = As[i * n + j];
+          const float4 v = *reinterpret_cast<const float4*>(&As[i * ns + j]);
           yr = fmaf(s[i], v.x, yr);
           yi = fmaf(s[i], v.y, yi);
+          zr = fmaf(s[i], v.z, zr);
+          zi = fmaf(s[i], v.w, zi);
         }
       }
-      const float tr = pr * yr - pi * yi;
+      float tr = pr * yr - pi * yi;
       pi = fmaf(pr, yi, pi * yr);
       pr = tr;
+      if (j + 1 < n) {
+        tr = pr * zr - pi * zi;
+        pi = fmaf(pr, zi, pi * zr);
+        pr = tr;
+      }
     }
     if (par) {
       pr = -pr;
