@@ -45,17 +45,20 @@ struct GvDesc {
 };
 
 // ---------------------------------------------------------------- norm bound
-// Dynamic shared memory: A (n x n), M and M^2 (n x n each), double2.
+// Float-float on the FP32 pipe (GB300's FP64 rate would make this the costliest part of a
+// call).  The matrix is first scaled by 2^-ea (ea: exponent of its largest entry) so every
+// product stays far inside the FP32 range; the bound is unscaled at the end.
+// Dynamic shared memory: A (n x n), M and M^2 (n x n each), float-float complex.
 __global__ void __launch_bounds__(128) gv_norm(const double2* __restrict__ mats, const GvDesc* __restrict__ descs,
                                                double* __restrict__ log2_bound, int32_t* __restrict__ scale_exp) {
   extern __shared__ __align__(16) unsigned char smem[];
   const GvDesc d = descs[blockIdx.x];
   const int n = d.n, tid = threadIdx.x;
-  double2* A = reinterpret_cast<double2*>(smem);
-  double2* M = A + n * n;
-  double2* M2 = M + n * n;
+  cdd* A = reinterpret_cast<cdd*>(smem);
+  cdd* M = A + n * n;
+  cdd* M2 = M + n * n;
   __shared__ double red[128];
-  __shared__ double s_log2;  // log2 of the running bound on lambda_max(A^H A)
+  __shared__ double s_log2;  // log2 of the running bound on lambda_max(A^H A), scaled A
   if (n == 0) {
     if (tid == 0) {
       log2_bound[blockIdx.x] = 0.0;
@@ -63,28 +66,41 @@ __global__ void __launch_bounds__(128) gv_norm(const double2* __restrict__ mats,
     }
     return;
   }
-  for (int e = tid; e < n * n; e += blockDim.x) A[e] = mats[d.off + e];
+  // largest |entry| -> exponent ea
+  double amax = 0.0;
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    const double2 v = mats[d.off + e];
+    amax = fmax(amax, fmax(fabs(v.x), fabs(v.y)));
+  }
+  red[tid] = amax;
+  __syncthreads();
+  for (int st = 64; st > 0; st >>= 1) {
+    if (tid < st) red[tid] = fmax(red[tid], red[tid + st]);
+    __syncthreads();
+  }
+  const int ea = red[0] > 0.0 ? ilogb(red[0]) + 1 : 0;
+  __syncthreads();
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    const double2 v = mats[d.off + e];
+    A[e] = cdd_from(ldexp(v.x, -ea), ldexp(v.y, -ea));
+  }
   __syncthreads();
   // M = A^H A: M_ij = sum_k conj(a_ki) a_kj
   for (int e = tid; e < n * n; e += blockDim.x) {
     const int i = e / n, j = e - i * n;
-    double re = 0.0, im = 0.0;
-    for (int k = 0; k < n; ++k) {
-      const double2 a = A[k * n + i], b = A[k * n + j];
-      re = fma(a.x, b.x, fma(a.y, b.y, re));
-      im = fma(a.x, b.y, fma(-a.y, b.x, im));
-    }
-    M[e] = make_double2(re, im);
+    cacc acc = cacc_zero();
+    for (int k = 0; k < n; ++k) cacc_fma(acc, cdd_conj(A[k * n + i]), A[k * n + j]);
+    M[e] = cacc_finish(acc);
   }
   __syncthreads();
   // trace-normalised repeated squaring
   for (int q = 0; q <= kGvSquarings; ++q) {
     double t = 0.0;
-    for (int i = tid; i < n; i += blockDim.x) t += M[i * n + i].x;
+    for (int i = tid; i < n; i += blockDim.x) t += dd_to_double(M[i * n + i].re);
     red[tid] = t;
     __syncthreads();
-    for (int s = 64; s > 0; s >>= 1) {
-      if (tid < s) red[tid] += red[tid + s];
+    for (int st = 64; st > 0; st >>= 1) {
+      if (tid < st) red[tid] += red[tid + st];
       __syncthreads();
     }
     const double tr = red[0];
@@ -95,28 +111,24 @@ __global__ void __launch_bounds__(128) gv_norm(const double2* __restrict__ mats,
     }
     __syncthreads();
     if (!(tr > 0.0) || q == kGvSquarings) break;
-    const double inv = 1.0 / tr;
-    for (int e = tid; e < n * n; e += blockDim.x) M[e] = make_double2(M[e].x * inv, M[e].y * inv);
+    const dd inv = dd_from_double(1.0 / tr);
+    for (int e = tid; e < n * n; e += blockDim.x) M[e] = {dd_mul(M[e].re, inv), dd_mul(M[e].im, inv)};
     __syncthreads();
     for (int e = tid; e < n * n; e += blockDim.x) {
       const int i = e / n, j = e - i * n;
-      double re = 0.0, im = 0.0;
-      for (int k = 0; k < n; ++k) {
-        const double2 a = M[i * n + k], b = M[k * n + j];
-        re = fma(a.x, b.x, fma(-a.y, b.y, re));
-        im = fma(a.x, b.y, fma(a.y, b.x, im));
-      }
-      M2[e] = make_double2(re, im);
+      cacc acc = cacc_zero();
+      for (int k = 0; k < n; ++k) cacc_fma(acc, M[i * n + k], M[k * n + j]);
+      M2[e] = cacc_finish(acc);
     }
     __syncthreads();
     for (int e = tid; e < n * n; e += blockDim.x) M[e] = M2[e];
     __syncthreads();
   }
   if (tid == 0) {
-    const double l2 = s_log2;             // log2 bound of lambda_max = ||A||_2^2
-    const double lnorm = 0.5 * l2;        // log2 bound of ||A||_2
-    log2_bound[blockIdx.x] = isfinite(lnorm) ? n * lnorm : -INFINITY;
-    scale_exp[blockIdx.x] = isfinite(lnorm) ? (int)ceil(lnorm) : 0;
+    const double l2 = s_log2;                 // log2 bound of lambda_max = ||A'||_2^2, A' = 2^-ea A
+    const double lnorm = 0.5 * l2 + ea;       // log2 bound of ||A||_2
+    log2_bound[blockIdx.x] = isfinite(l2) ? n * lnorm : -INFINITY;
+    scale_exp[blockIdx.x] = isfinite(l2) ? (int)ceil(lnorm) : 0;
   }
 }
 
