@@ -120,3 +120,24 @@ def test_slap_backend_api(native, oracle):
     with pytest.raises(AssertionError):
         b.prob_amplitude(FockState([0, 0, 0, 1, 1, 1]))
     assert not b.can_simulate_feed_forward([], inp)
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_slap_random_against_oracle(native, oracle, seed):
+    """Seeded random sizes (both walk endings: m >= 16 n and below) and inputs with
+    collisions: probabilities and amplitudes equal the oracle's SLOS at 1e-10."""
+    rng = np.random.default_rng(2000 + seed)
+    if seed % 2:  # few modes: the sibling-batch ending
+        n = int(rng.integers(1, 7))
+        m = int(rng.integers(2, 20))
+    else:  # many modes per photon: the one-node ending
+        n = int(rng.integers(1, 4))
+        m = int(rng.integers(16 * n, 16 * n + 20))
+    inp = np.zeros(m, dtype=np.int32)
+    for _ in range(n):
+        inp[rng.integers(0, m)] += 1
+    U = random_unitary(m, seed=seed)
+    Ud = torch.from_numpy(U).cuda()
+    rp, ra = oracle.slos(U, [int(v) for v in inp])
+    assert close(native.slap_all(Ud, inp).cpu().numpy(), rp)
+    assert close(native.slap_all(Ud, inp, amplitudes=True).cpu().numpy(), ra)

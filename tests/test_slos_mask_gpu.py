@@ -148,3 +148,39 @@ def test_backend_uses_masked_plans(native, oracle):
     assert len(sv) == len(sel)
     b.clear_mask()
     assert len(b.all_prob()) == len(rp)
+
+
+def _random_case(rng):
+    m = int(rng.integers(3, 11))
+    n = int(rng.integers(1, 6))
+    inp = np.zeros(m, dtype=int)
+    for _ in range(n):
+        inp[rng.integers(0, m)] += 1
+    nmask = int(rng.integers(1, 4))
+    masks = ["".join(rng.choice(list("**  00112"), size=m)) for _ in range(nmask)]
+    at_least = [int(i) for i in np.nonzero(rng.random(m) < 0.2)[0]]
+    mask_n = n + int(rng.integers(0, 2))
+    return m, tuple(int(v) for v in inp), masks, at_least, mask_n
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_masks_against_oracle(native, oracle, seed):
+    """Seeded random masks (digits 0..2, '*' and spaces, several strings, at-least modes,
+    a mask photon count of n or n + 1) on random inputs with collisions: the kept outputs
+    and their probabilities equal the oracle's full distribution restricted by
+    ``FSMask.accepts_space``."""
+    rng = np.random.default_rng(1000 + seed)
+    m, inp, masks, at_least, mask_n = _random_case(rng)
+    n = sum(inp)
+    mask = FSMask(m, mask_n, masks, at_least)
+    sel = kept_ranks(m, n, mask)
+    plan = native.SlosPlan(m, inp, mask=mask)
+    assert plan.count == len(sel)
+    if plan.count == 0:
+        return
+    assert np.array_equal(plan.output_ranks().astype(np.int64), sel)
+    U = random_unitary(m, seed=seed)
+    plan.forward(torch.from_numpy(U).cuda())
+    rp, ra = oracle.slos(U, list(inp))
+    assert close(plan.probabilities().cpu().numpy(), rp[sel])
+    assert close(plan.amplitudes().cpu().numpy(), ra[sel])
