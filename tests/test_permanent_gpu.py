@@ -117,3 +117,44 @@ def test_bad_arguments_raise(native):
                                np.array([41]), out)
     with pytest.raises(ValueError):
         native.permanent_batch(dev, np.array([0]), np.array([3]), out)
+
+
+@pytest.mark.parametrize("method", [0, 1])
+def test_permuted_diagonal_identity(native, method):
+    """perm(P D) = prod of the nonzeros: every Glynn / Ryser term has the same magnitude,
+    so the identity is checked at full precision up to n = 28."""
+    rng = np.random.default_rng(7 + method)
+    mats, refs = [], []
+    for n in (5, 13, 20, 24, 28):
+        d = np.exp(1j * rng.uniform(0, 2 * np.pi, n)) * rng.uniform(0.5, 1.5, n)
+        perm = rng.permutation(n)
+        a = np.zeros((n, n), complex)
+        a[np.arange(n), perm] = d
+        mats.append(a)
+        refs.append(np.prod(d))
+    got = gpu_perms(native, mats, method)
+    for g, r in zip(got, refs):
+        assert abs(g - r) <= RTOL * abs(r)
+
+
+def test_block_diagonal_identity(native, oracle):
+    """perm of a block-diagonal matrix = product of the blocks' permanents (n = 21 from
+    Haar blocks of 6, 7 and 8, and n = 16 from two blocks of 8, with the rows and columns
+    shuffled)."""
+    rng = np.random.default_rng(3)
+    mats, refs = [], []
+    for sizes in ((6, 7, 8), (8, 8)):
+        blocks = [haar_submatrices(1, s, s, seed=10 * s + i)[0] for i, s in enumerate(sizes)]
+        n = sum(sizes)
+        a = np.zeros((n, n), complex)
+        o = 0
+        for b in blocks:
+            a[o:o + b.shape[0], o:o + b.shape[0]] = b
+            o += b.shape[0]
+        a = a[rng.permutation(n)][:, rng.permutation(n)]
+        mats.append(np.ascontiguousarray(a))
+        flat, offs, sz = pack(blocks)
+        refs.append(np.prod(oracle.perm_batch(flat, offs, sz)))
+    got = gpu_perms(native, mats)
+    for g, r in zip(got, refs):
+        assert abs(g - r) <= RTOL * abs(r)
