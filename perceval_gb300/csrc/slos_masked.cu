@@ -92,16 +92,6 @@ __device__ void unrank_state(const MaskSpace& s, int k, uint64_t r, uint8_t* v) 
   v[s.m - 1] = (uint8_t)rem;
 }
 
-__device__ uint64_t rank_state(const MaskSpace& s, int k, const uint8_t* v) {
-  uint64_t r = 0;
-  int after = k;
-  for (int i = 0; i < s.m - 1; ++i) {
-    after -= v[i];
-    r += cnv(s, s.m - i, after - 1);
-  }
-  return r;
-}
-
 // Bit j set when the child p + e_j (j >= lo) of the (k-1)-photon state v is kept in layer k.
 __device__ uint32_t accepted_children(const MaskSpace& s, int k, const uint8_t* v, int lo) {
   uint32_t ok = 0;
