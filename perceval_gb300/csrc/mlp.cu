@@ -371,7 +371,6 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tma_kernel(const __grid_const
   } else if (warp == 1 && lane == 0 && nk > 0) {
     // MMA issuer
     const uint32_t idesc = umma_idesc();
-    int used = 0;
     for (int kt = 0; kt < nk; ++kt) {
       const int st = kt % kTmaStages;
       if (!mbar_wait(smem_u32(&full[st]), (kt / kTmaStages) & 1)) {
@@ -392,13 +391,11 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tma_kernel(const __grid_const
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                        smem_u32(&empty[st]))
                    : "memory");
-      used = kt + 1;
     }
     // completion of every MMA issued (a commit covers all earlier ones of this thread)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                      smem_u32(&done))
                  : "memory");
-    (void)used;
   }
   __syncwarp();
   bool ok = true;
