@@ -226,6 +226,17 @@ int pcvl_fock_mask_ranks(int32_t m, int32_t n, int32_t n_masks, const int8_t* di
 int pcvl_cc2017_sample(const double* u_d, int32_t m, const int32_t* input_state_h, int64_t count,
                        uint64_t seed, uint64_t first_sample, int32_t precision,
                        int32_t* out_counts_d, void* stream);
+/* Samples of several input states of one photon count in one wavefront (no reference
+ * counterpart as one call: it batches the per-input loop of SamplesProvider,
+ * perceval/simulators/noisy_sampling_simulator.py:68-69, 120-121, which calls
+ * set_input_state + samples(count) once per distinct input).  input_states_h: nstates x m
+ * (host), counts_h: nstates (host).  State b's samples are rows off_b .. off_b + counts_h[b] - 1
+ * of out_counts_d, off_b = counts of the states before it, and use the Philox counters of
+ * samples first_sample + off_b + j: identical to pcvl_cc2017_sample per state with
+ * first_sample + off_b. */
+int pcvl_cc2017_sample_multi(const double* u_d, int32_t m, int32_t nstates, const int32_t* input_states_h,
+                             const int64_t* counts_h, uint64_t seed, uint64_t first_sample, int32_t precision,
+                             int32_t* out_counts_d, void* stream);
 
 /* ------------------------------------------------------------------ learned proposal
  * No counterpart in the reference (its samplers have no learned part).  Kernels of

@@ -67,6 +67,9 @@ SYMBOLS = {
     "pcvl_cc2017_sample": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64,
                                           ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p,
                                           ctypes.c_void_p]),
+    "pcvl_cc2017_sample_multi": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                                ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int32,
+                                                ctypes.c_void_p, ctypes.c_void_p]),
     "pcvl_gemm_bf16": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int32] * 7 +
                        [ctypes.c_float, ctypes.c_float, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
@@ -476,10 +479,36 @@ def cc2017_sample(u: torch.Tensor, input_state, count: int, seed: int, first_sam
         raise ValueError("input_state must have m entries")
     if out is None:
         out = torch.empty((count, m), dtype=torch.int32, device="cuda")
+    if count == 0:
+        return out
     _dev_tensor(out, torch.int32, "out")
     check(lib.pcvl_cc2017_sample(u.data_ptr(), int(m), inp.ctypes.data, int(count), int(seed) & (2**64 - 1),
                                  int(first_sample), int(precision), out.data_ptr(), _stream_ptr(stream)),
           "pcvl_cc2017_sample")
+    return out
+
+
+def cc2017_sample_multi(u: torch.Tensor, input_states, counts, seed: int, first_sample: int = 0,
+                        precision: int = 0, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+    """Samples of several input states of one photon count in one wavefront
+    (``pcvl_cc2017_sample_multi``): int32 (sum(counts), m), state b's samples after those of
+    the states before it."""
+    lib = load()
+    _dev_tensor(u, torch.complex128, "u")
+    m = u.shape[-1]
+    states = np.ascontiguousarray(input_states, dtype=np.int32)
+    cnt = np.ascontiguousarray(counts, dtype=np.int64)
+    if states.ndim != 2 or states.shape[1] != m or states.shape[0] != cnt.shape[0] or states.shape[0] < 1:
+        raise ValueError("input_states must be (nstates x m) with one count per state")
+    total = int(cnt.sum())
+    if out is None:
+        out = torch.empty((total, m), dtype=torch.int32, device="cuda")
+    if total == 0:
+        return out
+    _dev_tensor(out, torch.int32, "out")
+    check(lib.pcvl_cc2017_sample_multi(u.data_ptr(), int(m), int(states.shape[0]), states.ctypes.data,
+                                       cnt.ctypes.data, int(seed) & (2**64 - 1), int(first_sample), int(precision),
+                                       out.data_ptr(), _stream_ptr(stream)), "pcvl_cc2017_sample_multi")
     return out
 
 

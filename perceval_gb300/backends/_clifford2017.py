@@ -53,3 +53,39 @@ class Clifford2017Backend(ASamplingBackend):
 
     def sample(self) -> FockState:
         return self.samples(1)[0]
+
+    def samples_many(self, input_states, counts) -> list[BSSamples]:
+        """``counts[b]`` samples of each input state ``input_states[b]`` through the current
+        circuit: the per-input loop of SamplesProvider (noisy_sampling_simulator.py:68-69,
+        120-121) as one wavefront per photon count.  The stream advances as for one
+        ``samples(sum(counts))`` call."""
+        states = [FockState(s) for s in input_states]
+        counts = [int(c) for c in counts]
+        assert len(states) == len(counts), "one count per input state"
+        m = self._umat.shape[0]
+        for st in states:
+            assert st.m == m, "Input state size mismatch"
+        seed, first = _random.take_samples(sum(counts))
+        res: list = [None] * len(states)
+        groups: dict[int, list[int]] = {}
+        for i, st in enumerate(states):
+            groups.setdefault(st.n, []).append(i)
+        offs = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+        U = self._unitary_device()
+        for n, idx in sorted(groups.items()):
+            # every state keeps the counters it holds in the whole request (offset offs[i])
+            arr = np.array([list(states[i]) for i in idx], dtype=np.int32)
+            grp_counts = [counts[i] for i in idx]
+            if idx == list(range(idx[0], idx[0] + len(idx))):
+                out = _native.cc2017_sample_multi(U, arr, grp_counts, seed, first + int(offs[idx[0]]),
+                                                  self._precision).cpu().numpy()
+                o = 0
+                for i, c in zip(idx, grp_counts):
+                    res[i] = BSSamples(FockState(row) for row in out[o:o + c])
+                    o += c
+            else:  # states of this count are not contiguous in the request: one call per state
+                for i in idx:
+                    out = _native.cc2017_sample(U, list(states[i]), counts[i], seed, first + int(offs[i]),
+                                                self._precision).cpu().numpy()
+                    res[i] = BSSamples(FockState(row) for row in out)
+        return res

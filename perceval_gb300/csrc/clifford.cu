@@ -328,7 +328,9 @@ struct CCDrawArgs {
   int64_t nsamp, s0;  // wavefront size and index of its first sample in the call
   uint64_t first;
   uint32_t k0, k1;
-  const int32_t* cols0;  // input columns (n, ascending)
+  const int32_t* cols0;      // input columns of every input state: [state][kMaxPhotons], ascending
+  const int64_t* state_off;  // first sample (call-relative) of every input state; nstates + 1 entries
+  int32_t nstates;
   int32_t* cols;
   int32_t* rows;
   const int32_t* cexp;
@@ -357,7 +359,18 @@ __global__ void __launch_bounds__(kDrawThreads) cc_draw_kernel(CCDrawArgs a) {
     int32_t* rows = a.rows + sl * kMaxPhotons;
     if (k == 1) {
       if (tid == 0) {
-        for (int l = 0; l < a.n; ++l) cols[l] = a.cols0[l];
+        // the input state of this sample: the last state starting at or before it
+        const int64_t g = a.s0 + sl;
+        int lo = 0, hi = a.nstates - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (a.state_off[mid] <= g)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        const int32_t* c0 = a.cols0 + (size_t)lo * kMaxPhotons;
+        for (int l = 0; l < a.n; ++l) cols[l] = c0[l];
         for (int q = a.n - 1; q >= 1; --q) {
           const u4 r = philox4x32_10({s_lo, s_hi, 0xffffffffu, (uint32_t)q}, a.k0, a.k1);
           const int j = (int)mulhi32(r.x, (uint32_t)(q + 1));
@@ -512,21 +525,36 @@ constexpr int64_t kWave = 32768;  // samples in flight
 
 using namespace pcvl;
 
-extern "C" int pcvl_cc2017_sample(const double* u_d, int32_t m, const int32_t* input_state_h, int64_t count,
-                                  uint64_t seed, uint64_t first_sample, int32_t precision, int32_t* out_counts_d,
-                                  void* stream_) {
-  cudaStream_t s = (cudaStream_t)stream_;
-  PCVL_CHECK(u_d && input_state_h && out_counts_d, "null pointer argument");
+// Samples of nstates input states of one photon count: state b's counts[b] samples
+// occupy rows off_b .. off_b + counts[b] - 1 of out_counts_d (off_b = counts of the states
+// before it) and use the Philox counters of samples first_sample + off_b + j.
+static int cc2017_run(const double* u_d, int32_t m, int32_t nstates, const int32_t* input_states_h,
+                      const int64_t* counts_h, uint64_t seed, uint64_t first_sample, int32_t precision,
+                      int32_t* out_counts_d, cudaStream_t s) {
+  PCVL_CHECK(u_d && input_states_h && counts_h && out_counts_d, "null pointer argument");
   PCVL_CHECK(m >= 1 && m <= 2048, "m=%d outside [1, 2048]", m);
-  PCVL_CHECK(count >= 0, "count must be >= 0");
+  PCVL_CHECK(nstates >= 1 && nstates <= (1 << 20), "nstates=%d outside [1, 2^20]", nstates);
   PCVL_CHECK(precision == 0 || precision == 1, "precision must be 0 (float-float) or 1 (FP32)");
-  std::vector<int32_t> cols;
-  for (int i = 0; i < m; ++i) {
-    PCVL_CHECK(input_state_h[i] >= 0, "negative photon count in input state");
-    for (int v = 0; v < input_state_h[i]; ++v) cols.push_back(i);
+  std::vector<int32_t> cols((size_t)nstates * kMaxPhotons, 0);
+  std::vector<int64_t> state_off(nstates + 1, 0);
+  int n = -1;
+  for (int b = 0; b < nstates; ++b) {
+    PCVL_CHECK(counts_h[b] >= 0, "count of input state %d is negative", b);
+    int nb = 0;
+    for (int i = 0; i < m; ++i) {
+      const int32_t v = input_states_h[(size_t)b * m + i];
+      PCVL_CHECK(v >= 0, "negative photon count in input state %d", b);
+      for (int t = 0; t < v; ++t) {
+        PCVL_CHECK(nb < kMaxPhotons, "input state %d has more than %d photons", b, kMaxPhotons);
+        cols[(size_t)b * kMaxPhotons + nb++] = i;
+      }
+    }
+    PCVL_CHECK(n < 0 || nb == n, "input state %d has %d photons, state 0 has %d: one call samples one photon count",
+               b, nb, n);
+    n = nb;
+    state_off[b + 1] = state_off[b] + counts_h[b];
   }
-  const int n = (int)cols.size();
-  PCVL_CHECK(n <= kMaxPhotons, "n=%d photons exceeds %d", n, kMaxPhotons);
+  const int64_t count = state_off[nstates];
   if (count == 0) return PCVL_OK;
   if (n == 0) {
     PCVL_CUDA(cudaMemsetAsync(out_counts_d, 0, (size_t)count * m * sizeof(int32_t), s));
@@ -544,7 +572,8 @@ extern "C" int pcvl_cc2017_sample(const double* u_d, int32_t m, const int32_t* i
 
   const size_t csz = precision == 0 ? sizeof(cdd) : sizeof(float2);
   const size_t o_cols0 = align_up((size_t)m * m * csz, 256);
-  const size_t o_cols = o_cols0 + 256;
+  const size_t o_soff = o_cols0 + align_up(cols.size() * sizeof(int32_t), 256);
+  const size_t o_cols = o_soff + align_up(state_off.size() * sizeof(int64_t), 256);
   const size_t st_bytes = align_up((size_t)W * kMaxPhotons * sizeof(int32_t), 256);
   const size_t o_rows = o_cols + st_bytes;
   const size_t o_cexp = o_rows + st_bytes;
@@ -553,7 +582,13 @@ extern "C" int pcvl_cc2017_sample(const double* u_d, int32_t m, const int32_t* i
   void* ws = nullptr;
   PCVL_TRY(workspace(WS_CC2017, total, &ws));
   unsigned char* base = (unsigned char*)ws;
-  PCVL_TRY(stage_h2d(cols.data(), cols.size() * sizeof(int32_t), base + o_cols0, s));
+  {
+    // one staged upload: the columns of every state, then the state offsets
+    std::vector<unsigned char> up(o_cols - o_cols0, 0);
+    std::memcpy(up.data(), cols.data(), cols.size() * sizeof(int32_t));
+    std::memcpy(up.data() + (o_soff - o_cols0), state_off.data(), state_off.size() * sizeof(int64_t));
+    PCVL_TRY(stage_h2d(up.data(), up.size(), base + o_cols0, s));
+  }
   const int cgrid = std::max(1, std::min(1024, (m * m + 255) / 256));
   if (precision == 0)
     cc_convert<ArDD><<<cgrid, 256, 0, s>>>((const double2*)u_d, m, (cdd*)base);
@@ -576,6 +611,8 @@ extern "C" int pcvl_cc2017_sample(const double* u_d, int32_t m, const int32_t* i
   da.k0 = (uint32_t)seed;
   da.k1 = (uint32_t)(seed >> 32);
   da.cols0 = (const int32_t*)(base + o_cols0);
+  da.state_off = (const int64_t*)(base + o_soff);
+  da.nstates = nstates;
   da.cols = (int32_t*)(base + o_cols);
   da.rows = (int32_t*)(base + o_rows);
   da.cexp = (const int32_t*)(base + o_cexp);
@@ -611,4 +648,19 @@ extern "C" int pcvl_cc2017_sample(const double* u_d, int32_t m, const int32_t* i
     }
   }
   return PCVL_OK;
+}
+
+extern "C" int pcvl_cc2017_sample(const double* u_d, int32_t m, const int32_t* input_state_h, int64_t count,
+                                  uint64_t seed, uint64_t first_sample, int32_t precision, int32_t* out_counts_d,
+                                  void* stream_) {
+  PCVL_CHECK(count >= 0, "count must be >= 0");
+  return cc2017_run(u_d, m, 1, input_state_h, &count, seed, first_sample, precision, out_counts_d,
+                    (cudaStream_t)stream_);
+}
+
+extern "C" int pcvl_cc2017_sample_multi(const double* u_d, int32_t m, int32_t nstates, const int32_t* input_states_h,
+                                        const int64_t* counts_h, uint64_t seed, uint64_t first_sample,
+                                        int32_t precision, int32_t* out_counts_d, void* stream_) {
+  return cc2017_run(u_d, m, nstates, input_states_h, counts_h, seed, first_sample, precision, out_counts_d,
+                    (cudaStream_t)stream_);
 }

@@ -90,3 +90,38 @@ def test_n26_marginals_and_precision_agreement(native, precision):
         ref = native.cc2017_sample(Ud, inp, N, seed=3, precision=0).cpu().numpy()
         agree = np.all(got == ref, axis=1).mean()
         assert agree >= 0.8, agree
+
+
+def test_many_input_states_in_one_wavefront(native):
+    """pcvl_cc2017_sample_multi: the samples of several input states of one photon count
+    (including a state with no samples) equal the single-state calls with the same Philox
+    counters, row for row; the backend's samples_many keeps request order across photon
+    counts."""
+    from perceval_gb300.backends import Clifford2017Backend
+    from perceval_gb300.utils import FockState, random_seed
+    m = 9
+    U = random_unitary(m, seed=21)
+    Ud = torch.from_numpy(U).cuda()
+    states = np.array([[1, 1, 0, 0, 1, 0, 0, 0, 0], [0, 2, 0, 0, 0, 0, 1, 0, 0], [0, 0, 0, 1, 1, 1, 0, 0, 0],
+                       [3, 0, 0, 0, 0, 0, 0, 0, 0]])
+    counts = [700, 0, 1300, 257]
+    got = native.cc2017_sample_multi(Ud, states, counts, seed=5, first_sample=11).cpu().numpy()
+    off = 11
+    row = 0
+    for st, c in zip(states, counts):
+        ref = native.cc2017_sample(Ud, st, c, seed=5, first_sample=off).cpu().numpy()
+        assert np.array_equal(got[row:row + c], ref)
+        off += c
+        row += c
+    b = Clifford2017Backend()
+    b.set_circuit(U)
+    reqs = [FockState([1, 1, 0, 0, 0, 0, 0, 0, 0]), FockState([0, 0, 0, 0, 0, 0, 0, 0, 1]),
+            FockState([0, 0, 1, 0, 0, 0, 0, 1, 0])]
+    random_seed(9)
+    many = b.samples_many(reqs, [40, 30, 20])
+    random_seed(9)
+    b.set_input_state(reqs[0])
+    first = b.samples(40)
+    assert [tuple(s) for s in many[0]] == [tuple(s) for s in first]
+    assert len(many[1]) == 30 and all(s.n == 1 for s in many[1])
+    assert len(many[2]) == 20 and all(s.n == 2 for s in many[2])
