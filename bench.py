@@ -523,6 +523,24 @@ def secondary(torch, _native, random_unitary, dev, flush):
     cnt = 20000
     t_cc = timed(lambda: _native.cc2017_sample(U4, [1] * 20 + [0] * 380, cnt, seed=1), reps=1)
     res["cc2017_n20_m400"] = {"samples_per_s": cnt / (t_cc * 1e-3), "samples": cnt, "precision": "float-float"}
+    # many input states (the per-input loop of a samples provider): 64 distinct 6-photon inputs
+    # on m = 64, 1000 samples each, one wavefront against one call per input
+    rng = np.random.default_rng(5)
+    U64 = torch.from_numpy(random_unitary(64, seed=1)).to(dev)
+    states = np.zeros((64, 64), dtype=np.int32)
+    for b in range(64):
+        states[b, rng.choice(64, 6, replace=False)] = 1
+    per = [1000] * 64
+    t_many = timed(lambda: _native.cc2017_sample_multi(U64, states, per, seed=3), reps=2)
+
+    def loop():
+        off = 0
+        for b in range(64):
+            _native.cc2017_sample(U64, states[b], per[b], seed=3, first_sample=off)
+            off += per[b]
+    t_loop = timed(loop, reps=2)
+    res["cc2017_64_inputs_m64_n6"] = {"samples": 64000, "one_wavefront_ms": t_many, "per_input_loop_ms": t_loop,
+                                      "samples_per_s": 64000 / (t_many * 1e-3)}
     # small case: SLOS m=12, n=6 and 1000 Naive amplitudes (latency-bound)
     from perceval_gb300 import BackendFactory, BasicState
     U12 = random_unitary(12, seed=0)
