@@ -6,7 +6,7 @@ warning and falls back to SLOS, as in the reference.
 """
 import logging
 
-from ._abstract_backends import ABackend, ASamplingBackend, AStrongSimulationBackend
+from ._abstract_backends import ABackend, ASamplingBackend, AStrongSimulationBackend, IFFBackend
 from ._clifford2017 import Clifford2017Backend
 from ._naive import NaiveBackend
 from ._naive_approx import NaiveApproxBackend
@@ -36,5 +36,5 @@ class BackendFactory:
         return list(BACKEND_LIST.keys())
 
 
-__all__ = ["ABackend", "ASamplingBackend", "AStrongSimulationBackend", "BACKEND_LIST", "BackendFactory",
+__all__ = ["ABackend", "ASamplingBackend", "AStrongSimulationBackend", "BACKEND_LIST", "BackendFactory", "IFFBackend",
            "Clifford2017Backend", "NaiveApproxBackend", "NaiveBackend", "SLAPBackend", "SLOSBackend"]

@@ -160,3 +160,18 @@ class AStrongSimulationBackend(ABackend):
         for s in self._get_iterator(self._input_state):
             res[s] = complex(self.prob_amplitude(s))
         return res
+
+
+class IFFBackend(ABC):
+    """Backends that can simulate feed-forward configurators themselves
+    (perceval/backends/_abstract_backends.py:211-236); the feed-forward simulator asks
+    ``can_simulate_feed_forward`` before handing them the components."""
+
+    @staticmethod
+    @abstractmethod
+    def can_simulate_feed_forward(components, input_state, detectors=None) -> bool:
+        """True when the backend's output for these components and input is correct."""
+
+    @abstractmethod
+    def set_feed_forward(self, components, m: int) -> None:
+        """Sets the components (with at least one configurator) in place of a circuit."""

@@ -82,6 +82,12 @@ class NaiveBackend(AStrongSimulationBackend):
         res[idx] = perms / norms
         return res
 
+    def _compute_permanent(self, M: np.ndarray) -> complex:
+        """Permanent of one square matrix (_naive.py:70-71), through the batched call."""
+        M = np.ascontiguousarray(M, dtype=np.complex128)
+        n = M.shape[0]
+        return complex(self._permanents(M.reshape(-1), np.zeros(1, dtype=np.int64), np.array([n], np.int32))[0])
+
     def _permanents(self, flat: np.ndarray, offs: np.ndarray, sizes: np.ndarray) -> np.ndarray:
         """Permanents of packed matrices, one batched launch (_naive.py:70-71)."""
         dev = torch.from_numpy(flat).to("cuda")

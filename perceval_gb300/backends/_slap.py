@@ -18,12 +18,12 @@ import torch
 
 from .. import _native
 from ..utils.states import BSDistribution, FockState, StateVector, fock_rank, fock_unrank_array
-from ._abstract_backends import AStrongSimulationBackend
+from ._abstract_backends import AStrongSimulationBackend, IFFBackend
 
 _LIST_LIMIT = 1 << 22
 
 
-class SLAPBackend(AStrongSimulationBackend):
+class SLAPBackend(AStrongSimulationBackend, IFFBackend):
     def __init__(self, mask=None):
         super().__init__()
         self._u_dev: torch.Tensor | None = None

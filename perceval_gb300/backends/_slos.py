@@ -90,14 +90,24 @@ class SLOSBackend(AStrongSimulationBackend):
         super().set_input_state(input_state)
         self._entry()
 
+    def preprocess(self, input_list) -> bool:
+        """Plans for the input states of ``input_list`` that have none yet (_slos.py:171-185);
+        True when at least one was new.  Their coefficients are computed on first use."""
+        found_new = False
+        for st in input_list:
+            st = FockState(st)
+            if st not in self._entries:
+                e = _Entry(_native.SlosPlan(st.m, list(st), batch=1, keep_layers=False, mask=self._mask))
+                if self._mask is not None:
+                    e.ranks = e.plan.output_ranks()
+                self._entries[st] = e
+                found_new = True
+        return found_new
+
     def _entry(self) -> _Entry:
         st = self._input_state
-        e = self._entries.get(st)
-        if e is None:
-            e = _Entry(_native.SlosPlan(st.m, list(st), batch=1, keep_layers=False, mask=self._mask))
-            if self._mask is not None:
-                e.ranks = e.plan.output_ranks()
-            self._entries[st] = e
+        self.preprocess([st])
+        e = self._entries[st]
         if not e.fresh:
             e.probs = e.amps = e.amps_host = None
             e.layer_ok = False

@@ -142,3 +142,24 @@ def test_clifford_bs_kat(native, kats):
     for o in case["outcomes"]:
         assert case["band"][0] * case["samples"] < counts[BasicState(o)] < case["band"][1] * case["samples"]
     assert isinstance(b.sample(), BasicState)
+
+
+def test_api_surface_helpers(native, oracle):
+    """preprocess (plans ahead, True when new), _compute_permanent (one matrix, through the
+    batch call; NaiveApprox's is the estimate), IFFBackend on SLAP."""
+    from perceval_gb300.backends import IFFBackend, NaiveApproxBackend, NaiveBackend, SLAPBackend, SLOSBackend
+    from perceval_gb300.utils.matrix import random_unitary
+    U = random_unitary(5, seed=3)
+    b = SLOSBackend()
+    b.set_circuit(U)
+    assert b.preprocess([BasicState([1, 1, 0, 0, 0]), BasicState([0, 1, 0, 1, 0])]) is True
+    assert b.preprocess([BasicState([1, 1, 0, 0, 0])]) is False
+    b.set_input_state(BasicState([0, 1, 0, 1, 0]))
+    rp, _ = oracle.slos(U, [0, 1, 0, 1, 0])
+    assert np.allclose(b.all_prob(), rp, atol=1e-12)
+    M = random_unitary(8, seed=1)[:6, :6]
+    ref = oracle.perm_batch(M.reshape(-1).copy(), np.array([0]), np.array([6]))[0]
+    assert abs(NaiveBackend()._compute_permanent(M) - ref) <= 1e-10 * abs(ref)
+    est = NaiveApproxBackend(gurvits_iterations=200000)._compute_permanent(M)
+    assert abs(est - ref) <= 0.05 * np.linalg.norm(M, 2) ** 6
+    assert isinstance(SLAPBackend(), IFFBackend) and not isinstance(SLOSBackend(), IFFBackend)
