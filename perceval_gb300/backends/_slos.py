@@ -9,8 +9,11 @@ recomputes their coefficients (_slos.py:130-141); a different size resets them.
 Outputs come back in descending-lexicographic order (the reference's
 ``allstate_iterator`` order).  With a mask (``set_mask``) the plans are masked plans:
 every layer holds only the states the mask can still accept (xq.FSArray(m, k, mask),
-_slos.py:161-164), and the outputs are the accepted states in the same order.  ``all_prob`` returns a list up to 2^22 outputs and a
-numpy array above; ``all_prob_tensor`` leaves the probabilities on the device.
+_slos.py:161-164), and the outputs are the accepted states in the same order.
+``all_prob`` returns a list up to 2^22 outputs and a numpy array above;
+``all_prob_tensor`` leaves the probabilities on the device.  Circuits wider than the
+32 modes of SLOS plans take the SLAP walk (``pcvl_slap_*``), which computes the same
+amplitudes, with the mask's outputs selected on the device.
 
 ``all_probs_many`` / ``prob_distributions`` evaluate many input states of the circuit
 at once (the per-input loop of Simulator._probs_svd_fast, simulator.py:454-468): states
@@ -30,12 +33,14 @@ from ..utils.states import BSDistribution, FSMask, FockState, StateVector, fock_
 from ._abstract_backends import AStrongSimulationBackend, _as_circuit
 
 _LIST_LIMIT = 1 << 22
+_PLAN_MAX_M = 32  # SLOS plans address modes with 32-bit masks; wider circuits take the SLAP walk
 
 
 class _Entry:
-    """Plan and cached results of one input state."""
+    """Plan and cached results of one input state (plan None: more than 32 modes, the
+    outputs come from the SLAP walk, which gives the same amplitudes)."""
 
-    def __init__(self, plan: _native.SlosPlan):
+    def __init__(self, plan: _native.SlosPlan | None):
         self.plan = plan
         self.fresh = False           # cached results belong to the current unitary
         self.layer_ok = False        # the plan's last layer holds this unitary's coefficients
@@ -61,7 +66,8 @@ class SLOSBackend(AStrongSimulationBackend):
 
     def _reset(self):
         for e in self._entries.values():
-            e.plan.close()
+            if e.plan is not None:
+                e.plan.close()
         self._entries = {}
         self.clear_iterator_cache()
 
@@ -97,9 +103,14 @@ class SLOSBackend(AStrongSimulationBackend):
         for st in input_list:
             st = FockState(st)
             if st not in self._entries:
-                e = _Entry(_native.SlosPlan(st.m, list(st), batch=1, keep_layers=False, mask=self._mask))
-                if self._mask is not None:
-                    e.ranks = e.plan.output_ranks()
+                if st.m > _PLAN_MAX_M:
+                    e = _Entry(None)
+                    if self._mask is not None:
+                        e.ranks = _native.fock_mask_ranks(st.m, st.n, self._mask).cpu().numpy().astype(np.uint64)
+                else:
+                    e = _Entry(_native.SlosPlan(st.m, list(st), batch=1, keep_layers=False, mask=self._mask))
+                    if self._mask is not None:
+                        e.ranks = e.plan.output_ranks()
                 self._entries[st] = e
                 found_new = True
         return found_new
@@ -122,8 +133,11 @@ class SLOSBackend(AStrongSimulationBackend):
             self.set_input_state(input_state)
         e = self._entry()
         if e.probs is None:
-            # probabilities alone: the last layer writes them directly (not stored)
-            e.probs = e.plan.probabilities() if e.layer_ok else e.plan.forward_probabilities(self._unitary_device())
+            if e.plan is None:
+                e.probs = self._slap(e, amplitudes=False)
+            else:
+                # probabilities alone: the last layer writes them directly (not stored)
+                e.probs = e.plan.probabilities() if e.layer_ok else e.plan.forward_probabilities(self._unitary_device())
         return e.probs
 
     def amplitudes_tensor(self) -> torch.Tensor:
@@ -131,11 +145,21 @@ class SLOSBackend(AStrongSimulationBackend):
         CUDA tensor, in descending-lexicographic order."""
         e = self._entry()
         if e.amps is None:
-            if not e.layer_ok:
-                e.plan.forward(self._unitary_device())
-                e.layer_ok = True
-            e.amps = e.plan.amplitudes()
+            if e.plan is None:
+                e.amps = self._slap(e, amplitudes=True)
+            else:
+                if not e.layer_ok:
+                    e.plan.forward(self._unitary_device())
+                    e.layer_ok = True
+                e.amps = e.plan.amplitudes()
         return e.amps
+
+    def _slap(self, e: _Entry, amplitudes: bool) -> torch.Tensor:
+        """Outputs of a circuit wider than SLOS plans, by the SLAP walk (mask applied)."""
+        full = _native.slap_all(self._unitary_device(), list(self._input_state), amplitudes=amplitudes)
+        if e.ranks is None:
+            return full
+        return full[torch.from_numpy(e.ranks.astype(np.int64)).to(full.device)]
 
     def _get_iterator(self, input_state):
         # under a mask, the accepted outputs are the plan's own (no full-space enumeration)
@@ -164,6 +188,14 @@ class SLOSBackend(AStrongSimulationBackend):
             groups.setdefault(s.n, []).append(i)
         U = self._unitary_device()
         res: list = [None] * len(states)
+        if m > _PLAN_MAX_M:  # wider than SLOS plans: the SLAP walk per input state
+            for n, idxs in groups.items():
+                mask = self._group_mask(m, n)
+                sel = None if mask is None else _native.fock_mask_ranks(m, n, mask)
+                for i in idxs:
+                    p = _native.slap_all(U, list(states[i]))
+                    res[i] = (p if sel is None else p[sel]).cpu().numpy()
+            return res
         for n, idxs in sorted(groups.items()):
             count = math.comb(m + n - 1, n)
             # two float-float layers per entry dominate a plan's memory
@@ -218,7 +250,9 @@ class SLOSBackend(AStrongSimulationBackend):
             pos = int(np.searchsorted(e.ranks, np.uint64(r)))
             assert pos < len(e.ranks) and int(e.ranks[pos]) == r, "output state is not accepted by the mask"
             r = pos
-        if e.plan.count <= _LIST_LIMIT:
+        count = e.plan.count if e.plan is not None else (
+            len(e.ranks) if e.ranks is not None else _native.slap_output_count(output_state.m, list(self._input_state)))
+        if count <= _LIST_LIMIT:
             if e.amps_host is None:
                 e.amps_host = self.amplitudes_tensor().cpu().numpy()
             return complex(e.amps_host[r])

@@ -163,3 +163,30 @@ def test_api_surface_helpers(native, oracle):
     est = NaiveApproxBackend(gurvits_iterations=200000)._compute_permanent(M)
     assert abs(est - ref) <= 0.05 * np.linalg.norm(M, 2) ** 6
     assert isinstance(SLAPBackend(), IFFBackend) and not isinstance(SLOSBackend(), IFFBackend)
+
+
+def test_slos_backend_beyond_32_modes(native, oracle):
+    """A 40-mode circuit on the SLOS backend (wider than SLOS plans): probabilities,
+    amplitudes, a masked distribution and many inputs come from the SLAP walk and equal
+    the oracle's SLOS."""
+    from perceval_gb300.backends import SLOSBackend
+    from perceval_gb300.utils import FSMask
+    from perceval_gb300.utils.matrix import random_unitary
+    from perceval_gb300.utils.states import fock_space_array
+    m = 40
+    U = random_unitary(m, seed=12)
+    inp = BasicState([1, 0, 1, 0, 1] + [0] * 35)
+    rp, ra = oracle.slos(U, list(inp))
+    b = SLOSBackend()
+    b.set_circuit(U)
+    b.set_input_state(inp)
+    assert np.abs(np.array(b.all_prob()) - rp).max() <= 1e-10 * rp.max()
+    out = BasicState([0] * 37 + [1, 1, 1])
+    idx = [tuple(r) for r in fock_space_array(m, 3)].index(tuple(out))
+    assert abs(b.prob_amplitude(out) - ra[idx]) <= 1e-10 * np.abs(ra).max()
+    many = b.all_probs_many([inp, BasicState([0, 2, 0, 0, 1] + [0] * 35)])
+    assert np.abs(many[0] - rp).max() <= 1e-10 * rp.max()
+    b.set_mask(["*" * 38 + "00"])
+    sel = np.nonzero(FSMask(m, 3, ["*" * 38 + "00"]).accepts_space(fock_space_array(m, 3)))[0]
+    assert np.abs(np.array(b.all_prob()) - rp[sel]).max() <= 1e-10 * rp.max()
+    assert len(b.prob_distribution()) == len(sel)
