@@ -105,14 +105,16 @@ def test_many_input_states_in_one_wavefront(native):
     states = np.array([[1, 1, 0, 0, 1, 0, 0, 0, 0], [0, 2, 0, 0, 0, 0, 1, 0, 0], [0, 0, 0, 1, 1, 1, 0, 0, 0],
                        [3, 0, 0, 0, 0, 0, 0, 0, 0]])
     counts = [700, 0, 1300, 257]
-    got = native.cc2017_sample_multi(Ud, states, counts, seed=5, first_sample=11).cpu().numpy()
-    off = 11
-    row = 0
-    for st, c in zip(states, counts):
-        ref = native.cc2017_sample(Ud, st, c, seed=5, first_sample=off).cpu().numpy()
-        assert np.array_equal(got[row:row + c], ref)
-        off += c
-        row += c
+    for precision in (0, 1):
+        got = native.cc2017_sample_multi(Ud, states, counts, seed=5, first_sample=11,
+                                         precision=precision).cpu().numpy()
+        off = 11
+        row = 0
+        for st, c in zip(states, counts):
+            ref = native.cc2017_sample(Ud, st, c, seed=5, first_sample=off, precision=precision).cpu().numpy()
+            assert np.array_equal(got[row:row + c], ref)
+            off += c
+            row += c
     b = Clifford2017Backend()
     b.set_circuit(U)
     reqs = [FockState([1, 1, 0, 0, 0, 0, 0, 0, 0]), FockState([0, 0, 0, 0, 0, 0, 0, 0, 1]),
