@@ -594,6 +594,60 @@ def secondary(torch, _native, random_unitary, dev, flush):
     t_loop = time.perf_counter() - t0
     res["slos_500_inputs_m12_n6"] = {"batched_ms": t_many * 1e3, "per_input_loop_ms": t_loop * 1e3,
                                      "max_abs_diff": dev_max}
+    # a noisy source through Simulator.probs_svd: |1,1,1,1,1,1,0,...> on m = 12, each photon
+    # lost (0.1), indistinguishable (0.8) or distinguishable (0.1): 729 separable inputs,
+    # distinct parts simulated in batched plans, against the same simulator taking one
+    # plan per distinct part (the reference's loop)
+    from perceval_gb300.simulators import Simulator
+
+    noisy = {}
+    for code in range(3 ** 6):
+        p, same, parts, c = 1.0, [0] * 12, [], code
+        for ph in range(6):
+            kind, c = c % 3, c // 3
+            p *= (0.1, 0.8, 0.1)[kind]
+            if kind == 1:
+                same[ph] = 1
+            elif kind == 2:
+                solo = [0] * 12
+                solo[ph] = 1
+                parts.append(BasicState(solo))
+        noisy[tuple([BasicState(same)] + parts)] = p
+
+    class _PerInput:
+        """The SLOS backend without its batched entry point."""
+
+        def __init__(self, be):
+            self._be, self._masks_str = be, None
+
+        def set_input_state(self, s):
+            self._be.set_input_state(s)
+
+        def prob_iterator(self, min_p):
+            return self._be.prob_iterator(min_p)
+
+        def prob_distribution(self):
+            return self._be.prob_distribution()
+
+    sim_b = Simulator(BackendFactory.get_backend("SLOS"))
+    sim_b.set_circuit(U12)
+    sim_b.probs_svd(dict(list(noisy.items())[:8]))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out_b = sim_b.probs_svd(noisy)
+    t_svd = time.perf_counter() - t0
+    be_l = BackendFactory.get_backend("SLOS")
+    be_l.set_circuit(U12)
+    sim_l = Simulator(_PerInput(be_l))
+    t0 = time.perf_counter()
+    out_l = sim_l.probs_svd(noisy)
+    t_svd_loop = time.perf_counter() - t0
+    n_parts = len({s for key in noisy for s in key})
+    res["probs_svd_noisy_m12_n6"] = {
+        "inputs": len(noisy), "distinct_parts": n_parts, "outputs": len(out_b["results"]),
+        "batched_ms": t_svd * 1e3, "per_part_loop_ms": t_svd_loop * 1e3,
+        "max_abs_diff": max(abs(out_b["results"][k] - out_l["results"].get(k, 0.0)) for k in out_b["results"]),
+        "logical_perf": out_b["logical_perf"]}
     # launch latency of a small batch (1000 permanents of 6x6 Haar submatrices): the
     # plan-free call against one graph launch of a plan, wall clock per call
     sub = np.stack([U12[np.ix_(rng.choice(12, 6, replace=False), rng.choice(12, 6, replace=False))]

@@ -18,6 +18,7 @@ occupation vector within a fixed photon number
 """
 from __future__ import annotations
 
+import functools
 import math
 import re
 from typing import Iterable, Iterator, Sequence
@@ -44,6 +45,11 @@ class FockState(tuple):
         if any(v < 0 for v in vals):
             raise ValueError("photon counts must be non-negative")
         return super().__new__(cls, vals)
+
+    @classmethod
+    def _trusted(cls, counts: tuple) -> "FockState":
+        """A state from a tuple of non-negative Python ints, without checks."""
+        return tuple.__new__(cls, counts)
 
     @property
     def m(self) -> int:
@@ -251,6 +257,30 @@ def fock_rank(state: Sequence[int]) -> int:
         if rest > 0:
             rank += fock_space_size(m - i, rest - 1)
     return rank
+
+
+@functools.lru_cache(maxsize=64)
+def _rank_sizes(m: int, n: int) -> np.ndarray:
+    """size[M, x] = count(M, x - 1), the states of x - 1 photons on M modes (0 for x = 0)."""
+    size = np.zeros((m + 1, n + 1), dtype=np.int64)
+    for M in range(1, m + 1):
+        for x in range(1, n + 1):
+            size[M, x] = fock_space_size(M, x - 1)
+    size.setflags(write=False)
+    return size
+
+
+def fock_rank_array(arr) -> np.ndarray:
+    """Ranks (int64) of the occupation vectors in the rows of ``arr``, all of one photon
+    count; vectorised ``fock_rank``."""
+    arr = np.asarray(arr, dtype=np.int64)
+    if arr.ndim != 2 or arr.shape[0] == 0:
+        return np.zeros(arr.shape[0] if arr.ndim == 2 else 0, dtype=np.int64)
+    k, m = arr.shape
+    n = int(arr[0].sum())
+    size = _rank_sizes(m, n)
+    rest = n - np.cumsum(arr, axis=1)  # photons after each mode
+    return size[np.arange(m, 0, -1)[None, :], rest].sum(axis=1)
 
 
 def fock_unrank(m: int, n: int, rank: int) -> FockState:

@@ -75,6 +75,10 @@ def test_mask_layers_and_device_spec():
     arr = fock_unrank_array(7, 4, ranks)
     assert [fock_rank(list(s)) for s in arr] == ranks.tolist()
     assert np.array_equal(fock_unrank_array(7, 4, np.arange(210)), fock_space_array(7, 4))
+    from perceval_gb300.utils.states import fock_rank_array
+    for m, n in [(1, 0), (1, 3), (4, 0), (7, 4), (12, 6)]:
+        assert np.array_equal(fock_rank_array(fock_space_array(m, n)), np.arange(math.comb(m + n - 1, n)))
+    assert fock_rank_array(arr).tolist() == ranks.tolist()
 
 
 def test_bsdistribution_and_counts():
