@@ -50,14 +50,11 @@ def _parts(key) -> tuple[FockState, ...]:
 
 
 def _input_items(input_dist) -> list[tuple[tuple[FockState, ...], float]]:
-    """(parts, probability) of every distinct input of a mapping or of (key, probability)
-    pairs; repeated inputs add up."""
+    """(parts, probability) of every input of a mapping (one entry per key, like an
+    SVDistribution) or of an iterable of (key, probability) pairs, kept entry by entry as
+    _probs_svd_fast takes its (states, prob) list (simulator.py:430-431)."""
     items = input_dist.items() if hasattr(input_dist, "items") else input_dist
-    acc: dict[tuple[FockState, ...], float] = {}
-    for key, p in items:
-        parts = _parts(key)
-        acc[parts] = acc.get(parts, 0.0) + float(p)
-    return list(acc.items())
+    return [(_parts(key), float(p)) for key, p in items]
 
 
 class Simulator:

@@ -138,9 +138,10 @@ def same_dist(got, ref, rtol):
 @pytest.mark.parametrize("batched", [True, False])
 @pytest.mark.parametrize("seed", range(4))
 def test_probs_svd_host_logic(oracle, batched, seed):
-    m = 6
+    m = 8
     U = random_unitary(m, seed=seed)
-    items = mixture(m, seed, 12)
+    items = mixture(m, 100 + seed, 40)  # holds repeated inputs, kept entry by entry
+    assert len({k for k, _ in items}) < len(items)
     be = FakeStrong(oracle, U, batched)
     sim = Simulator(be)
     sim.set_min_detected_photons_filter(2 if seed % 2 else 0)
