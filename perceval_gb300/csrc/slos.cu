@@ -405,11 +405,22 @@ __global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a, double* __restri
       const uint32_t tb = ws[MMAX + 1];
       const uint32_t* row = rows + (size_t)tau * a.t - p;
       cacc acc = cacc_zero();
+      // two occupied modes per iteration: both parent gathers are in flight before the
+      // first multiply-add (the accumulation order, and so the result, is unchanged)
       while (occ) {
         const int j = __ffs(occ) - 1;
         occ &= occ - 1;
         const uint32_t ad = j < p ? ws[j] + tau : tb + __ldg(&row[j]);
-        cacc_fma(acc, ld_cdd(&a.in[ad]), u[j]);
+        if (occ) {
+          const int j2 = __ffs(occ) - 1;
+          occ &= occ - 1;
+          const uint32_t ad2 = j2 < p ? ws[j2] + tau : tb + __ldg(&row[j2]);
+          const cdd v = ld_cdd(&a.in[ad]), v2 = ld_cdd(&a.in[ad2]);
+          cacc_fma(acc, v, u[j]);
+          cacc_fma(acc, v2, u[j2]);
+        } else {
+          cacc_fma(acc, ld_cdd(&a.in[ad]), u[j]);
+        }
       }
       if (PROB) {
         const dd fg = {__uint_as_float(ws[MMAX + 3]), __uint_as_float(ws[MMAX + 4])};
