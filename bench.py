@@ -254,8 +254,10 @@ def run_ours(args):
     from perceval_gb300.utils.matrix import random_unitary
     _native.load()
     dev = torch.device("cuda")
-    out_dir = ROOT / "gpurun_out"
-    out_dir.mkdir(exist_ok=True)
+    # the nvidia-smi clock samples of the timed region are logged here (the JSON line carries
+    # their summary)
+    out_dir = Path(os.environ.get("PCVL_BENCH_OUT", str(ROOT / "bench_out")))
+    out_dir.mkdir(parents=True, exist_ok=True)
     # launch shapes of the permanent bins: the cached autotuner table for this GPU, or a
     # fresh tuning run (about 20 s, untimed) that is then cached
     t_tune = time.perf_counter()
@@ -692,7 +694,7 @@ def run_learned(args):
     n = 30, m = 900 (Haar seed 0, input modes 0..29), plus the n = 8, m = 64 companion.
 
     Training data: exact Clifford & Clifford samples drawn by this library's sampler in
-    its FP32 mode (the float-float mode is the judged baseline).  ESS: Geyer's initial
+    its FP32 mode (the float-float mode is the baseline it is compared with).  ESS: Geyer's initial
     positive sequence estimator on each chain's log pi trace, summed over chains; the
     exact sampler's samples are independent (ESS = N).  Marginals: sample means of n_i
     and n_i n_j against the closed forms."""

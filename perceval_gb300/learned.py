@@ -1,7 +1,7 @@
 """Learned-proposal Metropolised independence sampler for boson sampling.
 
 There is no counterpart in the reference; its exact sampler (Clifford & Clifford,
-perceval/backends/_clifford2017.py) is both the fallback and the judge here.
+perceval/backends/_clifford2017.py) is both the fallback and the point of comparison here.
 
 Target.  For n photons in input modes ``in`` and a unitary U, an output *sequence*
 r = (r_1..r_n) of modes (one per photon, order kept) gets
