@@ -38,6 +38,9 @@ from .utils.states import (BSCount, BSDistribution, BSSamples, FockState, fock_r
 
 __all__ = ["Simulator", "SamplesProvider"]
 
+# outputs whose m per-mode counts fit in this many bits are merged as packed integer keys
+_PACKED_BITS = 64
+
 
 def _parts(key) -> tuple[FockState, ...]:
     """Separated parts of an input key: a Fock state, or a sequence of Fock states."""
@@ -146,6 +149,57 @@ class Simulator:
             p = prod[i, j]
         return (fock_rank_array(cur) if len(cur) else np.zeros(0, dtype=np.int64)), p
 
+    @staticmethod
+    def _merge_keys(parts, cache, keys_cache: dict, shifts: np.ndarray, threshold: float):
+        """``_merge`` on packed outputs: a state is one uint64 key (per-mode counts in digits
+        of fixed width, mode 0 highest), so merged photon counts are sums of keys.  Returns
+        (keys of the merged outputs, probabilities)."""
+
+        def keys(s):
+            if s not in keys_cache:
+                rows = fock_unrank_array(s.m, s.n, cache[s][0]).astype(np.uint64)
+                keys_cache[s] = (rows << shifts).sum(axis=1, dtype=np.uint64)
+            return keys_cache[s]
+
+        p = cache[parts[0]][1]
+        keep = p >= threshold
+        k, p = keys(parts[0])[keep], p[keep]
+        for s in parts[1:]:
+            prod = p[:, None] * cache[s][1][None, :]
+            i, j = np.nonzero(prod >= threshold)
+            k = k[i] + keys(s)[j]
+            p = prod[i, j]
+        return k, p
+
+    def _recombine_packed(self, decomposed, cache, p_threshold: float, m: int, bits: int) -> BSDistribution:
+        """Recombination on packed keys: each input's merged outputs summed per state in the
+        recursion's order, then every input's weighted sums added per state in input order
+        (one ``bincount`` over all of them), as the reference's dict accumulates them."""
+        shifts = (bits * np.arange(m - 1, -1, -1)).astype(np.uint64)
+        keys_cache: dict = {}
+        all_k, all_w = [], []
+        for prob0, parts, _ in decomposed:
+            k, p = self._merge_keys(parts, cache, keys_cache, shifts, p_threshold / (10 * prob0))
+            self.DEBUG_merge_count += len(parts) - 1
+            if len(parts) == 1:  # distinct outputs already
+                out, within = k, p
+            else:
+                out, inv = np.unique(k, return_inverse=True)
+                within = np.bincount(inv, weights=p, minlength=len(out))
+            self._logical_perf += float(within.sum()) * prob0
+            all_k.append(out)
+            all_w.append(within * prob0)
+        res = BSDistribution()
+        K = np.concatenate(all_k) if all_k else np.zeros(0, dtype=np.uint64)
+        if len(K):
+            uk, inv = np.unique(K, return_inverse=True)
+            acc = np.bincount(inv, weights=np.concatenate(all_w), minlength=len(uk))
+            rows = (uk[:, None] >> shifts) & np.uint64((1 << bits) - 1)
+            order = np.lexsort((~uk, rows.sum(axis=1)))  # by photon count, then descending-lex
+            for row, v in zip(rows[order].astype(np.int64).tolist(), acc[order].tolist()):
+                dict.__setitem__(res, FockState._trusted(tuple(row)), v)
+        return res
+
     def probs_svd(self, input_dist, progress_callback: Callable | None = None) -> dict:
         """Output distribution of a mixture of inputs and its performances.
 
@@ -202,8 +256,17 @@ class Simulator:
         if progress_callback is not None:
             progress_callback(0.5, "compute probability distributions")
 
-        # recombination, accumulated densely per photon count by output rank
         m = decomposed[0][1][0].m
+        bits = max(1, max(n for _, _, n in decomposed).bit_length())
+        if m * bits <= _PACKED_BITS:
+            res = self._recombine_packed(decomposed, cache, p_threshold, m, bits)
+            if progress_callback is not None:
+                progress_callback(1.0, "recombine distributions")
+            if len(res):
+                res.normalize()
+            return res
+
+        # wider states: recombination accumulated densely per photon count by output rank
         acc: dict[int, np.ndarray] = {}
         touched: dict[int, np.ndarray] = {}
         rows_cache: dict = {}

@@ -135,9 +135,14 @@ def same_dist(got, ref, rtol):
     assert all(abs(got[k] - ref[k]) <= rtol * top for k in ref)
 
 
+@pytest.mark.parametrize("packed", [True, False])
 @pytest.mark.parametrize("batched", [True, False])
 @pytest.mark.parametrize("seed", range(4))
-def test_probs_svd_host_logic(oracle, batched, seed):
+def test_probs_svd_host_logic(oracle, monkeypatch, packed, batched, seed):
+    """Both recombinations: packed integer keys, and output ranks (states too wide to pack)."""
+    import perceval_gb300.simulators as S
+    if not packed:
+        monkeypatch.setattr(S, "_PACKED_BITS", 0)
     m = 8
     U = random_unitary(m, seed=seed)
     items = mixture(m, 100 + seed, 40)  # holds repeated inputs, kept entry by entry
