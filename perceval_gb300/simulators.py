@@ -33,8 +33,7 @@ from typing import Callable
 import numpy as np
 
 from .utils.globals import global_params
-from .utils.states import (BSCount, BSDistribution, BSSamples, FockState, fock_rank_array, fock_space_size,
-                           fock_unrank_array)
+from .utils.states import BSCount, BSDistribution, BSSamples, FockState, fock_rank_array, fock_unrank_array
 
 __all__ = ["Simulator", "SamplesProvider"]
 
@@ -130,24 +129,22 @@ class Simulator:
         """_list_merge over the parts' outputs: every combination whose running product stays
         at or above ``threshold``, photon counts summed mode by mode; products are formed left
         to right and the combinations come in the order of the reference's recursion.
-        Returns (ranks of the merged outputs, probabilities)."""
+        Returns (occupation rows of the merged outputs, probabilities)."""
 
         def rows(s):
             if s not in rows_cache:
                 rows_cache[s] = fock_unrank_array(s.m, s.n, cache[s][0]).astype(np.int64)
             return rows_cache[s]
 
-        r0, p = cache[parts[0]]
+        p = cache[parts[0]][1]
         keep = p >= threshold
-        if len(parts) == 1:
-            return r0[keep], p[keep]
         cur, p = rows(parts[0])[keep], p[keep]
         for s in parts[1:]:
             prod = p[:, None] * cache[s][1][None, :]
             i, j = np.nonzero(prod >= threshold)
             cur = cur[i] + rows(s)[j]
             p = prod[i, j]
-        return (fock_rank_array(cur) if len(cur) else np.zeros(0, dtype=np.int64)), p
+        return cur, p
 
     @staticmethod
     def _merge_keys(parts, cache, keys_cache: dict, shifts: np.ndarray, threshold: float):
@@ -266,33 +263,30 @@ class Simulator:
                 res.normalize()
             return res
 
-        # wider states: recombination accumulated densely per photon count by output rank
-        acc: dict[int, np.ndarray] = {}
-        touched: dict[int, np.ndarray] = {}
+        # wider states: the same recombination on occupation rows
         rows_cache: dict = {}
-        for prob0, parts, n in decomposed:
-            ranks, p = self._merge(parts, cache, rows_cache, p_threshold / (10 * prob0))
+        all_r, all_w = [], []
+        for prob0, parts, _ in decomposed:
+            r, p = self._merge(parts, cache, rows_cache, p_threshold / (10 * prob0))
             self.DEBUG_merge_count += len(parts) - 1
-            if n not in acc:
-                size = fock_space_size(m, n)
-                acc[n] = np.zeros(size)
-                touched[n] = np.zeros(size, dtype=bool)
             if len(parts) == 1:  # distinct outputs already
-                out, within = ranks, p
+                out, within = r, p
             else:  # sums of one input per output, added in recursion order
-                out, inv = np.unique(ranks, return_inverse=True)
-                within = np.bincount(inv, weights=p, minlength=len(out))
+                out, inv = np.unique(r, axis=0, return_inverse=True)
+                within = np.bincount(inv.ravel(), weights=p, minlength=len(out))
             self._logical_perf += float(within.sum()) * prob0
-            acc[n][out] += within * prob0
-            touched[n][out] = True
+            all_r.append(out)
+            all_w.append(within * prob0)
         if progress_callback is not None:
             progress_callback(1.0, "recombine distributions")
-
         res = BSDistribution()
-        for n in sorted(acc):
-            idx = np.nonzero(touched[n])[0]
-            rows = fock_unrank_array(m, n, idx).tolist()
-            for row, v in zip(rows, acc[n][idx].tolist()):
+        R = np.concatenate(all_r) if all_r else np.zeros((0, m), dtype=np.int64)
+        if len(R):
+            ur, inv = np.unique(R, axis=0, return_inverse=True)
+            acc = np.bincount(inv.ravel(), weights=np.concatenate(all_w), minlength=len(ur))
+            # by photon count, then descending-lex
+            order = np.lexsort(tuple(-ur[:, i] for i in range(m - 1, -1, -1)) + (ur.sum(axis=1),))
+            for row, v in zip(ur[order].tolist(), acc[order].tolist()):
                 dict.__setitem__(res, FockState._trusted(tuple(row)), v)
         if len(res):
             res.normalize()

@@ -162,6 +162,19 @@ def test_probs_svd_host_logic(oracle, monkeypatch, packed, batched, seed):
         assert be.batched_calls == 1
 
 
+def test_probs_svd_wide_states(oracle):
+    """m = 40 with up to 3 photons: 40 modes x 2 bits do not pack into 64 bits, so the
+    recombination runs on occupation rows; memory follows the outputs, not the Fock space."""
+    m = 40
+    U = random_unitary(m, seed=5)
+    items = mixture(m, 7, 10, max_parts=3, max_n=1)
+    sim = Simulator(FakeStrong(oracle, U, True))
+    out = sim.probs_svd(items)
+    ref, phys, logical = ref_probs_svd(oracle_dist(oracle, U), items)
+    same_dist(out["results"], ref, 1e-13)
+    assert math.isclose(out["logical_perf"], logical, rel_tol=1e-12)
+
+
 def test_probs_svd_shortcut_and_thresholds(oracle):
     m = 5
     U = random_unitary(m, seed=9)
