@@ -3,10 +3,11 @@
 
 Headline workload (one step = one pass over one batch): exact permanents of 8192
 complex128 Haar submatrices, n uniform in 8..24, rows/columns drawn without
-replacement from a 1024x1024 Haar unitary (seed 0), all in one
-pcvl_permanent_batch call (size bins launched back to back).  `value` is perms/s
-with the matrices resident in HBM; `e2e` is the same through the C ABI from pinned
-host buffers with both copies inside the timed region.
+replacement from a 1024x1024 Haar unitary (seed 0), computed in native FP64 (the
+reference's arithmetic) by one permanent plan (one CUDA graph: prepare, the size bins
+as concurrent branches, reduce).  `value` is perms/s with the matrices resident in
+HBM; `e2e` is the same through the C ABI from pinned host buffers with both copies
+inside the timed region.  The float-float arithmetic (opt-in) is a secondary line.
 
 Secondary lines in the same JSON: SLOS full distribution m=24/n=12 (amplitudes/s,
 HBM roofline), batched SLOS forward+adjoint on 256 Clements meshes m=16/n=8,
@@ -261,8 +262,9 @@ def run_ours(args):
     # launch shapes of the permanent bins: the cached autotuner table for this GPU, or a
     # fresh tuning run (about 20 s, untimed) that is then cached
     t_tune = time.perf_counter()
-    table = autotune.ensure_tuned(range(8, 25), log=lambda s: print(s, file=sys.stderr))
-    tuning = {"sizes": "8..24", "source": "cached table" if table is None else "tuned in this run",
+    table = autotune.ensure_tuned(range(8, 25), log=lambda s: print(s, file=sys.stderr), precision="fp64")
+    tuning = {"sizes": "8..24", "arithmetic": "fp64",
+              "source": "cached table" if table is None else "tuned in this run",
               "seconds": round(time.perf_counter() - t_tune, 1)}
 
     mats, flat, offs, sizes = make_batch(seed=rank)
@@ -272,7 +274,7 @@ def run_ours(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     bins = len(set(int(n) for n in sizes))
     launches_per_step = bins + 2  # graph nodes: prepare + one per size bin + reduce
-    plan = _native.PermPlan(offs, sizes)  # fixed batch shape: one CUDA graph per step
+    plan = _native.PermPlan(offs, sizes, precision="fp64")  # fixed batch shape: one CUDA graph per step
 
     def step():
         plan(flat_d, out_d)
@@ -320,21 +322,21 @@ def run_ours(args):
            "h2d_bytes_per_step": int(flat.nbytes),
            "d2h_bytes_per_step": int(N_MATS * 16)}
 
-    # dominant kernel alone: the n = 24 bin (its CTAs' share of the step is largest)
+    # dominant kernel alone: the n = 24 bin (its CTAs' share of the step is largest), FP64
     sel = [i for i in range(N_MATS) if sizes[i] == 24]
     sub = np.concatenate([mats[i].reshape(-1) for i in sel])
     sub_d = torch.from_numpy(sub).to(dev)
     sub_out = torch.empty(len(sel), dtype=torch.complex128, device=dev)
     sub_offs = np.arange(len(sel), dtype=np.int64) * 576
     sub_sizes = np.full(len(sel), 24, dtype=np.int32)
-    _native.permanent_batch(sub_d, sub_offs, sub_sizes, sub_out)
+    _native.permanent_batch(sub_d, sub_offs, sub_sizes, sub_out, precision="fp64")
     torch.cuda.synchronize()
     kt = []
     for _ in range(3):
         flush.zero_()
         s, e = torch.cuda.Event(True), torch.cuda.Event(True)
         s.record()
-        _native.permanent_batch(sub_d, sub_offs, sub_sizes, sub_out)
+        _native.permanent_batch(sub_d, sub_offs, sub_sizes, sub_out, precision="fp64")
         e.record()
         e.synchronize()
         kt.append(s.elapsed_time(e))
@@ -342,15 +344,18 @@ def run_ours(args):
     fp64_peak = measured_fp64_peak(torch)
     achieved = len(sel) * glynn_flops(24) / (k_ms * 1e-3) / 1e12
     roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": achieved / fp64_peak, "traffic": traffic_from_profile("perm_bin_n24"),
-                "kernel": "perm_bin_kernel<24> (the n=24 bin of the batch)",
-                "peak_source": "measured cuBLAS DGEMM 4096^3 on this GPU (no FP64 entry in the measured peaks)",
-                "note": "float-float on the FP32 pipe: frac > 1 means faster than native FP64 peak",
-                "step_tflops_fp64_equiv": flops_total / (ms / args.steps * 1e-3) / 1e12}
+                "frac": achieved / fp64_peak, "traffic": traffic_from_profile("perm_bin_f64_n24"),
+                "kernel": "perm_bin_f64<24> (the n=24 bin of the batch)",
+                "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 on this GPU (the measured peaks file "
+                               "has no FP64 entry)",
+                "algorithmic_flops_per_permanent": "2^(n-1) (8n - 4)",
+                "note": "native FP64 arithmetic; the kernel issues 6n - 4 FP64 instructions per sign vector "
+                        "for 8n - 4 algorithmic flops, so frac <= (8n-4)/(2(6n-4)) = 0.67 at n = 24",
+                "step_tflops": flops_total / (ms / args.steps * 1e-3) / 1e12}
 
     line = {"metric": METRIC, "value": value, "unit": "perms/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "complex128 I/O, float-float (f32x2) arithmetic", "data": "synthetic",
+            "vs_baseline": None, "dtype": "complex128 (FP64)", "data": "synthetic",
             "config": {"workload": WORKLOAD, "l2": "flushed between timed steps (256 MiB write)",
                        "parallelism": f"replicas x{ws}",
                        "launch": f"one CUDA graph per step (pcvl_perm_plan_execute: prepare, {bins} size bins as "
@@ -368,12 +373,36 @@ def run_ours(args):
             flush.zero_()
             s, e = torch.cuda.Event(True), torch.cuda.Event(True)
             s.record()
-            _native.permanent_batch(flat_d, offs, sizes, out_d)
+            _native.permanent_batch(flat_d, offs, sizes, out_d, precision="fp64")
             e.record()
             e.synchronize()
             kb.append(s.elapsed_time(e))
-        sec["perm_batch_call_8192"] = {"ms": statistics.median(kb),
+        sec["perm_batch_call_8192"] = {"ms": statistics.median(kb), "arithmetic": "fp64",
                                        "perms_per_s": N_MATS / (statistics.median(kb) * 1e-3)}
+        # the same batch in float-float (opt-in): a plan of its own, its own tuned shapes
+        autotune.ensure_tuned(range(8, 25), log=lambda s: print(s, file=sys.stderr), precision="float-float")
+        ref64 = out_d.clone()
+        ff_plan = _native.PermPlan(offs, sizes, precision="float-float")
+        ff_out = torch.empty_like(out_d)
+        for _ in range(args.warmup):
+            ff_plan(flat_d, ff_out)
+        torch.cuda.synchronize()
+        kf = []
+        for _ in range(args.steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(True), torch.cuda.Event(True)
+            s.record()
+            ff_plan(flat_d, ff_out)
+            e.record()
+            e.synchronize()
+            kf.append(s.elapsed_time(e))
+        ff_ms = statistics.mean(kf)
+        sec["perm_batch_float_float"] = {
+            "ms_per_step": ff_ms, "perms_per_s": N_MATS / (ff_ms * 1e-3),
+            "speedup_vs_fp64": (ms / args.steps) / ff_ms,
+            "max_rel_diff_vs_fp64": float(((ff_out - ref64).abs() / ref64.abs()).max()),
+            "step_tflops_fp64_equiv": flops_total / (ff_ms * 1e-3) / 1e12}
+        del ff_plan
         sec.update(secondary(torch, _native, random_unitary, dev, flush))
         line["secondary"] = sec
     if rank == 0 and ws == 1 and not args.skip_cpu:
@@ -502,27 +531,40 @@ def secondary(torch, _native, random_unitary, dev, flush):
     # unitary), Glynn and Ryser, with their relative difference
     Ubig = random_unitary(1024, seed=0)
     rng = np.random.default_rng(5)
-    for n in (32, 36):
+    # n = 32 and 36 in both arithmetics (FP64 Ryser at 32 only: 3x Glynn's time); n = 40 in
+    # float-float, its FP64 time extrapolated from n = 36 by the 2^(n-1) (8n - 4) flop count
+    for n in (32, 36, 40):
         a = np.ascontiguousarray(Ubig[np.ix_(rng.choice(1024, n, False), rng.choice(1024, n, False))])
         ad = torch.from_numpy(a).to(dev)
         o = torch.empty(1, dtype=torch.complex128, device=dev)
         res_n = {}
-        for name, method in (("glynn", 0), ("ryser", 1)):
+        runs = [("glynn_fp64", 0, "fp64"), ("ryser_fp64", 1, "fp64"), ("glynn_ff", 0, "float-float"),
+                ("ryser_ff", 1, "float-float")]
+        if n == 36:
+            runs = [r for r in runs if r[0] != "ryser_fp64"]
+        if n == 40:
+            runs = [("glynn_ff", 0, "float-float")]
+        for name, method, prec in runs:
             s0, e0 = torch.cuda.Event(True), torch.cuda.Event(True)
             s0.record()
-            _native.permanent_batch(ad, np.array([0]), np.array([n]), o, method)
+            _native.permanent_batch(ad, np.array([0]), np.array([n]), o, method, precision=prec)
             e0.record()
             e0.synchronize()
-            res_n[name] = complex(o.cpu().item())
+            v = complex(o.cpu().item())
+            res_n[name] = [v.real, v.imag]
             res_n[f"{name}_ms"] = s0.elapsed_time(e0)
-        res_n["glynn_tflops_fp64_equiv"] = glynn_flops(n) / (res_n["glynn_ms"] * 1e-3) / 1e12
-        res_n["glynn_ryser_rel_diff"] = abs(res_n["glynn"] - res_n["ryser"]) / abs(res_n["glynn"])
-        res_n["glynn"] = [res_n["glynn"].real, res_n["glynn"].imag]
-        res_n["ryser"] = [res_n["ryser"].real, res_n["ryser"].imag]
+            res_n[f"{name}_tflops"] = glynn_flops(n) / (res_n[f"{name}_ms"] * 1e-3) / 1e12
+        if "glynn_fp64" in res_n:
+            ref = complex(*res_n["glynn_fp64"])
+            for name in ("ryser_fp64", "glynn_ff", "ryser_ff"):
+                if name in res_n:
+                    res_n[f"{name}_rel_diff_vs_glynn_fp64"] = abs(complex(*res_n[name]) - ref) / abs(ref)
         res[f"perm_single_n{n}"] = res_n
+    t36 = res["perm_single_n36"]["glynn_fp64_ms"]
+    res["perm_single_n40"]["glynn_fp64_ms_extrapolated"] = t36 * glynn_flops(40) / glynn_flops(36)
     # Clifford & Clifford, n=20, m=400
     U4 = torch.from_numpy(random_unitary(400, seed=0)).to(dev)
-    cnt = 20000
+    cnt = 100000  # the configuration's 1e5 samples
     t_cc = timed(lambda: _native.cc2017_sample(U4, [1] * 20 + [0] * 380, cnt, seed=1), reps=1)
     res["cc2017_n20_m400"] = {"samples_per_s": cnt / (t_cc * 1e-3), "samples": cnt, "precision": "float-float"}
     # many input states (the per-input loop of a samples provider): 64 distinct 6-photon inputs

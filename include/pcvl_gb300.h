@@ -26,12 +26,23 @@ extern "C" {
 #define PCVL_ERR_MEMORY 3   /* the request does not fit in device memory */
 #define PCVL_ERR_TIMEOUT 4  /* a bounded device-side wait gave up */
 
+/* Arithmetic of the permanent, SLOS and sampler kernels (`precision` arguments).
+ * PCVL_PREC_FP64: native FP64, the reference's own arithmetic (complex128 in
+ * exqalibur); the default of the Python layer.  PCVL_PREC_FLOAT_FLOAT: every value an
+ * unevaluated pair of FP32 numbers (~48 significant bits) on the FP32 pipe, several
+ * times faster on GB300, whose FP64 rate is a small fraction of its FP32 rate.
+ * PCVL_PREC_FP32: FP32 with compensated sums (sampler only). */
+#define PCVL_PREC_FLOAT_FLOAT 0
+#define PCVL_PREC_FP32 1
+#define PCVL_PREC_FP64 2
+
 /* ------------------------------------------------------------------ errors */
-/* Library version string, e.g. "pcvl_gb300 0.1.0 sm_103a". */
+/* Library version string, e.g. "pcvl_gb300 0.2.0 sm_103a". */
 const char* pcvl_version(void);
 /* Copies the calling thread's last error message into buf (NUL-terminated). */
 int pcvl_last_error(char* buf, size_t len);
-/* Frees every workspace the library cached on the current device. */
+/* Returns to the device the scratch memory the library's pool keeps on the current
+ * device (after a device synchronisation). */
 int pcvl_release_workspace(void);
 
 /* ------------------------------------------------------------------ permanents
@@ -41,13 +52,19 @@ int pcvl_release_workspace(void);
  * Batched exact permanents of `count` square complex128 matrices stored row-major
  * in mats_d; matrix i starts at complex element offsets_h[i] and has size
  * sizes_h[i] (0 <= n <= 40; the permanent of the 0x0 matrix is 1).  Results go to
- * out_d[i] (complex128).  method: 0 = Glynn (Gray-code over 2^(n-1) sign
- * vectors), 1 = Ryser (over 2^n column subsets).  Matrices are binned by size;
- * each bin's launch spreads Gray-code chunks across the whole chip, so one large
- * matrix uses every SM.  offsets_h and sizes_h are host arrays.
+ * out_d[i] (complex128).  method: 0 = Glynn (sum over the 2^(n-1) sign vectors),
+ * 1 = Ryser (over the 2^n column subsets).  The sign bits split into "lo" bits that
+ * every thread enumerates from a shared-memory table of row-sum parts and "hi" bits
+ * spread over threads and CTAs (walked in Gray-code order in FP64), so one large
+ * matrix uses every SM; matrices are binned by size, one launch per size.  precision:
+ * PCVL_PREC_FP64 or PCVL_PREC_FLOAT_FLOAT.  The matrices must not overlap in mats_d,
+ * except as identical entries (same offset and size): each is rescaled in place in
+ * the library's scratch at its own offsets.  offsets_h and sizes_h are host arrays.
+ * Scratch comes from a stream-ordered pool per call, so concurrent calls on
+ * different streams or threads are independent.
  */
 int pcvl_permanent_batch(const double* mats_d, const int64_t* offsets_h, const int32_t* sizes_h,
-                         int32_t count, double* out_d, int32_t method, void* stream);
+                         int32_t count, double* out_d, int32_t method, int32_t precision, void* stream);
 
 /* Allocation-free variant of pcvl_permanent_batch.  It has no counterpart in the
  * reference.  Some callers cannot call cudaMalloc: a plugin inside a host program
@@ -58,15 +75,20 @@ int pcvl_permanent_batch(const double* mats_d, const int64_t* offsets_h, const i
  * anything: its scratch is a fixed array of about 53 MB held on every GPU that loads
  * the library until the process exits.  Limits per call: at most 16384 matrices, at
  * most 3 * 2^20 complex elements spanned by offsets_h[i] + sizes_h[i]^2, at most 2^17
- * CTA partial sums (ample for batches within the first two limits); larger requests
- * are refused with PCVL_ERR_ARG and a message naming the limit.  The first call on a
- * device looks up the scratch's device address (cudaGetSymbolAddress); make that
- * first call before any stream capture.  Every call reuses the same scratch and
+ * CTA partial sums.  With the built-in launch shapes the third limit is reached only
+ * by batches beyond the first two; launch shapes tuned to many CTAs per SM
+ * (pcvl_perm_set_tuning) can reach it with a few large matrices in each of many size
+ * bins.  Larger requests are refused with PCVL_ERR_ARG and a message naming the
+ * limit.  The first call on a device looks up the scratch's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.  Every
+ * call copies its descriptors (about 24 bytes per matrix) from a static host buffer.
+ * Every call reuses the same scratch and
  * rewrites every part of it that it reads, so nothing needs clearing; but calls whose
  * GPU work overlaps (different streams, or different host threads without ordering)
  * race on it and must be serialised by the caller. */
 int pcvl_permanent_batch_noalloc(const double* mats_d, const int64_t* offsets_h, const int32_t* sizes_h,
-                                 int32_t count, double* out_d, int32_t method, void* stream);
+                                 int32_t count, double* out_d, int32_t method, int32_t precision,
+                                 void* stream);
 
 /* Monte-Carlo permanent estimates.  Replaces xq.estimate_permanent_cx(M, iterations),
  * which returns (estimate, error) to NaiveApproxBackend (perceval/backends/_naive_approx.py:52-59).
@@ -82,14 +104,15 @@ int pcvl_permanent_estimate_batch(const double* mats_d, const int64_t* offsets_h
                                   double* out_d, double* err_d, void* stream);
 
 /* Launch-shape tuning of the permanent kernels (no reference counterpart; written by the
- * autotuner in perceval_gb300/autotune.py).  For method (0 Glynn, 1 Ryser) and size n:
+ * autotuner in perceval_gb300/autotune.py).  For method (0 Glynn, 1 Ryser), precision
+ * (PCVL_PREC_FP64 or PCVL_PREC_FLOAT_FLOAT: each arithmetic has its own table) and size n:
  * lo_bits = sign bits every thread enumerates from the shared-memory table (-1: built-in
  * min(7, max(0, F - 7)) with F the free bits), ctas_per_sm = target CTAs per SM over a
  * size bin (0: built-in 8).  Applies to later calls and plans on every device; results
  * change only by rounding.  Host-only, thread-safe. */
-int pcvl_perm_set_tuning(int32_t method, int32_t n, int32_t lo_bits, int32_t ctas_per_sm);
-/* The effective lo bits and CTAs per SM for (method, n). */
-int pcvl_perm_get_tuning(int32_t method, int32_t n, int32_t* lo_bits, int32_t* ctas_per_sm);
+int pcvl_perm_set_tuning(int32_t method, int32_t precision, int32_t n, int32_t lo_bits, int32_t ctas_per_sm);
+/* The effective lo bits and CTAs per SM for (method, precision, n). */
+int pcvl_perm_get_tuning(int32_t method, int32_t precision, int32_t n, int32_t* lo_bits, int32_t* ctas_per_sm);
 
 /* Permanent plans (no reference counterpart): the batch layout of pcvl_permanent_batch
  * fixed once for given sizes and offsets and executed as one CUDA graph (prepare, every
@@ -101,7 +124,7 @@ int pcvl_perm_get_tuning(int32_t method, int32_t n, int32_t* lo_bits, int32_t* c
 typedef struct pcvl_perm_plan pcvl_perm_plan;
 
 int pcvl_perm_plan_create(pcvl_perm_plan** plan, const int64_t* offsets_h, const int32_t* sizes_h,
-                          int32_t count, int32_t method);
+                          int32_t count, int32_t method, int32_t precision);
 int pcvl_perm_plan_execute(pcvl_perm_plan* plan, const double* mats_d, double* out_d, void* stream);
 /* Device bytes the plan holds. */
 int pcvl_perm_plan_bytes(const pcvl_perm_plan* plan, int64_t* bytes);

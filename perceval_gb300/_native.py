@@ -21,19 +21,19 @@ SYMBOLS = {
     "pcvl_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     "pcvl_release_workspace": (ctypes.c_int, []),
     "pcvl_permanent_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
-                                            ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
+                                            ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]),
     "pcvl_permanent_batch_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                     ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
-                                                    ctypes.c_void_p]),
+                                                    ctypes.c_int32, ctypes.c_void_p]),
     "pcvl_permanent_estimate_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                      ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64,
                                                      ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
                                                      ctypes.c_void_p]),
-    "pcvl_perm_set_tuning": (ctypes.c_int, [ctypes.c_int32] * 4),
-    "pcvl_perm_get_tuning": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
-                                            ctypes.POINTER(ctypes.c_int32)]),
+    "pcvl_perm_set_tuning": (ctypes.c_int, [ctypes.c_int32] * 5),
+    "pcvl_perm_get_tuning": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                            ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "pcvl_perm_plan_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p, ctypes.c_void_p,
-                                             ctypes.c_int32, ctypes.c_int32]),
+                                             ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "pcvl_perm_plan_execute": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "pcvl_perm_plan_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     "pcvl_perm_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
@@ -134,6 +134,22 @@ def check(status: int, what: str):
         raise RuntimeError(f"{what} failed (status {status}): {last_error()}")
 
 
+# precision codes of the C ABI (PCVL_PREC_*)
+PREC_FLOAT_FLOAT, PREC_FP32, PREC_FP64 = 0, 1, 2
+_PREC_NAMES = {"fp64": PREC_FP64, "float64": PREC_FP64, "float-float": PREC_FLOAT_FLOAT,
+               "ff": PREC_FLOAT_FLOAT, "fp32": PREC_FP32}
+
+
+def precision_code(precision) -> int:
+    """ABI code of a precision given as a code or a name ("fp64", "float-float", "fp32")."""
+    if isinstance(precision, str):
+        try:
+            return _PREC_NAMES[precision.lower()]
+        except KeyError:
+            raise ValueError(f"unknown precision {precision!r}: use 'fp64' or 'float-float'") from None
+    return int(precision)
+
+
 def _stream_ptr(stream) -> int:
     if stream is None:
         stream = torch.cuda.current_stream()
@@ -152,8 +168,9 @@ def _dev_tensor(t: torch.Tensor, dtype, name: str) -> torch.Tensor:
 
 # ------------------------------------------------------------------ permanents
 def permanent_batch(mats: torch.Tensor, offsets: np.ndarray, sizes: np.ndarray, out: torch.Tensor,
-                    method: int = 0, stream=None) -> torch.Tensor:
-    """Permanents of packed square complex128 matrices (see pcvl_permanent_batch)."""
+                    method: int = 0, stream=None, precision="fp64") -> torch.Tensor:
+    """Permanents of packed square complex128 matrices (see pcvl_permanent_batch); FP64
+    arithmetic unless ``precision="float-float"``."""
     lib = load()
     _dev_tensor(mats, torch.complex128, "mats")
     _dev_tensor(out, torch.complex128, "out")
@@ -165,12 +182,13 @@ def permanent_batch(mats: torch.Tensor, offsets: np.ndarray, sizes: np.ndarray, 
     if count and int((offsets + sizes.astype(np.int64) ** 2).max()) > mats.numel():
         raise ValueError("a matrix extends beyond the end of mats")
     check(lib.pcvl_permanent_batch(mats.data_ptr(), offsets.ctypes.data, sizes.ctypes.data, count,
-                                   out.data_ptr(), int(method), _stream_ptr(stream)), "pcvl_permanent_batch")
+                                   out.data_ptr(), int(method), precision_code(precision), _stream_ptr(stream)),
+          "pcvl_permanent_batch")
     return out
 
 
 def permanent_batch_noalloc(mats: torch.Tensor, offsets: np.ndarray, sizes: np.ndarray, out: torch.Tensor,
-                            method: int = 0, stream=None) -> torch.Tensor:
+                            method: int = 0, stream=None, precision="fp64") -> torch.Tensor:
     """Same as ``permanent_batch`` through the allocation-free entry point: the library
     allocates no device memory for the call (fixed per-call limits, see the header)."""
     lib = load()
@@ -184,7 +202,8 @@ def permanent_batch_noalloc(mats: torch.Tensor, offsets: np.ndarray, sizes: np.n
     if count and int((offsets + sizes.astype(np.int64) ** 2).max()) > mats.numel():
         raise ValueError("a matrix extends beyond the end of mats")
     check(lib.pcvl_permanent_batch_noalloc(mats.data_ptr(), offsets.ctypes.data, sizes.ctypes.data, count,
-                                           out.data_ptr(), int(method), _stream_ptr(stream)),
+                                           out.data_ptr(), int(method), precision_code(precision),
+                                           _stream_ptr(stream)),
           "pcvl_permanent_batch_noalloc")
     return out
 
@@ -212,17 +231,18 @@ def permanent_estimate_batch(mats: torch.Tensor, offsets: np.ndarray, sizes: np.
     return out, err
 
 
-def set_perm_tuning(method: int, n: int, lo_bits: int = -1, ctas_per_sm: int = 0):
-    """Launch shape of the size-n permanent bin (-1 / 0: built-in choice).  Host-only."""
-    check(load(require_cuda=False).pcvl_perm_set_tuning(int(method), int(n), int(lo_bits), int(ctas_per_sm)),
-          "pcvl_perm_set_tuning")
+def set_perm_tuning(method: int, n: int, lo_bits: int = -1, ctas_per_sm: int = 0, precision="fp64"):
+    """Launch shape of the size-n permanent bin of one arithmetic (-1 / 0: built-in
+    choice).  Host-only."""
+    check(load(require_cuda=False).pcvl_perm_set_tuning(int(method), precision_code(precision), int(n),
+                                                        int(lo_bits), int(ctas_per_sm)), "pcvl_perm_set_tuning")
 
 
-def get_perm_tuning(method: int, n: int) -> tuple[int, int]:
-    """Effective (lo_bits, ctas_per_sm) of the size-n permanent bin."""
+def get_perm_tuning(method: int, n: int, precision="fp64") -> tuple[int, int]:
+    """Effective (lo_bits, ctas_per_sm) of the size-n permanent bin of one arithmetic."""
     lo, ct = ctypes.c_int32(), ctypes.c_int32()
-    check(load(require_cuda=False).pcvl_perm_get_tuning(int(method), int(n), ctypes.byref(lo), ctypes.byref(ct)),
-          "pcvl_perm_get_tuning")
+    check(load(require_cuda=False).pcvl_perm_get_tuning(int(method), precision_code(precision), int(n),
+                                                        ctypes.byref(lo), ctypes.byref(ct)), "pcvl_perm_get_tuning")
     return lo.value, ct.value
 
 
@@ -230,8 +250,9 @@ class PermPlan:
     """Owner of a ``pcvl_perm_plan``: permanents of a fixed batch shape, executed as one
     CUDA graph per call (see pcvl_perm_plan_create)."""
 
-    def __init__(self, offsets: np.ndarray, sizes: np.ndarray, method: int = 0):
+    def __init__(self, offsets: np.ndarray, sizes: np.ndarray, method: int = 0, precision="fp64"):
         self._lib = load()
+        self.precision = precision_code(precision)
         self.offsets = np.ascontiguousarray(offsets, dtype=np.int64)
         self.sizes = np.ascontiguousarray(sizes, dtype=np.int32)
         self.count = int(self.sizes.shape[0])
@@ -240,7 +261,7 @@ class PermPlan:
         self.span = int((self.offsets + self.sizes.astype(np.int64) ** 2).max())
         h = ctypes.c_void_p()
         check(self._lib.pcvl_perm_plan_create(ctypes.byref(h), self.offsets.ctypes.data, self.sizes.ctypes.data,
-                                              self.count, int(method)), "pcvl_perm_plan_create")
+                                              self.count, int(method), self.precision), "pcvl_perm_plan_create")
         self._h = h
 
     @property

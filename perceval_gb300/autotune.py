@@ -11,8 +11,10 @@ fastest through ``pcvl_perm_set_tuning`` and records the table.  Tables are cach
 JSON keyed by device name, SM count and library version; ``load`` ignores a table made
 on another device or build.
 
-Results do not depend on the tuning beyond rounding: every candidate computes the same
-Gray-code sum, only split differently (the tuner checks this on each candidate).
+Each arithmetic (FP64, float-float) has its own table: their kernels differ in register
+and shared-memory footprint.  Results do not depend on the tuning beyond rounding: every
+candidate computes the same sign-vector sum, only split differently (the tuner checks this
+on each candidate).
 """
 from __future__ import annotations
 
@@ -91,9 +93,13 @@ def _time_ms(fn, reps: int) -> float:
 
 
 def tune_permanents(sizes=range(8, 27), method: int = 0, target_ms: float = 20.0, reps: int = 3,
-                    seed: int = 0, rate_flops: float = 3.5e12, log=None) -> dict:
-    """Tunes every size in ``sizes`` and installs the winners; returns the table
-    {"key": device_key(), "method": method, "entries": {n: {...}}}."""
+                    seed: int = 0, rate_flops: float | None = None, log=None, precision="fp64") -> dict:
+    """Tunes every size in ``sizes`` for one arithmetic and installs the winners; returns
+    the table {"key": device_key(), "method": method, "precision": name, "entries": {n: {...}}}."""
+    code = _native.precision_code(precision)
+    name = "fp64" if code == _native.PREC_FP64 else "float-float"
+    if rate_flops is None:  # work per candidate run: about target_ms at the expected rate
+        rate_flops = 0.7e12 if code == _native.PREC_FP64 else 3.5e12
     entries = {}
     for n in sizes:
         n = int(n)
@@ -102,15 +108,15 @@ def tune_permanents(sizes=range(8, 27), method: int = 0, target_ms: float = 20.0
         out = torch.empty(count, dtype=torch.complex128, device=mats.device)
 
         def run():
-            _native.permanent_batch(mats, offsets, sizes_a, out, method)
+            _native.permanent_batch(mats, offsets, sizes_a, out, method, precision=code)
 
-        _native.set_perm_tuning(method, n)  # built-in shape first: reference values and time
+        _native.set_perm_tuning(method, n, precision=code)  # built-in shape first: reference values and time
         t_default = _time_ms(run, reps)
         ref = out.clone()
         best = (t_default, -1, 0)
         tol = 1e-8 if method == 0 else 1e-4  # Ryser's cancellation leaves more rounding
         for lo, c in candidates(n, method):
-            _native.set_perm_tuning(method, n, lo, c)
+            _native.set_perm_tuning(method, n, lo, c, precision=code)
             t = _time_ms(run, reps)
             rel = float(((out - ref).abs() / ref.abs().clamp_min(1e-300)).max())
             if rel > tol:
@@ -118,52 +124,88 @@ def tune_permanents(sizes=range(8, 27), method: int = 0, target_ms: float = 20.0
             if t < best[0]:
                 best = (t, lo, c)
         t, lo, c = best
-        _native.set_perm_tuning(method, n, lo, c)
-        eff_lo, eff_c = _native.get_perm_tuning(method, n)
+        _native.set_perm_tuning(method, n, lo, c, precision=code)
+        eff_lo, eff_c = _native.get_perm_tuning(method, n, precision=code)
         entries[str(n)] = {"lo_bits": eff_lo, "ctas_per_sm": eff_c, "ms": t, "default_ms": t_default,
                            "matrices": count}
         if log:
-            log(f"n={n}: lo={eff_lo} ctas/SM={eff_c} {t:.3f} ms (built-in {t_default:.3f} ms, {count} matrices)")
-    return {"key": device_key(), "method": method, "entries": entries}
+            log(f"{name} n={n}: lo={eff_lo} ctas/SM={eff_c} {t:.3f} ms (built-in {t_default:.3f} ms, "
+                f"{count} matrices)")
+    return {"key": device_key(), "method": method, "precision": name, "entries": entries}
+
+
+def _tables(doc: dict) -> list[dict]:
+    """The tables of a cache document (one table per method and arithmetic)."""
+    if "tables" in doc:
+        return list(doc["tables"])
+    if "entries" in doc:  # a document holding one table
+        return [doc]
+    return []
 
 
 def apply(table: dict) -> int:
-    """Installs a table's entries; returns how many were set."""
-    method = int(table.get("method", 0))
+    """Installs a table's entries (a table, or a cache document of several); returns how
+    many were set."""
     k = 0
-    for n, e in table.get("entries", {}).items():
-        _native.set_perm_tuning(method, int(n), int(e["lo_bits"]), int(e["ctas_per_sm"]))
-        k += 1
+    for t in _tables(table):
+        method = int(t.get("method", 0))
+        prec = t.get("precision", "float-float")
+        for n, e in t.get("entries", {}).items():
+            _native.set_perm_tuning(method, int(n), int(e["lo_bits"]), int(e["ctas_per_sm"]), precision=prec)
+            k += 1
     return k
 
 
 def save(table: dict, path: Path | None = None) -> Path:
+    """Adds (or replaces) a table in the cache document for this device and build."""
     path = Path(path) if path else default_cache_path()
     path.parent.mkdir(parents=True, exist_ok=True)
+    doc = {"key": table["key"], "tables": []}
+    try:
+        old = json.loads(path.read_text())
+        if old.get("key") == table["key"]:
+            doc["tables"] = [t for t in _tables(old)
+                             if (t.get("method", 0), t.get("precision", "float-float")) !=
+                             (table.get("method", 0), table.get("precision", "float-float"))]
+    except (OSError, ValueError):
+        pass
+    doc["tables"].append({k: v for k, v in table.items() if k != "key"})
     tmp = path.with_name(f"{path.name}.{os.getpid()}.tmp")
-    tmp.write_text(json.dumps(table, indent=1, sort_keys=True))
+    tmp.write_text(json.dumps(doc, indent=1, sort_keys=True))
     os.replace(tmp, path)  # atomic: concurrent processes never read a partial table
     return path
 
 
-def load(path: Path | None = None, key: dict | None = None) -> bool:
-    """Applies a cached table if it exists and was made for this device and build."""
-    path = Path(path) if path else default_cache_path()
+def _cached(path: Path, key: dict) -> list[dict]:
     if not path.exists():
-        return False
+        return []
     try:
-        table = json.loads(path.read_text())
+        doc = json.loads(path.read_text())
     except (OSError, ValueError):
-        return False
-    if table.get("key") != (key if key is not None else device_key()):
-        return False
-    return apply(table) > 0
+        return []
+    if doc.get("key") != key:
+        return []
+    return _tables(doc)
 
 
-def ensure_tuned(sizes=range(8, 27), method: int = 0, path: Path | None = None, log=None) -> dict | None:
-    """Loads the cached table for this device, or tunes ``sizes`` and caches the result."""
-    if load(path):
-        return None
-    table = tune_permanents(sizes, method, log=log)
+def load(path: Path | None = None, key: dict | None = None) -> bool:
+    """Applies the cached tables if they exist and were made for this device and build."""
+    path = Path(path) if path else default_cache_path()
+    tables = _cached(path, key if key is not None else device_key())
+    return sum(apply(t) for t in tables) > 0
+
+
+def ensure_tuned(sizes=range(8, 27), method: int = 0, path: Path | None = None, log=None,
+                 precision="fp64") -> dict | None:
+    """Loads the cached table of (method, arithmetic) for this device, or tunes ``sizes``
+    and caches the result."""
+    path = Path(path) if path else default_cache_path()
+    name = "fp64" if _native.precision_code(precision) == _native.PREC_FP64 else "float-float"
+    tables = _cached(path, device_key())
+    for t in tables:
+        if int(t.get("method", 0)) == method and t.get("precision", "float-float") == name:
+            apply(t)
+            return None
+    table = tune_permanents(sizes, method, log=log, precision=precision)
     save(table, path)
     return table

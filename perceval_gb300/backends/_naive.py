@@ -5,7 +5,9 @@
 _naive.py:51-68) and evaluates its permanent on the GPU, divided by
 sqrt(prod out! * prod in!); the 1 x 1 case returns the element itself (:46-49).
 ``prob_amplitudes`` batches many outputs into one ``pcvl_permanent_batch`` call; the
-full-space methods (``all_prob``, ``prob_distribution``, ``evolve``) use it.
+full-space methods (``all_prob``, ``prob_distribution``, ``evolve``) use it.  The
+permanents are computed in native FP64, the reference's arithmetic; ``precision=
+"float-float"`` selects the faster FP32-pipe pairs (about 48 significant bits).
 """
 from __future__ import annotations
 
@@ -26,11 +28,14 @@ def _expand(state) -> np.ndarray:
 class NaiveBackend(AStrongSimulationBackend):
     """Naive algorithm: no cached calculation path, every output recomputed."""
 
-    def __init__(self, method: str = "glynn"):
+    def __init__(self, method: str = "glynn", precision: str = "fp64"):
         super().__init__()
         if method not in ("glynn", "ryser"):
             raise ValueError("method must be 'glynn' or 'ryser'")
         self._method = 0 if method == "glynn" else 1
+        self._precision = _native.precision_code(precision)
+        if self._precision not in (_native.PREC_FP64, _native.PREC_FLOAT_FLOAT):
+            raise ValueError("precision must be 'fp64' or 'float-float'")
 
     @property
     def name(self) -> str:
@@ -92,7 +97,7 @@ class NaiveBackend(AStrongSimulationBackend):
         """Permanents of packed matrices, one batched launch (_naive.py:70-71)."""
         dev = torch.from_numpy(flat).to("cuda")
         out = torch.empty(len(sizes), dtype=torch.complex128, device="cuda")
-        _native.permanent_batch(dev, offs, sizes, out, self._method)
+        _native.permanent_batch(dev, offs, sizes, out, self._method, precision=self._precision)
         return out.cpu().numpy()
 
     def all_prob(self, input_state=None):

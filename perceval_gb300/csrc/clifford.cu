@@ -579,8 +579,9 @@ static int cc2017_run(const double* u_d, int32_t m, int32_t nstates, const int32
   const size_t o_cexp = o_rows + st_bytes;
   const size_t o_part = o_cexp + st_bytes;
   const size_t total = o_part + (size_t)W * max_chunks * kMaxPhotons * sizeof(double2);
+  ScratchGuard scratch(s);
   void* ws = nullptr;
-  PCVL_TRY(workspace(WS_CC2017, total, &ws));
+  PCVL_TRY(scratch.alloc(total, &ws));
   unsigned char* base = (unsigned char*)ws;
   {
     // one staged upload: the columns of every state, then the state offsets

@@ -309,8 +309,9 @@ extern "C" int pcvl_permanent_estimate_batch(const double* mats_d, const int64_t
   std::vector<unsigned char> blob(o_part - o_desc, 0);
   memcpy(blob.data(), descs.data(), (size_t)count * sizeof(GvDesc));
   if (!cta_mat.empty()) memcpy(blob.data() + o_cta, cta_mat.data(), cta_mat.size() * 4);
+  ScratchGuard scratch(s);
   void* ws = nullptr;
-  PCVL_TRY(workspace(WS_GURVITS, total, &ws));
+  PCVL_TRY(scratch.alloc(total, &ws));
   unsigned char* base = (unsigned char*)ws;
   PCVL_TRY(stage_h2d(blob.data(), blob.size(), base, s));
   const GvDesc* descs_d = (const GvDesc*)(base + o_desc);

@@ -5,10 +5,12 @@
 // Flow of pcvl_permanent_batch:
 //  1. perm_prepare: every row i of every matrix is scaled by an exact power of two
 //     2^{e_i} so that its l1 norm lies in [2^{c-1}, 2^c), c = min(20, 120 / n); then
-//     every |row sum| <= 2^c and every row-sum product stays inside the FP32 range.
-//     The scaled matrix is stored as float-float pairs; sum_i e_i is kept.
-//  2. one perm_bin_kernel<n> launch per distinct size n, each CTA handling a chunk
-//     of Gray-code hi patterns of one matrix and writing one FP64 partial.
+//     every |row sum| <= 2^c and every row-sum product stays inside the FP32 range
+//     (and far inside the FP64 range).  The scaled matrix is stored as double2 (FP64)
+//     or float-float pairs; sum_i e_i is kept.
+//  2. one bin launch per distinct size n (perm_bin_f64<n> or perm_bin_kernel<n>),
+//     each CTA handling a chunk of hi sign patterns of one matrix and writing one FP64
+//     partial.
 //  3. perm_reduce: per matrix, Neumaier-compensated FP64 sum of its partials, times
 //     2^{1-n} (Glynn) or (-1)^n (Ryser), times 2^{-sum e_i}.
 #include <algorithm>
@@ -29,8 +31,12 @@ struct PermDesc {
   int32_t n;
 };
 
+__device__ __forceinline__ void store_prepared(cdd* dst, double re, double im) { *dst = cdd_from(re, im); }
+__device__ __forceinline__ void store_prepared(double2* dst, double re, double im) { *dst = make_double2(re, im); }
+
+template <typename E>
 __global__ void perm_prepare(const double2* __restrict__ src, const int64_t* __restrict__ offs,
-                             const int32_t* __restrict__ sizes, int32_t count, cdd* __restrict__ dst,
+                             const int32_t* __restrict__ sizes, int32_t count, E* __restrict__ dst,
                              int32_t* __restrict__ exps) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -58,7 +64,7 @@ __global__ void perm_prepare(const double2* __restrict__ src, const int64_t* __r
     esum += e;
     for (int j = 0; j < n; ++j) {
       const double2 v = src[off + (int64_t)i * n + j];
-      dst[off + (int64_t)i * n + j] = cdd_from(ldexp(v.x, e), ldexp(v.y, e));
+      store_prepared(&dst[off + (int64_t)i * n + j], ldexp(v.x, e), ldexp(v.y, e));
     }
   }
 #pragma unroll
@@ -112,10 +118,27 @@ static int launch_bin(int n, const PermBinArgs& a, PermNode* node = nullptr) {
   return launch_perm_bin_37_40(n, a, node);
 }
 
-// Tuning table: per method and size, the lo bits and the target CTAs per SM of a bin,
-// packed as (L + 1) | ctas << 8 (0 in a field: the built-in choice).  Written by
-// pcvl_perm_set_tuning (the autotuner), read without locks by every launch.
-static std::atomic<uint32_t> g_tune[2][kPermMaxN + 1];
+// Tuning table: per arithmetic (0 float-float, 1 FP64), method and size, the lo bits and
+// the target CTAs per SM of a bin, packed as (L + 1) | ctas << 8 (0 in a field: the
+// built-in choice).  Written by pcvl_perm_set_tuning (the autotuner), read without locks
+// by every launch.
+static std::atomic<uint32_t> g_tune[2][2][kPermMaxN + 1];
+
+static int prec_slot(int prec) { return prec == kPrecFP64 ? 1 : 0; }
+
+// prepare kernel of an arithmetic (prepared elements: double2 for FP64, cdd otherwise)
+static void* prepare_func(int prec) {
+  return prec == kPrecFP64 ? reinterpret_cast<void*>(perm_prepare<double2>)
+                           : reinterpret_cast<void*>(perm_prepare<cdd>);
+}
+
+static void launch_prepare(int prec, unsigned blocks, cudaStream_t stream, const double2* src, const int64_t* offs,
+                           const int32_t* sizes, int32_t count, void* prep, int32_t* exps) {
+  if (prec == kPrecFP64)
+    perm_prepare<double2><<<blocks, 256, 0, stream>>>(src, offs, sizes, count, (double2*)prep, exps);
+  else
+    perm_prepare<cdd><<<blocks, 256, 0, stream>>>(src, offs, sizes, count, (cdd*)prep, exps);
+}
 
 constexpr int kDefaultCtasPerSm = 8;
 constexpr size_t kMaxPermSmem = 227 * 1024;
@@ -128,8 +151,8 @@ struct BinShape {
   int64_t P, items_per_mat;
 };
 
-static BinShape bin_shape(int n, int ryser, int64_t nmat, int sms) {
-  const uint32_t t = g_tune[ryser][n].load(std::memory_order_relaxed);
+static BinShape bin_shape(int n, int ryser, int prec, int64_t nmat, int sms) {
+  const uint32_t t = g_tune[prec_slot(prec)][ryser][n].load(std::memory_order_relaxed);
   const int F = ryser ? n : n - 1;  // free bits
   const int tl = (int)(t & 0xffu) - 1;
   const int tc = (int)((t >> 8) & 0xffu);
@@ -153,15 +176,15 @@ struct BinPlan {
   std::vector<int32_t> mids;
 };
 
-static void plan_bin(BinPlan& b, int ryser, int sms) {
-  const BinShape s = bin_shape(b.n, ryser, (int64_t)b.mids.size(), sms);
+static void plan_bin(BinPlan& b, int ryser, int prec, int sms) {
+  const BinShape s = bin_shape(b.n, ryser, prec, (int64_t)b.mids.size(), sms);
   b.L = s.L;
   b.Hbits = s.Hbits;
   b.P = s.P;
   b.items_per_mat = s.items_per_mat;
 }
 
-// Device layout of one batch: [prepared cdd][exps][offs][sizes][mids][descs][partials];
+// Device layout of one batch: [prepared elements][exps][offs][sizes][mids][descs][partials];
 // the small arrays travel as one host blob covering [offs, partials).
 struct BatchLayout {
   std::vector<BinPlan> bins;  // indexed by n; empty bins have no mids
@@ -171,7 +194,37 @@ struct BatchLayout {
   std::vector<unsigned char> blob;
 };
 
-static int make_layout(const int64_t* offsets_h, const int32_t* sizes_h, int32_t count, int ryser,
+// The prepare kernel writes each scaled matrix over the caller's offsets, so two
+// matrices may share elements only as identical entries (same offset and size).  One
+// linear pass accepts the usual packed, ascending layout; otherwise `order` (count
+// entries of scratch) is sorted by offset.
+static int check_no_overlap(const int64_t* offs, const int32_t* sizes, int32_t count, int32_t* order) {
+  bool sorted = true;
+  int64_t end = 0;
+  for (int i = 0; i < count && sorted; ++i) {
+    if (sizes[i] == 0) continue;
+    if (offs[i] < end) sorted = false;
+    end = offs[i] + (int64_t)sizes[i] * sizes[i];
+  }
+  if (sorted) return PCVL_OK;
+  int32_t k = 0;
+  for (int i = 0; i < count; ++i)
+    if (sizes[i] > 0) order[k++] = i;
+  std::sort(order, order + k, [&](int32_t a, int32_t b) {
+    return offs[a] != offs[b] ? offs[a] < offs[b] : sizes[a] < sizes[b];
+  });
+  for (int32_t q = 1; q < k; ++q) {
+    const int32_t a = order[q - 1], b = order[q];
+    if (offs[a] == offs[b] && sizes[a] == sizes[b]) continue;
+    PCVL_CHECK(offs[b] >= offs[a] + (int64_t)sizes[a] * sizes[a],
+               "matrices %d and %d overlap in mats (offsets %lld and %lld): matrices may share elements only as "
+               "identical entries (same offset and size)",
+               a, b, (long long)offs[a], (long long)offs[b]);
+  }
+  return PCVL_OK;
+}
+
+static int make_layout(const int64_t* offsets_h, const int32_t* sizes_h, int32_t count, int ryser, int prec,
                        BatchLayout& L) {
   L.bins.assign(kPermMaxN + 1, BinPlan());
   for (int i = 0; i < count; ++i) {
@@ -181,19 +234,23 @@ static int make_layout(const int64_t* offsets_h, const int32_t* sizes_h, int32_t
     L.total_elems = std::max<int64_t>(L.total_elems, offsets_h[i] + (int64_t)n * n);
     if (n > 0) L.bins[n].mids.push_back(i);
   }
+  {
+    std::vector<int32_t> order(count);
+    PCVL_TRY(check_no_overlap(offsets_h, sizes_h, count, order.data()));
+  }
   const int sms = num_sms();
   L.descs.assign(count, PermDesc{0, 0, 0});
   for (int n = 1; n <= kPermMaxN; ++n) {
     BinPlan& b = L.bins[n];
     if (b.mids.empty()) continue;
     b.n = n;
-    plan_bin(b, ryser, sms);
+    plan_bin(b, ryser, prec, sms);
     for (size_t k = 0; k < b.mids.size(); ++k)
       L.descs[b.mids[k]] = {L.total_items + (int64_t)k * b.items_per_mat, (int32_t)b.items_per_mat, n};
     L.total_items += (int64_t)b.mids.size() * b.items_per_mat;
   }
   L.o_prep = 0;
-  L.o_exps = align_up(L.o_prep + (size_t)L.total_elems * sizeof(cdd), 256);
+  L.o_exps = align_up(L.o_prep + (size_t)L.total_elems * sizeof(double2), 256);
   L.o_offs = align_up(L.o_exps + (size_t)count * 4, 256);
   L.o_size = align_up(L.o_offs + (size_t)count * 8, 256);
   L.o_mids = align_up(L.o_size + (size_t)count * 4, 256);
@@ -213,11 +270,11 @@ static int make_layout(const int64_t* offsets_h, const int32_t* sizes_h, int32_t
 }
 
 // Bin kernel arguments of a layout placed at device address base.
-static PermBinArgs bin_args(const BatchLayout& L, unsigned char* base, int n, int64_t mid_off, int ryser,
+static PermBinArgs bin_args(const BatchLayout& L, unsigned char* base, int n, int64_t mid_off, int ryser, int prec,
                             cudaStream_t stream) {
   const BinPlan& b = L.bins[n];
   PermBinArgs a;
-  a.A = (const cdd*)(base + L.o_prep);
+  a.A = base + L.o_prep;
   a.offs = (const int64_t*)(base + L.o_offs);
   a.mids = (const int32_t*)(base + L.o_mids) + mid_off;
   a.nmat = (int32_t)b.mids.size();
@@ -226,6 +283,7 @@ static PermBinArgs bin_args(const BatchLayout& L, unsigned char* base, int n, in
   a.P = b.P;
   a.items_per_mat = b.items_per_mat;
   a.ryser = ryser;
+  a.prec = prec;
   a.partials = (double2*)(base + L.o_part) + L.descs[b.mids[0]].base;
   a.stream = stream;
   return a;
@@ -235,37 +293,42 @@ static PermBinArgs bin_args(const BatchLayout& L, unsigned char* base, int n, in
 
 using namespace pcvl;
 
+#define PCVL_CHECK_PERM_PREC(p)                                                                        \
+  PCVL_CHECK((p) == PCVL_PREC_FP64 || (p) == PCVL_PREC_FLOAT_FLOAT,                                       \
+             "precision must be %d (FP64) or %d (float-float), got %d", PCVL_PREC_FP64, PCVL_PREC_FLOAT_FLOAT, \
+             (p))
+
 extern "C" int pcvl_permanent_batch(const double* mats_d, const int64_t* offsets_h, const int32_t* sizes_h,
-                                    int32_t count, double* out_d, int32_t method, void* stream_) {
+                                    int32_t count, double* out_d, int32_t method, int32_t precision, void* stream_) {
   cudaStream_t stream = (cudaStream_t)stream_;
   PCVL_CHECK(count >= 0, "count must be >= 0 (got %d)", count);
   if (count == 0) return PCVL_OK;
   PCVL_CHECK(mats_d && offsets_h && sizes_h && out_d, "null pointer argument");
   PCVL_CHECK(method == 0 || method == 1, "method must be 0 (Glynn) or 1 (Ryser), got %d", method);
+  PCVL_CHECK_PERM_PREC(precision);
   const int ryser = method;
   BatchLayout L;
-  PCVL_TRY(make_layout(offsets_h, sizes_h, count, ryser, L));
+  PCVL_TRY(make_layout(offsets_h, sizes_h, count, ryser, precision, L));
+  ScratchGuard scratch(stream);
   void* ws = nullptr;
-  PCVL_TRY(workspace(WS_PERM, L.total, &ws));
+  PCVL_TRY(scratch.alloc(L.total, &ws));
   unsigned char* base = (unsigned char*)ws;
   PCVL_TRY(stage_h2d(L.blob.data(), L.blob.size(), base + L.o_offs, stream));
 
-  cdd* prep = (cdd*)(base + L.o_prep);
   int32_t* exps_d = (int32_t*)(base + L.o_exps);
   const int64_t* offs_d = (const int64_t*)(base + L.o_offs);
   const int32_t* sizes_d = (const int32_t*)(base + L.o_size);
   const PermDesc* descs_d = (const PermDesc*)(base + L.o_desc);
   double2* parts = (double2*)(base + L.o_part);
   {
-    const int threads = 256;
-    const int blocks = (int)(((int64_t)count * 32 + threads - 1) / threads);
-    perm_prepare<<<blocks, threads, 0, stream>>>((const double2*)mats_d, offs_d, sizes_d, count, prep, exps_d);
+    const unsigned blocks = (unsigned)(((int64_t)count * 32 + 255) / 256);
+    launch_prepare(precision, blocks, stream, (const double2*)mats_d, offs_d, sizes_d, count, base + L.o_prep, exps_d);
     PCVL_CUDA(cudaGetLastError());
   }
   int64_t mid_off = 0;
   for (int n = 1; n <= kPermMaxN; ++n) {
     if (L.bins[n].mids.empty()) continue;
-    const PermBinArgs a = bin_args(L, base, n, mid_off, ryser, stream);
+    const PermBinArgs a = bin_args(L, base, n, mid_off, ryser, precision, stream);
     const int rc = launch_bin(n, a);
     if (rc != 0) {
       set_error("permanent kernel launch for n=%d failed: %s", n, cudaGetErrorString((cudaError_t)rc));
@@ -279,27 +342,32 @@ extern "C" int pcvl_permanent_batch(const double* mats_d, const int64_t* offsets
 }
 
 // ------------------------------------------------------------------ tuning
-extern "C" int pcvl_perm_set_tuning(int32_t method, int32_t n, int32_t lo_bits, int32_t ctas_per_sm) {
+extern "C" int pcvl_perm_set_tuning(int32_t method, int32_t precision, int32_t n, int32_t lo_bits,
+                                    int32_t ctas_per_sm) {
   PCVL_CHECK(method == 0 || method == 1, "method must be 0 (Glynn) or 1 (Ryser), got %d", method);
+  PCVL_CHECK_PERM_PREC(precision);
   PCVL_CHECK(n >= 1 && n <= kPermMaxN, "n=%d outside [1, %d]", n, kPermMaxN);
   PCVL_CHECK(lo_bits >= -1 && lo_bits <= 12, "lo_bits=%d outside [-1, 12]", lo_bits);
   PCVL_CHECK(ctas_per_sm >= 0 && ctas_per_sm <= 64, "ctas_per_sm=%d outside [0, 64]", ctas_per_sm);
   if (lo_bits >= 0) {
     const int F = method ? n : n - 1;
     const int l = std::min(lo_bits, F);
-    const size_t smem = (size_t)(n * n + (1 << l) * n) * sizeof(cdd);
+    const size_t smem = (size_t)(n * n + (1 << l) * n) * sizeof(double2);
     PCVL_CHECK(smem <= kMaxPermSmem, "n=%d with %d lo bits needs %zu bytes of shared memory (max %zu)", n, l, smem,
                kMaxPermSmem);
   }
-  g_tune[method][n].store((uint32_t)(lo_bits + 1) | ((uint32_t)ctas_per_sm << 8), std::memory_order_relaxed);
+  g_tune[prec_slot(precision)][method][n].store((uint32_t)(lo_bits + 1) | ((uint32_t)ctas_per_sm << 8),
+                                                std::memory_order_relaxed);
   return PCVL_OK;
 }
 
-extern "C" int pcvl_perm_get_tuning(int32_t method, int32_t n, int32_t* lo_bits, int32_t* ctas_per_sm) {
+extern "C" int pcvl_perm_get_tuning(int32_t method, int32_t precision, int32_t n, int32_t* lo_bits,
+                                    int32_t* ctas_per_sm) {
   PCVL_CHECK(method == 0 || method == 1, "method must be 0 (Glynn) or 1 (Ryser), got %d", method);
+  PCVL_CHECK_PERM_PREC(precision);
   PCVL_CHECK(n >= 1 && n <= kPermMaxN, "n=%d outside [1, %d]", n, kPermMaxN);
   PCVL_CHECK(lo_bits && ctas_per_sm, "null pointer argument");
-  const uint32_t t = g_tune[method][n].load(std::memory_order_relaxed);
+  const uint32_t t = g_tune[prec_slot(precision)][method][n].load(std::memory_order_relaxed);
   const int F = method ? n : n - 1;
   const int tl = (int)(t & 0xffu) - 1;
   const int tc = (int)((t >> 8) & 0xffu);
@@ -315,7 +383,7 @@ extern "C" int pcvl_perm_get_tuning(int32_t method, int32_t n, int32_t* lo_bits,
 // Executing again only updates the input and output pointers of the first and last
 // nodes and relaunches the graph.
 struct pcvl_perm_plan {
-  int device = 0, count = 0, ryser = 0;
+  int device = 0, count = 0, ryser = 0, prec = 0;
   size_t bytes = 0;
   unsigned char* dev = nullptr;
   cudaGraph_t graph = nullptr;
@@ -326,7 +394,7 @@ struct pcvl_perm_plan {
   const double2* src = nullptr;
   const int64_t* offs_d = nullptr;
   const int32_t* sizes_d = nullptr;
-  cdd* prep = nullptr;
+  void* prep = nullptr;
   int32_t* exps_d = nullptr;
   double2* parts = nullptr;
   const PermDesc* descs_d = nullptr;
@@ -351,7 +419,7 @@ cudaKernelNodeParams prep_params(pcvl_perm_plan* p, void** args) {
   args[4] = &p->prep;
   args[5] = &p->exps_d;
   cudaKernelNodeParams kp{};
-  kp.func = reinterpret_cast<void*>(perm_prepare);
+  kp.func = prepare_func(p->prec);
   kp.gridDim = dim3(p->prep_blocks);
   kp.blockDim = dim3(256);
   kp.sharedMemBytes = 0;
@@ -378,18 +446,20 @@ cudaKernelNodeParams red_params(pcvl_perm_plan* p, void** args) {
 }  // namespace
 
 extern "C" int pcvl_perm_plan_create(pcvl_perm_plan** plan, const int64_t* offsets_h, const int32_t* sizes_h,
-                                     int32_t count, int32_t method) {
+                                     int32_t count, int32_t method, int32_t precision) {
   PCVL_CHECK(plan, "null plan pointer");
   *plan = nullptr;
   PCVL_CHECK(offsets_h && sizes_h, "null pointer argument");
   PCVL_CHECK(count >= 1, "a plan needs at least one matrix (got %d)", count);
   PCVL_CHECK(method == 0 || method == 1, "method must be 0 (Glynn) or 1 (Ryser), got %d", method);
+  PCVL_CHECK_PERM_PREC(precision);
   BatchLayout L;
-  PCVL_TRY(make_layout(offsets_h, sizes_h, count, method, L));
+  PCVL_TRY(make_layout(offsets_h, sizes_h, count, method, precision, L));
   pcvl_perm_plan* p = new (std::nothrow) pcvl_perm_plan();
   PCVL_CHECK(p, "out of host memory");
   p->count = count;
   p->ryser = method;
+  p->prec = precision;
   p->bytes = L.total;
   cudaError_t e = cudaGetDevice(&p->device);
   if (e == cudaSuccess) e = cudaMalloc(&p->dev, L.total);
@@ -401,7 +471,7 @@ extern "C" int pcvl_perm_plan_create(pcvl_perm_plan** plan, const int64_t* offse
   e = cudaMemcpy(p->dev + L.o_offs, L.blob.data(), L.blob.size(), cudaMemcpyHostToDevice);
   p->offs_d = (const int64_t*)(p->dev + L.o_offs);
   p->sizes_d = (const int32_t*)(p->dev + L.o_size);
-  p->prep = (cdd*)(p->dev + L.o_prep);
+  p->prep = p->dev + L.o_prep;
   p->exps_d = (int32_t*)(p->dev + L.o_exps);
   p->parts = (double2*)(p->dev + L.o_part);
   p->descs_d = (const PermDesc*)(p->dev + L.o_desc);
@@ -418,7 +488,7 @@ extern "C" int pcvl_perm_plan_create(pcvl_perm_plan** plan, const int64_t* offse
   int64_t mid_off = 0;
   for (int n = 1; n <= kPermMaxN && e == cudaSuccess; ++n) {
     if (L.bins[n].mids.empty()) continue;
-    PermBinArgs a = bin_args(L, p->dev, n, mid_off, method, nullptr);
+    PermBinArgs a = bin_args(L, p->dev, n, mid_off, method, precision, nullptr);
     PermNode nd{};
     const int rc = launch_bin(n, a, &nd);
     if (rc != 0) {
@@ -493,25 +563,25 @@ extern "C" int pcvl_perm_plan_destroy(pcvl_perm_plan* p) {
 namespace pcvl {
 namespace noalloc {
 
-constexpr int64_t kMaxElems = int64_t(3) << 20;  // matrix elements per call (48 MiB as float-float)
+constexpr size_t align_up_c(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+constexpr int64_t kMaxElems = int64_t(3) << 20;  // matrix elements per call (48 MiB prepared, 16 B each)
 constexpr int32_t kMaxCount = 16384;             // matrices per call
 constexpr int64_t kMaxItems = int64_t(1) << 17;  // CTA partial sums per call (2 MiB)
 
 constexpr size_t kPrep = 0;
-constexpr size_t kExps = kPrep + (size_t)kMaxElems * sizeof(cdd);
+constexpr size_t kExps = kPrep + (size_t)kMaxElems * sizeof(double2);
 constexpr size_t kOffs = kExps + (size_t)kMaxCount * 4;
-constexpr size_t kSize = kOffs + (size_t)kMaxCount * 8;
-constexpr size_t kMids = kSize + (size_t)kMaxCount * 4;
-constexpr size_t kDesc = kMids + (size_t)kMaxCount * 4;
-constexpr size_t kPart = kDesc + (size_t)kMaxCount * sizeof(PermDesc);
+// offsets, sizes, matrix ids by size and descriptors of one call, packed by count
+constexpr size_t kDescBytes = 3 * 256 + (size_t)kMaxCount * (8 + 4 + 4 + sizeof(PermDesc));
+constexpr size_t kPart = align_up_c(kOffs + kDescBytes, 256);
 constexpr size_t kBytes = kPart + (size_t)kMaxItems * sizeof(double2);
-static_assert(kExps % 256 == 0 && kOffs % 256 == 0 && kSize % 256 == 0 && kMids % 256 == 0 &&
-                  kDesc % 256 == 0 && kPart % 256 == 0,
-              "scratch regions stay 256-byte aligned");
+static_assert(kExps % 256 == 0 && kOffs % 256 == 0 && kPart % 256 == 0, "scratch regions stay 256-byte aligned");
 
 constexpr int kMaxDevices = 64;
 void* g_dev_ptr[kMaxDevices] = {};
-unsigned char g_host_blob[kPart - kOffs];  // offsets, sizes, mids, descriptors of one call
+unsigned char g_host_blob[kDescBytes];  // offsets, sizes, mids, descriptors of one call
+int32_t g_order[kMaxCount];               // matrix order of the overlap check
 std::mutex g_mu;
 
 }  // namespace noalloc
@@ -542,13 +612,14 @@ static int noalloc_scratch(unsigned char** ptr) {
 
 extern "C" int pcvl_permanent_batch_noalloc(const double* mats_d, const int64_t* offsets_h,
                                             const int32_t* sizes_h, int32_t count, double* out_d,
-                                            int32_t method, void* stream_) {
+                                            int32_t method, int32_t precision, void* stream_) {
   using namespace pcvl::noalloc;
   cudaStream_t stream = (cudaStream_t)stream_;
   PCVL_CHECK(count >= 0, "count must be >= 0 (got %d)", count);
   if (count == 0) return PCVL_OK;
   PCVL_CHECK(mats_d && offsets_h && sizes_h && out_d, "null pointer argument");
   PCVL_CHECK(method == 0 || method == 1, "method must be 0 (Glynn) or 1 (Ryser), got %d", method);
+  PCVL_CHECK_PERM_PREC(precision);
   PCVL_CHECK(count <= kMaxCount, "allocation-free permanents: %d matrices exceed the maximum of %d per call",
              count, kMaxCount);
   const int ryser = method;
@@ -575,7 +646,7 @@ extern "C" int pcvl_permanent_batch_noalloc(const double* mats_d, const int64_t*
     mid_base[n] = mids_so_far;
     item_base[n] = total_items;
     if (bin_count[n] == 0) continue;
-    const BinShape sh = bin_shape(n, ryser, bin_count[n], sms);
+    const BinShape sh = bin_shape(n, ryser, precision, bin_count[n], sms);
     L[n] = sh.L;
     Hb[n] = sh.Hbits;
     P[n] = sh.P;
@@ -588,14 +659,21 @@ extern "C" int pcvl_permanent_batch_noalloc(const double* mats_d, const int64_t*
              (long long)total_items, (long long)kMaxItems);
 
   std::lock_guard<std::mutex> lock(g_mu);
+  PCVL_TRY(check_no_overlap(offsets_h, sizes_h, count, g_order));
   unsigned char* scratch = nullptr;
   PCVL_TRY(noalloc_scratch(&scratch));
 
-  // descriptors into the static host buffer (same layout as the device region [kOffs, kPart))
-  int64_t* h_offs = (int64_t*)(g_host_blob + (kOffs - kOffs));
-  int32_t* h_size = (int32_t*)(g_host_blob + (kSize - kOffs));
-  int32_t* h_mids = (int32_t*)(g_host_blob + (kMids - kOffs));
-  PermDesc* h_desc = (PermDesc*)(g_host_blob + (kDesc - kOffs));
+  // descriptors of this call packed at the start of the static host buffer: offsets,
+  // sizes, matrix ids by size, descriptors (each region 256-byte aligned, sized by count),
+  // so one copy of about 24 bytes per matrix travels, not the whole descriptor region
+  const size_t r_size = align_up((size_t)count * 8, 256);
+  const size_t r_mids = r_size + align_up((size_t)count * 4, 256);
+  const size_t r_desc = r_mids + align_up((size_t)count * 4, 256);
+  const size_t r_end = r_desc + (size_t)count * sizeof(PermDesc);
+  int64_t* h_offs = (int64_t*)g_host_blob;
+  int32_t* h_size = (int32_t*)(g_host_blob + r_size);
+  int32_t* h_mids = (int32_t*)(g_host_blob + r_mids);
+  PermDesc* h_desc = (PermDesc*)(g_host_blob + r_desc);
   int64_t fill[kPermMaxN + 1];
   for (int n = 0; n <= kPermMaxN; ++n) fill[n] = 0;
   for (int i = 0; i < count; ++i) {
@@ -611,25 +689,24 @@ extern "C" int pcvl_permanent_batch_noalloc(const double* mats_d, const int64_t*
     h_desc[i] = {item_base[n] + k * ipm[n], (int32_t)ipm[n], n};
   }
   // pageable source: the call returns once the bytes are staged, so the buffer is reusable
-  PCVL_CUDA(cudaMemcpyAsync(scratch + kOffs, g_host_blob, kPart - kOffs, cudaMemcpyHostToDevice, stream));
+  PCVL_CUDA(cudaMemcpyAsync(scratch + kOffs, g_host_blob, r_end, cudaMemcpyHostToDevice, stream));
 
-  cdd* prep = (cdd*)(scratch + kPrep);
   int32_t* exps_d = (int32_t*)(scratch + kExps);
   const int64_t* offs_d = (const int64_t*)(scratch + kOffs);
-  const int32_t* sizes_d = (const int32_t*)(scratch + kSize);
-  int32_t* mids_d = (int32_t*)(scratch + kMids);
-  const PermDesc* descs_d = (const PermDesc*)(scratch + kDesc);
+  const int32_t* sizes_d = (const int32_t*)(scratch + kOffs + r_size);
+  int32_t* mids_d = (int32_t*)(scratch + kOffs + r_mids);
+  const PermDesc* descs_d = (const PermDesc*)(scratch + kOffs + r_desc);
   double2* parts = (double2*)(scratch + kPart);
   {
-    const int threads = 256;
-    const int blocks = (int)(((int64_t)count * 32 + threads - 1) / threads);
-    perm_prepare<<<blocks, threads, 0, stream>>>((const double2*)mats_d, offs_d, sizes_d, count, prep, exps_d);
+    const unsigned blocks = (unsigned)(((int64_t)count * 32 + 255) / 256);
+    launch_prepare(precision, blocks, stream, (const double2*)mats_d, offs_d, sizes_d, count, scratch + kPrep,
+                   exps_d);
     PCVL_CUDA(cudaGetLastError());
   }
   for (int n = 1; n <= kPermMaxN; ++n) {
     if (bin_count[n] == 0) continue;
     PermBinArgs a;
-    a.A = prep;
+    a.A = scratch + kPrep;
     a.offs = offs_d;
     a.mids = mids_d + mid_base[n];
     a.nmat = bin_count[n];
@@ -638,6 +715,7 @@ extern "C" int pcvl_permanent_batch_noalloc(const double* mats_d, const int64_t*
     a.P = P[n];
     a.items_per_mat = ipm[n];
     a.ryser = ryser;
+    a.prec = precision;
     a.partials = parts + item_base[n];
     a.stream = stream;
     const int rc = launch_bin(n, a);

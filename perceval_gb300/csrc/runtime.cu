@@ -17,38 +17,42 @@ void set_error(const char* fmt, ...) {
 
 namespace {
 constexpr int kMaxDevices = 64;
-struct Buf {
-  void* ptr = nullptr;
-  size_t bytes = 0;
-};
-Buf g_ws[kMaxDevices][WS_SLOTS];
-std::mutex g_ws_mu;
+cudaMemPool_t g_pool[kMaxDevices] = {};
+std::mutex g_pool_mu;
+
+int device_pool(int dev, cudaMemPool_t* pool) {
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  if (!g_pool[dev]) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p = nullptr;
+    PCVL_CUDA(cudaMemPoolCreate(&p, &props));
+    uint64_t keep = ~0ull;  // freed blocks stay in the pool for the next call
+    PCVL_CUDA(cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep));
+    g_pool[dev] = p;
+  }
+  *pool = g_pool[dev];
+  return PCVL_OK;
+}
 }  // namespace
 
-int workspace(int slot, size_t bytes, void** ptr) {
+int scratch_alloc(size_t bytes, cudaStream_t stream, void** ptr) {
+  *ptr = nullptr;
   int dev = 0;
   PCVL_CUDA(cudaGetDevice(&dev));
-  PCVL_CHECK(dev >= 0 && dev < kMaxDevices && slot >= 0 && slot < WS_SLOTS, "bad workspace slot");
-  std::lock_guard<std::mutex> lock(g_ws_mu);
-  Buf& b = g_ws[dev][slot];
-  if (b.bytes < bytes) {
-    if (b.ptr) {
-      // the old buffer may still be read by work queued on any stream
-      PCVL_CUDA(cudaDeviceSynchronize());
-      PCVL_CUDA(cudaFree(b.ptr));
-      b.ptr = nullptr;
-      b.bytes = 0;
-    }
-    size_t want = bytes < 4096 ? 4096 : bytes;
-    cudaError_t e = cudaMalloc(&b.ptr, want);
-    if (e != cudaSuccess) {
-      b.ptr = nullptr;
-      set_error("workspace allocation of %zu bytes failed: %s", want, cudaGetErrorString(e));
-      return PCVL_ERR_MEMORY;
-    }
-    b.bytes = want;
+  PCVL_CHECK(dev >= 0 && dev < kMaxDevices, "device index %d out of range", dev);
+  cudaMemPool_t pool = nullptr;
+  PCVL_TRY(device_pool(dev, &pool));
+  const size_t want = bytes < 4096 ? 4096 : bytes;
+  cudaError_t e = cudaMallocFromPoolAsync(ptr, want, pool, stream);
+  if (e != cudaSuccess) {
+    *ptr = nullptr;
+    set_error("scratch allocation of %zu bytes failed: %s", want, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? PCVL_ERR_MEMORY : PCVL_ERR_CUDA;
   }
-  *ptr = b.ptr;
   return PCVL_OK;
 }
 
@@ -96,7 +100,7 @@ int stage_h2d(const void* src, size_t bytes, void* dst_d, cudaStream_t stream) {
 
 }  // namespace pcvl
 
-extern "C" const char* pcvl_version(void) { return "pcvl_gb300 0.1.0 sm_103a"; }
+extern "C" const char* pcvl_version(void) { return "pcvl_gb300 0.2.0 sm_103a"; }
 
 extern "C" int pcvl_last_error(char* buf, size_t len) {
   if (!buf || len == 0) return PCVL_ERR_ARG;
@@ -108,13 +112,9 @@ extern "C" int pcvl_last_error(char* buf, size_t len) {
 extern "C" int pcvl_release_workspace(void) {
   int dev = 0;
   PCVL_CUDA(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lock(pcvl::g_ws_mu);
+  PCVL_CHECK(dev >= 0 && dev < pcvl::kMaxDevices, "device index %d out of range", dev);
+  std::lock_guard<std::mutex> lock(pcvl::g_pool_mu);
   PCVL_CUDA(cudaDeviceSynchronize());
-  for (int s = 0; s < pcvl::WS_SLOTS; ++s) {
-    auto& b = pcvl::g_ws[dev][s];
-    if (b.ptr) PCVL_CUDA(cudaFree(b.ptr));
-    b.ptr = nullptr;
-    b.bytes = 0;
-  }
+  if (pcvl::g_pool[dev]) PCVL_CUDA(cudaMemPoolTrimTo(pcvl::g_pool[dev], 0));
   return PCVL_OK;
 }

@@ -37,12 +37,31 @@ void set_error(const char* fmt, ...);
     if (_s != PCVL_OK) return _s; \
   } while (0)
 
-// Workspace cached per (device, slot); grown on demand, freed by
-// pcvl_release_workspace().  Slots let independent kernels keep their buffers.
-enum WorkspaceSlot {
-  WS_PERM = 0, WS_PERM_ITEMS = 1, WS_CC2017 = 2, WS_GURVITS = 3, WS_SLAP = 4, WS_MASK = 5, WS_SLOTS = 6
+// Scratch of one call, stream-ordered: taken from the library's memory pool of the
+// current device on `stream` and handed back on the same stream after the work queued
+// by the call (ScratchGuard does both), so calls on different streams or host threads
+// never share scratch.  The pool keeps freed memory for reuse (release threshold at
+// the maximum) until pcvl_release_workspace() trims it.
+int scratch_alloc(size_t bytes, cudaStream_t stream, void** ptr);
+
+class ScratchGuard {
+ public:
+  explicit ScratchGuard(cudaStream_t s) : s_(s) {}
+  ScratchGuard(const ScratchGuard&) = delete;
+  ScratchGuard& operator=(const ScratchGuard&) = delete;
+  int alloc(size_t bytes, void** ptr) {
+    const int rc = scratch_alloc(bytes, s_, &p_);
+    *ptr = p_;
+    return rc;
+  }
+  ~ScratchGuard() {
+    if (p_) cudaFreeAsync(p_, s_);
+  }
+
+ private:
+  cudaStream_t s_;
+  void* p_ = nullptr;
 };
-int workspace(int slot, size_t bytes, void** ptr);
 
 // Copies `bytes` of host memory to device memory on `stream` through a pinned
 // staging buffer (kept per device); the host buffer may be reused on return.

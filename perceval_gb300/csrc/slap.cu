@@ -394,8 +394,9 @@ int slap_run(const double* u_d, int32_t m, const int32_t* input_state_h, int32_t
   std::memcpy(host.data() + o_moff, moff.data(), moff.size() * 4);
   std::memcpy(host.data() + o_masks, masks.data(), masks.size() * 2);
   std::memcpy(host.data() + o_invf, invf.data(), invf.size() * sizeof(dd));
+  ScratchGuard scratch(s);
   void* ws = nullptr;
-  PCVL_TRY(workspace(WS_SLAP, total, &ws));
+  PCVL_TRY(scratch.alloc(total, &ws));
   unsigned char* base = static_cast<unsigned char*>(ws);
   PCVL_TRY(stage_h2d(host.data(), o_uc, base, s));
   slap_convert<<<(m * n + 255) / 256, 256, 0, s>>>((const double2*)u_d, m, n, (const int32_t*)(base + o_cols),
@@ -530,9 +531,9 @@ int mask_ranks(int32_t m, int32_t n, int32_t n_masks, const int8_t* digits_h, co
   const size_t o_dg = align_up(cn.size() * 8, 16), o_atl = o_dg + align_up((size_t)n_masks * m, 16);
   const size_t o_suf = o_atl + align_up(m, 16), o_bsum = o_suf + align_up(suf.size() * 4, 16);
   const size_t o_boff = o_bsum + align_up(nb * 4, 16), total = o_boff + nb * 8;
+  ScratchGuard scratch(nullptr);
   void* ws = nullptr;
-  // its own slot: a SLAP walk still running on another stream keeps its tables
-  PCVL_TRY(workspace(WS_MASK, total, &ws));
+  PCVL_TRY(scratch.alloc(total, &ws));
   unsigned char* base = static_cast<unsigned char*>(ws);
   PCVL_CUDA(cudaMemcpy(base, cn.data(), cn.size() * 8, cudaMemcpyHostToDevice));
   PCVL_CUDA(cudaMemcpy(base + o_dg, digits_h, (size_t)n_masks * m, cudaMemcpyHostToDevice));

@@ -50,10 +50,21 @@ def test_argument_errors_are_reported_without_device_work(lib):
     offs = np.array([0], dtype=np.int64)
     # size 50 exceeds the kernel's limit: refused on the host before any CUDA call
     rc = L.pcvl_permanent_batch(ctypes.c_void_p(16), offs.ctypes.data, sizes.ctypes.data, 1, ctypes.c_void_p(16), 0,
-                                None)
+                                2, None)
     assert rc == 1 and "outside" in _native.last_error()
-    rc = L.pcvl_permanent_batch(None, None, None, -1, None, 0, None)
+    rc = L.pcvl_permanent_batch(None, None, None, -1, None, 0, 2, None)
     assert rc == 1
+    # an unknown arithmetic is refused (FP32 serves the sampler only)
+    sizes = np.array([3], dtype=np.int32)
+    rc = L.pcvl_permanent_batch(ctypes.c_void_p(16), offs.ctypes.data, sizes.ctypes.data, 1, ctypes.c_void_p(16), 0,
+                                1, None)
+    assert rc == 1 and "precision" in _native.last_error()
+    # overlapping matrices are refused before any device work (identical entries are allowed)
+    sizes = np.array([3, 3, 2], dtype=np.int32)
+    offs = np.array([0, 0, 4], dtype=np.int64)
+    rc = L.pcvl_permanent_batch(ctypes.c_void_p(16), offs.ctypes.data, sizes.ctypes.data, 3, ctypes.c_void_p(16), 0,
+                                2, None)
+    assert rc == 1 and "overlap" in _native.last_error()
     h = ctypes.c_void_p()
     inp = np.array([1] * 40, dtype=np.int32)
     rc = L.pcvl_slos_plan_create(ctypes.byref(h), 40, inp.ctypes.data, 1, 0)

@@ -16,9 +16,10 @@ RTOL = 1e-10
 def reset_table():
     yield
     from perceval_gb300 import _native
-    for method in (0, 1):
-        for n in range(1, 41):
-            _native.set_perm_tuning(method, n)
+    for prec in ("fp64", "float-float"):
+        for method in (0, 1):
+            for n in range(1, 41):
+                _native.set_perm_tuning(method, n, precision=prec)
 
 
 def _mixed(seed):
@@ -27,14 +28,15 @@ def _mixed(seed):
     return mats
 
 
+@pytest.mark.parametrize("prec", ["fp64", "float-float"])
 @pytest.mark.parametrize("method", [0, 1])
-def test_plan_equals_batch_call(native, method):
+def test_plan_equals_batch_call(native, method, prec):
     mats = _mixed(1)
     flat, offs, sizes = pack(mats)
     dev = torch.from_numpy(flat).cuda()
     ref = torch.empty(len(mats), dtype=torch.complex128, device="cuda")
-    native.permanent_batch(dev, offs, sizes, ref, method)
-    plan = native.PermPlan(offs, sizes, method)
+    native.permanent_batch(dev, offs, sizes, ref, method, precision=prec)
+    plan = native.PermPlan(offs, sizes, method, precision=prec)
     got = plan(dev)
     assert torch.equal(got, ref)
     assert got[5].item() == 1.0
@@ -44,7 +46,7 @@ def test_plan_equals_batch_call(native, method):
     flat2 = np.concatenate([m.reshape(-1) for m in mats2])
     dev2 = torch.from_numpy(flat2).cuda()
     ref2 = torch.empty_like(ref)
-    native.permanent_batch(dev2, offs, sizes, ref2, method)
+    native.permanent_batch(dev2, offs, sizes, ref2, method, precision=prec)
     out2 = torch.empty_like(ref)
     for _ in range(3):
         plan(dev2, out2)
@@ -78,30 +80,37 @@ def test_plan_on_side_stream(native):
     assert torch.equal(out, ref)
 
 
+@pytest.mark.parametrize("prec", ["fp64", "float-float"])
 @pytest.mark.parametrize("n,lo,ctas", [(14, 3, 4), (18, 9, 32), (20, 8, 16), (22, 4, 2)])
-def test_tuned_shapes_keep_parity(native, oracle, n, lo, ctas):
+def test_tuned_shapes_keep_parity(native, oracle, n, lo, ctas, prec):
     mats = haar_submatrices(6, n, n, seed=n)
     flat, offs, sizes = pack(mats)
     ref = oracle.perm_batch(flat, offs, sizes)
-    native.set_perm_tuning(0, n, lo, ctas)
+    native.set_perm_tuning(0, n, lo, ctas, precision=prec)
     dev = torch.from_numpy(flat).cuda()
     out = torch.empty(len(mats), dtype=torch.complex128, device="cuda")
-    native.permanent_batch(dev, offs, sizes, out)
+    native.permanent_batch(dev, offs, sizes, out, precision=prec)
     assert np.all(np.abs(out.cpu().numpy() - ref) <= RTOL * np.abs(ref))
-    plan_out = native.PermPlan(offs, sizes)(dev).cpu().numpy()
+    plan_out = native.PermPlan(offs, sizes, precision=prec)(dev).cpu().numpy()
     assert np.array_equal(plan_out, out.cpu().numpy())
 
 
 def test_autotuner_installs_and_caches(native, tmp_path):
     from perceval_gb300 import autotune
     table = autotune.tune_permanents(sizes=[9, 13], target_ms=1.0, reps=1)
+    assert table["precision"] == "fp64"
     assert set(table["entries"]) == {"9", "13"}
     for n, e in table["entries"].items():
         assert native.get_perm_tuning(0, int(n)) == (e["lo_bits"], e["ctas_per_sm"])
         assert e["ms"] <= e["default_ms"]
     path = autotune.save(table, tmp_path / "tuning.json")
+    ff = autotune.tune_permanents(sizes=[11], target_ms=1.0, reps=1, precision="float-float")
+    autotune.save(ff, path)
     for n in (9, 13):
         native.set_perm_tuning(0, n)
+    native.set_perm_tuning(0, 11, precision="float-float")
     assert autotune.load(path)
     for n, e in table["entries"].items():
         assert native.get_perm_tuning(0, int(n)) == (e["lo_bits"], e["ctas_per_sm"])
+    e = ff["entries"]["11"]
+    assert native.get_perm_tuning(0, 11, precision="float-float") == (e["lo_bits"], e["ctas_per_sm"])

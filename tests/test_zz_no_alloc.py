@@ -30,14 +30,15 @@ def batch(seed: int, count: int, nmax: int):
     return flat, offs, sizes
 
 
-def test_noalloc_matches_allocating_entry_point_on_two_calls(native):
+@pytest.mark.parametrize("prec", ["fp64", "float-float"])
+def test_noalloc_matches_allocating_entry_point_on_two_calls(native, prec):
     # two calls in a row on different batches: the second must not see the first's scratch
     for seed, count, nmax in ((1, 300, 20), (2, 120, 24)):
         flat, offs, sizes = batch(seed, count, nmax)
         ref = torch.empty(len(sizes), dtype=torch.complex128, device="cuda")
-        native.permanent_batch(flat, offs, sizes, ref)
+        native.permanent_batch(flat, offs, sizes, ref, precision=prec)
         got = torch.full((len(sizes),), complex("nan"), dtype=torch.complex128, device="cuda")
-        native.permanent_batch_noalloc(flat, offs, sizes, got)
+        native.permanent_batch_noalloc(flat, offs, sizes, got, precision=prec)
         ref, got = ref.cpu().numpy(), got.cpu().numpy()
         assert got[0] == 1 and got[1] == 0.5 - 0.25j
         assert np.all(np.abs(got - ref) <= RTOL * np.abs(ref)), np.max(np.abs(got - ref) / np.abs(ref))
@@ -51,3 +52,22 @@ def test_noalloc_refuses_requests_beyond_its_limits(native):
     big = torch.zeros(40 * 40 * 2000, dtype=torch.complex128, device="cuda")
     with pytest.raises(RuntimeError, match="elements, more than the maximum"):
         native.permanent_batch_noalloc(big, np.arange(2000) * 1600, np.full(2000, 40, np.int32), out)
+
+
+def test_noalloc_refuses_too_many_partial_sums(native):
+    """Launch shapes tuned to many CTAs per SM give a single large matrix thousands of
+    partial sums; one such matrix in each of the 14 sizes 27..40 passes the 2^17 limit
+    and is refused before any device work."""
+    sizes = np.arange(27, 41, dtype=np.int32)
+    offs = np.zeros(len(sizes), dtype=np.int64)
+    offs[1:] = np.cumsum(sizes.astype(np.int64) ** 2)[:-1]
+    mats = torch.zeros(int((sizes.astype(np.int64) ** 2).sum()), dtype=torch.complex128, device="cuda")
+    out = torch.empty(len(sizes), dtype=torch.complex128, device="cuda")
+    try:
+        for n in sizes:
+            native.set_perm_tuning(0, int(n), 7, 64)
+        with pytest.raises(RuntimeError, match="partial sums, more than the maximum"):
+            native.permanent_batch_noalloc(mats, offs, sizes, out)
+    finally:
+        for n in sizes:
+            native.set_perm_tuning(0, int(n))
