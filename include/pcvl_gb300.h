@@ -144,12 +144,14 @@ int pcvl_perm_plan_destroy(pcvl_perm_plan* plan);
  * Output index r of a circuit is the rank of the output state in descending
  * lexicographic order (|n,0,..,0> first), the order of the reference's
  * allstate_iterator.  keep_layers != 0 keeps every layer resident for
- * pcvl_slos_backward.
+ * pcvl_slos_backward.  precision (PCVL_PREC_FP64 or PCVL_PREC_FLOAT_FLOAT) fixes the
+ * arithmetic of every layer's multiply-adds and of the normalisation; a layer holds 16
+ * bytes per coefficient in both.
  */
 typedef struct pcvl_slos_plan pcvl_slos_plan;
 
 int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int32_t* input_state_h,
-                          int32_t batch, int32_t keep_layers);
+                          int32_t batch, int32_t keep_layers, int32_t precision);
 /* Plan whose `batch` entries each have their own input state (input_states_h: batch x m,
  * host; every state must hold the same photon count).  No reference counterpart as one
  * call: it batches the per-input-state loop of Simulator._probs_svd_fast
@@ -157,7 +159,7 @@ int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int32_t* input
  * prob_iterator once per distinct input.  Entry b's outputs are normalised by its own
  * prod(in_b!). */
 int pcvl_slos_plan_create_multi(pcvl_slos_plan** plan, int32_t m, const int32_t* input_states_h,
-                                int32_t batch, int32_t keep_layers);
+                                int32_t batch, int32_t keep_layers, int32_t precision);
 /* Plan restricted by a mask: replaces xq.FSMask + xq.FSArray(m, k, mask) /
  * xq.FSMap(cur, prev, True) of a masked SLOSBackend (perceval/backends/_abstract_backends.py:
  * 103-137 set_mask / _init_mask; perceval/backends/_slos.py:152-166 _deploy).  Mask q is
@@ -172,7 +174,8 @@ int pcvl_slos_plan_create_multi(pcvl_slos_plan** plan, int32_t m, const int32_t*
  * arguments as for a full plan, indexed by kept output. */
 int pcvl_slos_plan_create_masked(pcvl_slos_plan** plan, int32_t m, const int32_t* input_states_h,
                                  int32_t batch, int32_t keep_layers, int32_t n_masks,
-                                 const int8_t* digits_h, uint32_t at_least_modes, int32_t mask_n);
+                                 const int8_t* digits_h, uint32_t at_least_modes, int32_t mask_n,
+                                 int32_t precision);
 /* Ranks of the plan's outputs in the full n-photon space (descending lexicographic order,
  * rank 0 = |n,0,..,0>), ascending: ranks_h receives pcvl_slos_output_count entries (host).
  * For a plan without mask this is 0, 1, 2, ... */

@@ -38,13 +38,14 @@ SYMBOLS = {
     "pcvl_perm_plan_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     "pcvl_perm_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "pcvl_slos_plan_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.c_void_p,
-                                             ctypes.c_int32, ctypes.c_int32]),
+                                             ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "pcvl_slos_plan_create_multi": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
-                                                   ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
+                                                   ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                                   ctypes.c_int32]),
     "pcvl_slos_plan_create_masked": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32,
                                                      ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                                      ctypes.c_int32, ctypes.c_void_p, ctypes.c_uint32,
-                                                     ctypes.c_int32]),
+                                                     ctypes.c_int32, ctypes.c_int32]),
     "pcvl_slos_output_ranks": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "pcvl_slos_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "pcvl_fock_mask_ranks": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
@@ -303,11 +304,15 @@ class SlosPlan:
     array of per-entry states with one photon count (``pcvl_slos_plan_create_multi``).
     ``mask`` (an ``FSMask``) restricts every layer to the states the mask can still
     accept (``pcvl_slos_plan_create_masked``): the outputs are then the accepted states,
-    ``output_ranks()`` gives their ranks in the full n-photon space.
+    ``output_ranks()`` gives their ranks in the full n-photon space.  ``precision``:
+    "fp64" (native FP64, the reference's arithmetic) or "float-float".
     """
 
-    def __init__(self, m: int, input_state, batch: int = 1, keep_layers: bool = False, mask=None):
+    def __init__(self, m: int, input_state, batch: int = 1, keep_layers: bool = False, mask=None,
+                 precision="fp64"):
         self._lib = load()
+        self.precision = precision_code(precision)
+        prec = self.precision
         inp = np.ascontiguousarray(input_state, dtype=np.int32)
         h = ctypes.c_void_p()
         self.masked = mask is not None
@@ -327,20 +332,21 @@ class SlosPlan:
                 raise ValueError("mask and input state lengths differ")
             check(self._lib.pcvl_slos_plan_create_masked(ctypes.byref(h), int(m), inp.ctypes.data, int(batch),
                                                          1 if keep_layers else 0, int(digits.shape[0]),
-                                                         digits.ctypes.data, int(at_least), int(mask_n)),
+                                                         digits.ctypes.data, int(at_least), int(mask_n), prec),
                   "pcvl_slos_plan_create_masked")
         elif inp.ndim == 2:
             if inp.shape[1] != m or inp.shape[0] < 1:
                 raise ValueError("input states must form a (batch x m) array")
             batch = inp.shape[0]
             check(self._lib.pcvl_slos_plan_create_multi(ctypes.byref(h), int(m), inp.ctypes.data, int(batch),
-                                                        1 if keep_layers else 0), "pcvl_slos_plan_create_multi")
+                                                        1 if keep_layers else 0, prec),
+                  "pcvl_slos_plan_create_multi")
             self.input_state = [tuple(int(v) for v in row) for row in inp]
         else:
             if inp.shape != (m,):
                 raise ValueError("input_state must have m entries")
             check(self._lib.pcvl_slos_plan_create(ctypes.byref(h), int(m), inp.ctypes.data, int(batch),
-                                                  1 if keep_layers else 0), "pcvl_slos_plan_create")
+                                                  1 if keep_layers else 0, prec), "pcvl_slos_plan_create")
             self.input_state = tuple(int(v) for v in inp)
         self._h = h
         self.m, self.batch, self.keep_layers = m, batch, keep_layers

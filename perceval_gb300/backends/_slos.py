@@ -2,7 +2,9 @@
 
 Each distinct input state gets a device plan (``pcvl_slos_plan``): the layer chain in
 the photon order of ``_Path._decompose`` (_slos.py:61-86) runs as one gather kernel
-per photon over on-the-fly Fock ranks, in float-float arithmetic.  As in the
+per photon over on-the-fly Fock ranks, in native FP64 (complex128 coefficients, as the
+reference's layers, _slos.py:44,99) unless the backend is made with
+``precision="float-float"`` (FP32-pipe pairs, ~48 significant bits, faster).  As in the
 reference, changing the circuit to another one of the same size keeps the plans and
 recomputes their coefficients (_slos.py:130-141); a different size resets them.
 
@@ -12,8 +14,8 @@ every layer holds only the states the mask can still accept (xq.FSArray(m, k, ma
 _slos.py:161-164), and the outputs are the accepted states in the same order.
 ``all_prob`` returns a list up to 2^22 outputs and a numpy array above;
 ``all_prob_tensor`` leaves the probabilities on the device.  Circuits wider than the
-32 modes of SLOS plans take the SLAP walk (``pcvl_slap_*``), which computes the same
-amplitudes, with the mask's outputs selected on the device.
+32 modes of SLOS plans take the SLAP walk (``pcvl_slap_*``, float-float arithmetic),
+which computes the same amplitudes, with the mask's outputs selected on the device.
 
 ``all_probs_many`` / ``prob_distributions`` evaluate many input states of the circuit
 at once (the per-input loop of Simulator._probs_svd_fast, simulator.py:454-468): states
@@ -51,10 +53,13 @@ class _Entry:
 
 
 class SLOSBackend(AStrongSimulationBackend):
-    def __init__(self, mask=None, use_symbolic: bool = False):
+    def __init__(self, mask=None, use_symbolic: bool = False, precision: str = "fp64"):
         super().__init__()
         if use_symbolic:
             raise NotImplementedError("symbolic SLOS stays on the CPU reference; this backend is numeric only")
+        self._precision = _native.precision_code(precision)
+        if self._precision not in (_native.PREC_FP64, _native.PREC_FLOAT_FLOAT):
+            raise ValueError("precision must be 'fp64' or 'float-float'")
         self._entries: dict[FockState, _Entry] = {}
         self._u_dev: torch.Tensor | None = None
         if mask is not None:
@@ -108,7 +113,8 @@ class SLOSBackend(AStrongSimulationBackend):
                     if self._mask is not None:
                         e.ranks = _native.fock_mask_ranks(st.m, st.n, self._mask).cpu().numpy().astype(np.uint64)
                 else:
-                    e = _Entry(_native.SlosPlan(st.m, list(st), batch=1, keep_layers=False, mask=self._mask))
+                    e = _Entry(_native.SlosPlan(st.m, list(st), batch=1, keep_layers=False, mask=self._mask,
+                                                precision=self._precision))
                     if self._mask is not None:
                         e.ranks = e.plan.output_ranks()
                 self._entries[st] = e
@@ -198,14 +204,14 @@ class SLOSBackend(AStrongSimulationBackend):
             return res
         for n, idxs in sorted(groups.items()):
             count = math.comb(m + n - 1, n)
-            # two float-float layers per entry dominate a plan's memory
+            # two layers of 16-byte coefficients per entry dominate a plan's memory
             per_entry = 2 * 16 * max(count, 1)
             step = max(1, min(len(idxs), max_device_bytes // per_entry))
             mask = self._group_mask(m, n)
             for c0 in range(0, len(idxs), step):
                 chunk = idxs[c0:c0 + step]
                 arr = np.array([list(states[i]) for i in chunk], dtype=np.int32)
-                plan = _native.SlosPlan(m, arr, keep_layers=False, mask=mask)
+                plan = _native.SlosPlan(m, arr, keep_layers=False, mask=mask, precision=self._precision)
                 try:
                     plan.forward(U)
                     host = plan.probabilities().view(plan.count, len(chunk)).cpu().numpy()

@@ -1,14 +1,14 @@
 // Shared device/host helpers for the linear-optics kernels.
 //
 // Arithmetic: GB300 issues FP64 at 1/73 of its FP32 rate (measured: 505 G FP64 FMA/s
-// against 36.8 T FP32 FMA/s), so the hot loops carry FP64-class precision as
-// float-float pairs ("df64": value = hi + lo, |lo| <= ulp(hi)/2 when normalised)
-// built from error-free transformations on the FP32 pipe:
+// against 36.8 T FP32 FMA/s).  The kernels compute in native FP64 by default (the
+// reference's arithmetic) and offer, opt-in, FP64-class precision as float-float pairs
+// ("df64": value = hi + lo, |lo| <= ulp(hi)/2 when normalised) built from error-free
+// transformations on the FP32 pipe:
 //   two_sum   (Knuth 1969):  s = fl(a+b), e = (a+b) - s exactly;
 //   two_prod  (FMA form):    p = fl(a*b), e = fma(a, b, -p) exactly;
 //   fast_two_sum (Dekker 1971) when |a| >= |b|.
 // The pair carries ~48 significant bits (relative error ~2^-47 per operation).
-// Native FP64 appears only in the final per-result reductions.
 #pragma once
 #include <cstdint>
 #include <cmath>
@@ -17,6 +17,9 @@
 #define PCVL_HD __host__ __device__ __forceinline__
 
 namespace pcvl {
+
+// Arithmetic of the permanent, SLOS and sampler kernels (the ABI's PCVL_PREC_* codes).
+enum Precision : int { kPrecFloatFloat = 0, kPrecFP32 = 1, kPrecFP64 = 2 };
 
 // ------------------------------------------------------------------ df64 scalars
 struct dd {

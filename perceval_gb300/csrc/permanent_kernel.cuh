@@ -34,9 +34,6 @@
 
 namespace pcvl {
 
-// Arithmetic of the permanent, SLOS and sampler kernels (the ABI's precision codes).
-enum Precision : int { kPrecFloatFloat = 0, kPrecFP32 = 1, kPrecFP64 = 2 };
-
 struct PermBinArgs {
   const void* A;          // prepared (scaled) matrices: cdd (float-float) or double2 (FP64)
   const int64_t* offs;    // element offset of each matrix in A (global matrix index)

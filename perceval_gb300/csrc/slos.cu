@@ -31,7 +31,12 @@
 // small-table read (tail modes).  Each lane of a warp computes the descriptor of one
 // tile of a group of 32; the warp then sweeps the group's states.
 //
-// Layout.  Coefficients are float-float complex (16 bytes, FP64-class precision),
+// Arithmetic.  Every kernel is instantiated for the two policies of arith.cuh: native
+// FP64 (Arith64, the default: complex128 coefficients and DFMA multiply-adds, as the
+// reference's complex128 layers) and float-float (ArithFF, opt-in: FP32-pipe pairs,
+// ~48 significant bits).  A plan fixes its arithmetic at creation.
+//
+// Layout.  Coefficients are 16-byte complex values (double2 or a float-float pair),
 // state-major with the circuit index b innermost: element (r, b) at r * B + b.  With
 // B == 1 the lanes take consecutive states; with B >= 2 the lanes take 32 circuits
 // of one state (blockIdx.y selects the 32-circuit chunk), so loads are coalesced
@@ -47,6 +52,7 @@
 #include <new>
 #include <vector>
 
+#include "arith.cuh"
 #include "common.cuh"
 #include "runtime.cuh"
 #include "slos_plan.cuh"
@@ -59,19 +65,21 @@ constexpr uint32_t kNone = 0xffffffffu;
 constexpr int kWarps = 8;  // warps per CTA (256 threads)
 constexpr int kBwdGroups = 2;  // mode groups per warp of the batched adjoint (measured: 2 beats 1 and 4)
 
+// Values (P::V, 16 bytes) and factors (P::F, 8 bytes) travel as untyped pointers; each
+// kernel reads them with its arithmetic's types.
 struct SlosArgs {
   int m, k, p, t, B;      // k: photons of the layer whose states are the tiles
   uint32_t ntiles;
-  const cdd* in;          // forward: parent layer; adjoint: child-layer adjoint
-  cdd* out;               // forward: child layer; adjoint: parent-layer adjoint
-  const cdd* ucol;        // u_j (b) = U_b[j, mk] at ucol[j * B + b]
-  const cdd* cpar;        // adjoint: forward coefficients of the parent layer
-  cdd* gpart;             // adjoint: per-CTA partials of dL/du_j, [blockIdx.x][j][b]
+  const void* in;         // forward: parent layer; adjoint: child-layer adjoint
+  void* out;              // forward: child layer; adjoint: parent-layer adjoint
+  const void* ucol;       // u_j (b) = U_b[j, mk] at ucol[j * B + b]
+  const void* cpar;       // adjoint: forward coefficients of the parent layer
+  void* gpart;            // adjoint: per-CTA partials of dL/du_j, [blockIdx.x][j][b]
   const uint32_t* cn;
   int cn_stride;
   const uint32_t* tail;   // TP (forward) or TC (adjoint)
-  const dd* ftail;        // prod tau_j! per tail state
-  const dd* inv_in;       // 1 / prod(in_b!) per batch entry
+  const void* ftail;      // prod tau_j! per tail state (factors)
+  const void* inv_in;     // 1 / prod(in_b!) per batch entry (factors)
   const uint8_t* tocc;    // occupied tail modes per tail state (bit j)
   uint32_t tail_off[kSlosMaxN + 2];    // entry offset of the block of r tail photons
   uint32_t tstate_off[kSlosMaxN + 2];  // state offset of that block
@@ -101,25 +109,25 @@ __device__ __forceinline__ uint32_t cn_at(const uint32_t* cn, int stride, int M,
   return x < 0 ? 0u : cn[M * stride + x];
 }
 
-// Prefix descriptor of one tile, in registers.
-template <int MMAX>
+// Prefix descriptor of one tile, in registers (F: the arithmetic's factor type).
+template <int MMAX, typename F>
 struct Desc {
   uint32_t A;             // rank of the tile's first state
   uint32_t tb;            // forward: A - Pfx_p; adjoint: A + Q_p
   uint32_t mask;          // occupied prefix modes
   uint32_t base[MMAX];    // forward: A - Pfx_j (occupied j); adjoint: A + Q_j
-  dd f;                   // prod pi_i! / prod(in!)  (normalisation only)
+  F f;                    // prod pi_i! / prod(in!)  (normalisation only)
 };
 
 // Unranks prefix pi_idx of the q-photon prefix space (p modes) for a tile with r
 // tail photons and walks the modes once for the tile's offsets.
-template <int MMAX, bool ADJ, bool FACT>
+template <int MMAX, bool ADJ, bool FACT, class P>
 __device__ __forceinline__ void describe(uint32_t pi_idx, int q, int r, const SlosArgs& a, const uint32_t* cn,
-                                         Desc<MMAX>& d, dd inv_in, uint32_t* base) {
+                                         Desc<MMAX, typename P::F>& d, typename P::F inv_in, uint32_t* base) {
   const int m = a.m, p = a.p, st = a.cn_stride;
   uint32_t rho = pi_idx, A = 0, acc = 0, mask = 0;
   int Rp = q, R = q + r;
-  dd f = inv_in;
+  typename P::F f = inv_in;
 #pragma unroll
   for (int i = 0; i < MMAX; ++i) {
     if (i < p) {
@@ -137,7 +145,7 @@ __device__ __forceinline__ void describe(uint32_t pi_idx, int q, int r, const Sl
         v = Rp - x;
       }
       if (FACT)
-        for (int s2 = 2; s2 <= v; ++s2) f = dd_mul_f(f, (float)s2);
+        for (int s2 = 2; s2 <= v; ++s2) f = P::f_mul_int(f, s2);
       Rp -= v;
       const int Rn = R - v;
       if (ADJ) {
@@ -183,24 +191,26 @@ __host__ __device__ inline size_t smem_cn_bytes(int m, int stride) {
 }
 template <int MMAX>
 __host__ __device__ inline size_t smem_bytes(int m, int stride) {
-  return smem_cn_bytes(m, stride) + (size_t)MMAX * 32 * sizeof(cdd);
+  return smem_cn_bytes(m, stride) + (size_t)MMAX * 32 * sizeof(double2);
 }
 // rank table and u (conjugated for the adjoint) into shared memory
-template <int MMAX, bool BATCHED, bool CONJ>
-__device__ __forceinline__ cdd* load_shared(const SlosArgs& a, unsigned char* raw, uint32_t*& cn) {
+template <int MMAX, bool BATCHED, bool CONJ, class P>
+__device__ __forceinline__ typename P::V* load_shared(const SlosArgs& a, unsigned char* raw, uint32_t*& cn) {
+  using V = typename P::V;
   cn = reinterpret_cast<uint32_t*>(raw);
-  cdd* u = reinterpret_cast<cdd*>(raw + smem_cn_bytes(a.m, a.cn_stride));
+  V* u = reinterpret_cast<V*>(raw + smem_cn_bytes(a.m, a.cn_stride));
+  const V* ucol = static_cast<const V*>(a.ucol);
   const int ncn = (a.m + 1) * a.cn_stride;
   for (int i = threadIdx.x; i < ncn; i += blockDim.x) cn[i] = a.cn[i];
   if (BATCHED) {
     for (int i = threadIdx.x; i < MMAX * 32; i += blockDim.x) {
       const int j = i >> 5, b = blockIdx.y * 32 + (i & 31);
-      cdd v = (j < a.m && b < a.B) ? a.ucol[(size_t)j * a.B + b] : cdd_zero();
-      u[i] = CONJ ? cdd_conj(v) : v;
+      V v = (j < a.m && b < a.B) ? ucol[(size_t)j * a.B + b] : P::zero();
+      u[i] = CONJ ? P::conj(v) : v;
     }
   } else if (threadIdx.x < MMAX) {
-    cdd v = (int)threadIdx.x < a.m ? a.ucol[threadIdx.x] : cdd_zero();
-    u[threadIdx.x] = CONJ ? cdd_conj(v) : v;
+    V v = (int)threadIdx.x < a.m ? ucol[threadIdx.x] : P::zero();
+    u[threadIdx.x] = CONJ ? P::conj(v) : v;
   }
   __syncthreads();
   return u;
@@ -209,16 +219,17 @@ __device__ __forceinline__ cdd* load_shared(const SlosArgs& a, unsigned char* ra
 // Forward value of state (d, tau) with r tail photons for circuit b of a batch: sum over
 // its occupied modes of u_j x[parent_j].  Prefix modes follow the tile mask (uniform over
 // a tile); tail modes loop over the set bits of the state's own tail occupation.
-template <int MMAX>
-__device__ __forceinline__ cdd fwd_value(const SlosArgs& a, const Desc<MMAX>& d, int r, uint32_t tau,
-                                         const cdd* __restrict__ x, const cdd* u, int us, int b) {
+template <int MMAX, class P>
+__device__ __forceinline__ typename P::V fwd_value(const SlosArgs& a, const Desc<MMAX, typename P::F>& d, int r,
+                                                   uint32_t tau, const typename P::V* __restrict__ x,
+                                                   const typename P::V* u, int us, int b) {
   const int p = a.p;
-  cacc acc = cacc_zero();
+  typename P::Acc acc = P::acc_zero();
 #pragma unroll
   for (int j = 0; j < MMAX; ++j) {
     if (j < p && ((d.mask >> j) & 1u)) {
       const uint32_t ad = d.base[j] + tau;
-      cacc_fma(acc, ld_cdd(&x[(size_t)ad * a.B + b]), u[j * us]);
+      P::fma(acc, P::ld(&x[(size_t)ad * a.B + b]), u[j * us]);
     }
   }
   if (r > 0) {
@@ -228,34 +239,37 @@ __device__ __forceinline__ cdd fwd_value(const SlosArgs& a, const Desc<MMAX>& d,
       const int jl = __ffs(occ) - 1;
       occ &= occ - 1;
       const uint32_t ad = d.tb + __ldg(&row[jl]);
-      cacc_fma(acc, ld_cdd(&x[(size_t)ad * a.B + b]), u[(p + jl) * us]);
+      P::fma(acc, P::ld(&x[(size_t)ad * a.B + b]), u[(p + jl) * us]);
     }
   }
-  return cacc_finish(acc);
+  return P::finish(acc);
 }
 
 // Batched forward layer: a warp takes a unit (one tile, up to kChunkB states) and its
 // lanes 32 circuits; the parent offsets are warp-uniform, the loads coalesced.
-template <int MMAX>
+template <int MMAX, class P>
 __global__ void __launch_bounds__(256, 4) slos_fwdb(SlosArgs a) {
+  using V = typename P::V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t* cn;
-  const cdd* us_base = load_shared<MMAX, true, false>(a, smem_raw, cn);
+  const V* us_base = load_shared<MMAX, true, false, P>(a, smem_raw, cn);
+  const V* xin = static_cast<const V*>(a.in);
+  V* xout = static_cast<V*>(a.out);
   const int lane = threadIdx.x & 31;
   const int b = blockIdx.y * 32 + lane;
-  const cdd* u = us_base + lane;
+  const V* u = us_base + lane;
   const uint32_t total = a.uoff[a.k + 1];
   const uint32_t nw = gridDim.x * kWarps;
   for (uint32_t unit = blockIdx.x * kWarps + (threadIdx.x >> 5); unit < total; unit += nw) {
     const int r = unit_class(a, unit);
     const uint32_t S = a.tsize[r], lu = unit - a.uoff[r], cpt = a.cpt[r];
     const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
-    Desc<MMAX> d;
-    describe<MMAX, false, false>(pi, a.k - r, r, a, cn, d, dd{0.f, 0.f}, d.base);
+    Desc<MMAX, typename P::F> d;
+    describe<MMAX, false, false, P>(pi, a.k - r, r, a, cn, d, P::f_from(0.0), d.base);
     const uint32_t t0 = ch * a.chunkB, t1 = min(S, t0 + a.chunkB);
     if (b < a.B)
       for (uint32_t tau = t0; tau < t1; ++tau)
-        a.out[(size_t)(d.A + tau) * a.B + b] = fwd_value<MMAX>(a, d, r, tau, a.in, u, 32, b);
+        xout[(size_t)(d.A + tau) * a.B + b] = fwd_value<MMAX, P>(a, d, r, tau, xin, u, 32, b);
   }
 }
 
@@ -274,13 +288,6 @@ __host__ __device__ constexpr int fwd1_slot() {
   return PROB ? MMAX + 5 : MMAX + 4;
 }
 
-// Probability of a last-layer state from its coefficient and F = prod(out!) / prod(in!)
-// (the arithmetic of fin_state, so the fused and the two-pass results are identical).
-__device__ __forceinline__ double fwd_prob(const cdd& c, const dd& F) {
-  const dd c2 = dd_add(dd_mul(c.re, c.re), dd_mul(c.im, c.im));
-  return dd_to_double_fast(dd_mul(c2, F));
-}
-
 // Single-circuit forward layer.
 //  * Tiles of >= chunk1 / 2 states: a unit is up to chunk1 states of one tile, so the warp shares
 //    the tile.  Lane 0 unranks it into its slot; the prefix modes are a warp-uniform loop
@@ -297,15 +304,21 @@ __device__ __forceinline__ double fwd_prob(const cdd& c, const dd& F) {
 //  * PROB (the last layer, when only probabilities are wanted): each state's probability
 //    |c|^2 prod(out!) / prod(in!) goes to probs instead of its coefficient to a.out, so the
 //    last layer is never stored nor read back.
-template <int MMAX, bool PROB>
+template <int MMAX, bool PROB, class P>
 __global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a, double* __restrict__ probs) {
+  using V = typename P::V;
+  using F = typename P::F;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int SL = fwd1_slot<MMAX, PROB>();
   uint32_t* cn;
-  const cdd* u = load_shared<MMAX, false, false>(a, smem_raw, cn);
+  const V* u = load_shared<MMAX, false, false, P>(a, smem_raw, cn);
+  const V* __restrict__ xin = static_cast<const V*>(a.in);
+  V* __restrict__ xout = static_cast<V*>(a.out);
+  const F* __restrict__ ftail_all = static_cast<const F*>(a.ftail);
+  const F inv0 = PROB ? static_cast<const F*>(a.inv_in)[0] : P::f_from(0.0);
   // one circuit: u holds MMAX entries; the slots follow
   uint32_t* slots = reinterpret_cast<uint32_t*>(smem_raw + smem_cn_bytes(a.m, a.cn_stride) +
-                                                (size_t)MMAX * sizeof(cdd));
+                                                (size_t)MMAX * sizeof(V));
   const int lane = threadIdx.x & 31, p = a.p;
   uint32_t* myslot = slots + (size_t)threadIdx.x * SL;
   const uint32_t* wslots = slots + (size_t)(threadIdx.x - lane) * SL;  // the warp's 32 slots
@@ -322,60 +335,53 @@ __global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a, double* __restri
       const uint32_t c0 = (lu - pi * cpt) * a.chunk1;
       const uint32_t c1 = min(S, c0 + a.chunk1);
       uint32_t A = 0, tb = 0, mask = 0;
-      float fh = 0.f, fl = 0.f;
+      F ft = P::f_from(0.0);
       if (lane == 0) {
-        Desc<MMAX> d;
-        describe<MMAX, false, PROB>(pi, q, r, a, cn, d, PROB ? a.inv_in[0] : dd{0.f, 0.f}, myslot);
+        Desc<MMAX, F> d;
+        describe<MMAX, false, PROB, P>(pi, q, r, a, cn, d, inv0, myslot);
         A = d.A;
         tb = d.tb;
         mask = d.mask;
-        if (PROB) {
-          fh = d.f.hi;
-          fl = d.f.lo;
-        }
+        if (PROB) ft = d.f;
       }
       __syncwarp();
       A = __shfl_sync(0xffffffffu, A, 0);
       tb = __shfl_sync(0xffffffffu, tb, 0);
       mask = __shfl_sync(0xffffffffu, mask, 0);
-      if (PROB) {
-        fh = __shfl_sync(0xffffffffu, fh, 0);
-        fl = __shfl_sync(0xffffffffu, fl, 0);
-      }
-      const dd ft = {fh, fl};
-      const dd* ftail = a.ftail + a.tstate_off[r];
+      if (PROB) ft = P::f_shfl(ft, 0);
+      const F* ftail = ftail_all + a.tstate_off[r];
       for (uint32_t t0 = c0 + lane; t0 < c1; t0 += 64) {
         const uint32_t t1 = t0 + 32;
         const bool two = t1 < c1;
-        cacc acc0 = cacc_zero(), acc1 = cacc_zero();
+        typename P::Acc acc0 = P::acc_zero(), acc1 = P::acc_zero();
         for (uint32_t mm = mask; mm; mm &= mm - 1) {
           const int j = __ffs(mm) - 1;
           const uint32_t bj = wslots[j];
-          const cdd uj = u[j];
-          cacc_fma(acc0, ld_cdd(&a.in[bj + t0]), uj);
-          if (two) cacc_fma(acc1, ld_cdd(&a.in[bj + t1]), uj);
+          const V uj = u[j];
+          P::fma(acc0, P::ld(&xin[bj + t0]), uj);
+          if (two) P::fma(acc1, P::ld(&xin[bj + t1]), uj);
         }
         {
           const uint32_t* row = rows + (size_t)t0 * a.t;
           for (uint32_t o = __ldg(&occ_t[t0]); o; o &= o - 1) {
             const int jl = __ffs(o) - 1;
-            cacc_fma(acc0, ld_cdd(&a.in[tb + __ldg(&row[jl])]), u[p + jl]);
+            P::fma(acc0, P::ld(&xin[tb + __ldg(&row[jl])]), u[p + jl]);
           }
           if (PROB)
-            probs[A + t0] = fwd_prob(cacc_finish(acc0), dd_mul(ft, ftail[t0]));
+            probs[A + t0] = P::prob(P::finish(acc0), P::f_mul(ft, ftail[t0]));
           else
-            a.out[A + t0] = cacc_finish(acc0);
+            xout[A + t0] = P::finish(acc0);
         }
         if (two) {
           const uint32_t* row = rows + (size_t)t1 * a.t;
           for (uint32_t o = __ldg(&occ_t[t1]); o; o &= o - 1) {
             const int jl = __ffs(o) - 1;
-            cacc_fma(acc1, ld_cdd(&a.in[tb + __ldg(&row[jl])]), u[p + jl]);
+            P::fma(acc1, P::ld(&xin[tb + __ldg(&row[jl])]), u[p + jl]);
           }
           if (PROB)
-            probs[A + t1] = fwd_prob(cacc_finish(acc1), dd_mul(ft, ftail[t1]));
+            probs[A + t1] = P::prob(P::finish(acc1), P::f_mul(ft, ftail[t1]));
           else
-            a.out[A + t1] = cacc_finish(acc1);
+            xout[A + t1] = P::finish(acc1);
         }
       }
       __syncwarp();  // lane 0's slot is rewritten by the next unit
@@ -386,15 +392,12 @@ __global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a, double* __restri
     const uint32_t g0 = lu * G;
     const uint32_t ng = min(G, a.npf[r] - g0);
     if ((uint32_t)lane < ng) {
-      Desc<MMAX> d;
-      describe<MMAX, false, PROB>(g0 + lane, q, r, a, cn, d, PROB ? a.inv_in[0] : dd{0.f, 0.f}, myslot);
+      Desc<MMAX, F> d;
+      describe<MMAX, false, PROB, P>(g0 + lane, q, r, a, cn, d, inv0, myslot);
       myslot[MMAX] = d.A;
       myslot[MMAX + 1] = d.tb;
       myslot[MMAX + 2] = d.mask;
-      if (PROB) {
-        myslot[MMAX + 3] = __float_as_uint(d.f.hi);
-        myslot[MMAX + 4] = __float_as_uint(d.f.lo);
-      }
+      if (PROB) P::f_pack(d.f, myslot + MMAX + 3);
     }
     __syncwarp();
     // state f = g * S + tau of the group, f = lane, lane + 32, ...
@@ -405,7 +408,7 @@ __global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a, double* __restri
       uint32_t occ = ws[MMAX + 2] | ((uint32_t)__ldg(&occ_t[tau]) << p);
       const uint32_t tb = ws[MMAX + 1];
       const uint32_t* row = rows + (size_t)tau * a.t - p;
-      cacc acc = cacc_zero();
+      typename P::Acc acc = P::acc_zero();
       // two occupied modes per iteration: both parent gathers are in flight before the
       // first multiply-add (the accumulation order, and so the result, is unchanged)
       while (occ) {
@@ -416,18 +419,18 @@ __global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a, double* __restri
           const int j2 = __ffs(occ) - 1;
           occ &= occ - 1;
           const uint32_t ad2 = j2 < p ? ws[j2] + tau : tb + __ldg(&row[j2]);
-          const cdd v = ld_cdd(&a.in[ad]), v2 = ld_cdd(&a.in[ad2]);
-          cacc_fma(acc, v, u[j]);
-          cacc_fma(acc, v2, u[j2]);
+          const V v = P::ld(&xin[ad]), v2 = P::ld(&xin[ad2]);
+          P::fma(acc, v, u[j]);
+          P::fma(acc, v2, u[j2]);
         } else {
-          cacc_fma(acc, ld_cdd(&a.in[ad]), u[j]);
+          P::fma(acc, P::ld(&xin[ad]), u[j]);
         }
       }
       if (PROB) {
-        const dd fg = {__uint_as_float(ws[MMAX + 3]), __uint_as_float(ws[MMAX + 4])};
-        probs[ws[MMAX] + tau] = fwd_prob(cacc_finish(acc), dd_mul(fg, a.ftail[a.tstate_off[r] + tau]));
+        const F fg = P::f_unpack(ws + MMAX + 3);
+        probs[ws[MMAX] + tau] = P::prob(P::finish(acc), P::f_mul(fg, ftail_all[a.tstate_off[r] + tau]));
       } else {
-        a.out[ws[MMAX] + tau] = cacc_finish(acc);
+        xout[ws[MMAX] + tau] = P::finish(acc);
       }
       g += q32;
       tau += r32;
@@ -442,80 +445,77 @@ __global__ void __launch_bounds__(256, 6) slos_fwd1(SlosArgs a, double* __restri
 
 // Adjoint value of parent state (d, tau) of one circuit: a_{k-1} = sum_j conj(u_j)
 // a_k[child_j], and g_j += conj(c_{k-1}) a_k[child_j] (every child exists).
-template <int MMAX>
-__device__ __forceinline__ void bwd_state(const SlosArgs& a, const Desc<MMAX>& d, int r, uint32_t tau,
-                                          const cdd* uc, cacc (&g)[MMAX]) {
+template <int MMAX, class P>
+__device__ __forceinline__ void bwd_state(const SlosArgs& a, const Desc<MMAX, typename P::F>& d, int r,
+                                          uint32_t tau, const typename P::V* uc, typename P::Acc (&g)[MMAX]) {
+  using V = typename P::V;
   const int p = a.p, m = a.m;
+  const V* __restrict__ xin = static_cast<const V*>(a.in);
   const size_t pidx = (size_t)(d.A + tau);
-  const cdd cp = cdd_conj(ld_cdd(&a.cpar[pidx]));
+  const V cp = P::conj(P::ld(&static_cast<const V*>(a.cpar)[pidx]));
   const uint32_t* row = a.tail + a.tail_off[r] + (size_t)tau * a.t;
-  cacc acc = cacc_zero();
+  typename P::Acc acc = P::acc_zero();
 #pragma unroll
   for (int j = 0; j < MMAX; ++j) {
     if (j < m) {
       const uint32_t ad = j < p ? d.base[j] + tau : d.tb + __ldg(&row[j - p]);
-      const cdd v = ld_cdd(&a.in[ad]);
-      cacc_fma(acc, v, uc[j]);
-      cacc_fma(g[j], v, cp);
+      const V v = P::ld(&xin[ad]);
+      P::fma(acc, v, uc[j]);
+      P::fma(g[j], v, cp);
     }
   }
-  a.out[pidx] = cacc_finish(acc);
+  static_cast<V*>(a.out)[pidx] = P::finish(acc);
 }
 
 // Single-circuit adjoint step over the parent layer (its states are the units' states);
 // per-CTA partials of dL/du_j go to gpart.  Batches use slos_bwd_g.
-template <int MMAX>
+template <int MMAX, class P>
 __global__ void __launch_bounds__(256) slos_bwd(SlosArgs a) {
+  using V = typename P::V;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ cdd red[kWarps][32];
+  __shared__ V red[kWarps][32];
   uint32_t* cn;
-  const cdd* uc = load_shared<MMAX, false, true>(a, smem_raw, cn);
+  const V* uc = load_shared<MMAX, false, true, P>(a, smem_raw, cn);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int m = a.m;
-  cacc g[MMAX];
+  typename P::Acc g[MMAX];
 #pragma unroll
-  for (int j = 0; j < MMAX; ++j) g[j] = cacc_zero();
+  for (int j = 0; j < MMAX; ++j) g[j] = P::acc_zero();
   const uint32_t total = a.uoff[a.k + 1];
   const uint32_t nw = gridDim.x * kWarps;
   for (uint32_t unit = blockIdx.x * kWarps + wid; unit < total; unit += nw) {
     const int r = unit_class(a, unit);
     const int q = a.k - r;
     const uint32_t S = a.tsize[r], lu = unit - a.uoff[r], cpt = a.cpt[r];
-    Desc<MMAX> d;
+    Desc<MMAX, typename P::F> d;
     if (cpt > 0) {
       const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
-      describe<MMAX, true, false>(pi, q, r, a, cn, d, dd{0.f, 0.f}, d.base);
+      describe<MMAX, true, false, P>(pi, q, r, a, cn, d, P::f_from(0.0), d.base);
       const uint32_t t0 = ch * kChunk, t1 = min(S, t0 + kChunk);
-      for (uint32_t tau = t0 + lane; tau < t1; tau += 32) bwd_state<MMAX>(a, d, r, tau, uc, g);
+      for (uint32_t tau = t0 + lane; tau < t1; tau += 32) bwd_state<MMAX, P>(a, d, r, tau, uc, g);
     } else {
       // small tiles: one tile per lane
       const uint32_t pi = lu * 32 + lane;
       if (pi < a.npf[r]) {
-        describe<MMAX, true, false>(pi, q, r, a, cn, d, dd{0.f, 0.f}, d.base);
-        for (uint32_t tau = 0; tau < S; ++tau) bwd_state<MMAX>(a, d, r, tau, uc, g);
+        describe<MMAX, true, false, P>(pi, q, r, a, cn, d, P::f_from(0.0), d.base);
+        for (uint32_t tau = 0; tau < S; ++tau) bwd_state<MMAX, P>(a, d, r, tau, uc, g);
       }
     }
   }
   // reduce g over the CTA's threads
+  V* gpart = static_cast<V*>(a.gpart);
 #pragma unroll
   for (int j = 0; j < MMAX; ++j) {
     if (j >= m) break;
-    cdd v = cacc_finish(g[j]);
+    V v = P::finish(g[j]);
 #pragma unroll
-    for (int dlt = 16; dlt > 0; dlt >>= 1) {
-      cdd o;
-      o.re.hi = __shfl_down_sync(0xffffffffu, v.re.hi, dlt);
-      o.re.lo = __shfl_down_sync(0xffffffffu, v.re.lo, dlt);
-      o.im.hi = __shfl_down_sync(0xffffffffu, v.im.hi, dlt);
-      o.im.lo = __shfl_down_sync(0xffffffffu, v.im.lo, dlt);
-      v = cdd_add(v, o);
-    }
+    for (int dlt = 16; dlt > 0; dlt >>= 1) v = P::add(v, P::shfl_down(v, dlt));
     red[wid][lane] = v;
     __syncthreads();
     if (wid == 0 && lane == 0) {
-      cdd s2 = red[0][0];
-      for (int w = 1; w < kWarps; ++w) s2 = cdd_add(s2, red[w][0]);
-      a.gpart[(size_t)blockIdx.x * m + j] = s2;
+      V s2 = red[0][0];
+      for (int w = 1; w < kWarps; ++w) s2 = P::add(s2, red[w][0]);
+      gpart[(size_t)blockIdx.x * m + j] = s2;
     }
     __syncthreads();
   }
@@ -528,18 +528,23 @@ __global__ void __launch_bounds__(256) slos_bwd(SlosArgs a) {
 // dL/du_j for MMAX/G modes; the G group parts of a parent's
 // a_{k-1} = sum_j conj(u_j) a_k[child_j] meet by log2(G) shuffles.  Every (parent, mode,
 // circuit) child value is loaded once, as in slos_bwd.
-template <int MMAX, int G>
+template <int MMAX, int G, class P>
 __global__ void __launch_bounds__(256, MMAX <= 16 ? 4 : 2) slos_bwd_g(SlosArgs a) {
+  using V = typename P::V;
   constexpr int NC = 32 / G, MG = MMAX / G;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ cdd red[kWarps][32];
+  __shared__ V red[kWarps][32];
   uint32_t* cn = reinterpret_cast<uint32_t*>(smem_raw);
-  cdd* us = reinterpret_cast<cdd*>(smem_raw + smem_cn_bytes(a.m, a.cn_stride));  // [j][NC circuits], conjugated
+  V* us = reinterpret_cast<V*>(smem_raw + smem_cn_bytes(a.m, a.cn_stride));  // [j][NC circuits], conjugated
+  const V* ucol = static_cast<const V*>(a.ucol);
+  const V* __restrict__ xin = static_cast<const V*>(a.in);
+  const V* __restrict__ cpar = static_cast<const V*>(a.cpar);
+  V* __restrict__ xout = static_cast<V*>(a.out);
   const int ncn = (a.m + 1) * a.cn_stride;
   for (int i = threadIdx.x; i < ncn; i += blockDim.x) cn[i] = a.cn[i];
   for (int i = threadIdx.x; i < MMAX * NC; i += blockDim.x) {
     const int j = i / NC, b = blockIdx.y * NC + (i % NC);
-    us[i] = (j < a.m && b < a.B) ? cdd_conj(a.ucol[(size_t)j * a.B + b]) : cdd_zero();
+    us[i] = (j < a.m && b < a.B) ? P::conj(ucol[(size_t)j * a.B + b]) : P::zero();
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -547,57 +552,51 @@ __global__ void __launch_bounds__(256, MMAX <= 16 ? 4 : 2) slos_bwd_g(SlosArgs a
   const int b = blockIdx.y * NC + cl;
   const bool live = b < a.B;
   const int m = a.m, p = a.p;
-  cacc g[MG];
+  typename P::Acc g[MG];
 #pragma unroll
-  for (int jj = 0; jj < MG; ++jj) g[jj] = cacc_zero();
+  for (int jj = 0; jj < MG; ++jj) g[jj] = P::acc_zero();
   const uint32_t total = a.uoff[a.k + 1];
   const uint32_t nw = gridDim.x * kWarps;
   for (uint32_t unit = blockIdx.x * kWarps + wid; unit < total; unit += nw) {
     const int r = unit_class(a, unit);
     const int q = a.k - r;
     const uint32_t S = a.tsize[r], lu = unit - a.uoff[r], cpt = a.cpt[r];
-    Desc<MMAX> d;
+    Desc<MMAX, typename P::F> d;
     const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
-    describe<MMAX, true, false>(pi, q, r, a, cn, d, dd{0.f, 0.f}, d.base);
+    describe<MMAX, true, false, P>(pi, q, r, a, cn, d, P::f_from(0.0), d.base);
     const uint32_t t0 = ch * a.chunkB, t1 = min(S, t0 + a.chunkB);
     for (uint32_t tau = t0; tau < t1; ++tau) {
       const size_t pidx = (size_t)(d.A + tau) * a.B + b;
-      const cdd cp = live ? cdd_conj(ld_cdd(&a.cpar[pidx])) : cdd_zero();
+      const V cp = live ? P::conj(P::ld(&cpar[pidx])) : P::zero();
       const uint32_t* row = a.tail + a.tail_off[r] + (size_t)tau * a.t;
-      cacc acc = cacc_zero();
+      typename P::Acc acc = P::acc_zero();
 #pragma unroll
       for (int jj = 0; jj < MG; ++jj) {
         const int j = grp * MG + jj;
         if (j < m && live) {
           const uint32_t ad = j < p ? d.base[j] + tau : d.tb + __ldg(&row[j - p]);
-          const cdd v = ld_cdd(&a.in[(size_t)ad * a.B + b]);
-          cacc_fma(acc, v, us[j * NC + cl]);
-          cacc_fma(g[jj], v, cp);
+          const V v = P::ld(&xin[(size_t)ad * a.B + b]);
+          P::fma(acc, v, us[j * NC + cl]);
+          P::fma(g[jj], v, cp);
         }
       }
-      cdd part = cacc_finish(acc);
+      V part = P::finish(acc);
 #pragma unroll
-      for (int dl = NC; dl < 32; dl <<= 1) {
-        cdd other;
-        other.re.hi = __shfl_xor_sync(0xffffffffu, part.re.hi, dl);
-        other.re.lo = __shfl_xor_sync(0xffffffffu, part.re.lo, dl);
-        other.im.hi = __shfl_xor_sync(0xffffffffu, part.im.hi, dl);
-        other.im.lo = __shfl_xor_sync(0xffffffffu, part.im.lo, dl);
-        part = cdd_add(part, other);
-      }
-      if (grp == 0 && live) a.out[pidx] = part;
+      for (int dl = NC; dl < 32; dl <<= 1) part = P::add(part, P::shfl_xor(part, dl));
+      if (grp == 0 && live) xout[pidx] = part;
     }
   }
   // per-CTA partials: lane l holds mode (l / NC) * MG + jj of circuit l % NC
+  V* gpart = static_cast<V*>(a.gpart);
 #pragma unroll
   for (int jj = 0; jj < MG; ++jj) {
-    red[wid][lane] = cacc_finish(g[jj]);
+    red[wid][lane] = P::finish(g[jj]);
     __syncthreads();
     if (wid == 0) {
-      cdd s2 = red[0][lane];
-      for (int w = 1; w < kWarps; ++w) s2 = cdd_add(s2, red[w][lane]);
+      V s2 = red[0][lane];
+      for (int w = 1; w < kWarps; ++w) s2 = P::add(s2, red[w][lane]);
       const int j = grp * MG + jj;
-      if (j < m && live) a.gpart[((size_t)blockIdx.x * m + j) * a.B + b] = s2;
+      if (j < m && live) gpart[((size_t)blockIdx.x * m + j) * a.B + b] = s2;
     }
     __syncthreads();
   }
@@ -605,32 +604,33 @@ __global__ void __launch_bounds__(256, MMAX <= 16 ? 4 : 2) slos_bwd_g(SlosArgs a
 
 // Last layer -> probabilities (mode 0), amplitudes (mode 1) or the adjoint seed
 // a_n = 2 w F c_n (mode 2), with F = prod(out!) / prod(in!) = f(tile) x ftail[tau].
-__device__ __forceinline__ void fin_state(const SlosArgs& a, dd f, int r, size_t idx, int mode,
+template <class P>
+__device__ __forceinline__ void fin_state(const SlosArgs& a, typename P::F f, int r, size_t idx, int mode,
                                           const double* __restrict__ w_in, double* __restrict__ out_real,
-                                          double2* __restrict__ out_c, cdd* __restrict__ seed, uint32_t tau) {
-  const dd F = dd_mul(f, a.ftail[a.tstate_off[r] + tau]);
-  const cdd c = ld_cdd(&a.in[idx]);
-  if (mode == 0) {
-    const dd c2 = dd_add(dd_mul(c.re, c.re), dd_mul(c.im, c.im));
-    out_real[idx] = dd_to_double_fast(dd_mul(c2, F));
-  } else if (mode == 1) {
-    const double sF = sqrt(dd_to_double_fast(F));
-    out_c[idx] = make_double2(dd_to_double_fast(c.re) * sF, dd_to_double_fast(c.im) * sF);
-  } else {
-    const dd f2 = dd_mul(dd_from_double(2.0 * w_in[idx]), F);
-    seed[idx] = {dd_mul(c.re, f2), dd_mul(c.im, f2)};
-  }
+                                          double2* __restrict__ out_c, void* __restrict__ seed, uint32_t tau) {
+  using V = typename P::V;
+  const typename P::F F = P::f_mul(f, static_cast<const typename P::F*>(a.ftail)[a.tstate_off[r] + tau]);
+  const V c = P::ld(&static_cast<const V*>(a.in)[idx]);
+  if (mode == 0)
+    out_real[idx] = P::prob(c, F);
+  else if (mode == 1)
+    out_c[idx] = P::amp(c, F);
+  else
+    static_cast<V*>(seed)[idx] = P::seed(c, w_in[idx], F);
 }
 
-template <int MMAX>
-__global__ void __launch_bounds__(256) slos_fin(SlosArgs a, dd inv_in, int mode, const double* __restrict__ w_in,
+template <int MMAX, class P>
+__global__ void __launch_bounds__(256) slos_fin(SlosArgs a, int mode, const double* __restrict__ w_in,
                                                double* __restrict__ out_real, double2* __restrict__ out_c,
-                                               cdd* __restrict__ seed) {
+                                               void* __restrict__ seed) {
+  using F = typename P::F;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t* cn = reinterpret_cast<uint32_t*>(smem_raw);
   const int ncn = (a.m + 1) * a.cn_stride;
   for (int i = threadIdx.x; i < ncn; i += blockDim.x) cn[i] = a.cn[i];
   __syncthreads();
+  const F* inv_in = static_cast<const F*>(a.inv_in);
+  const F one = P::f_from(1.0);
   const int lane = threadIdx.x & 31;
   const bool batched = a.B > 1;
   const int b = batched ? blockIdx.y * 32 + lane : 0;
@@ -640,29 +640,30 @@ __global__ void __launch_bounds__(256) slos_fin(SlosArgs a, dd inv_in, int mode,
     const int r = unit_class(a, unit);
     const int q = a.k - r;
     const uint32_t S = a.tsize[r], lu = unit - a.uoff[r], cpt = a.cpt[r];
-    Desc<MMAX> d;
+    Desc<MMAX, F> d;
     if (cpt > 0) {
       const uint32_t pi = lu / cpt, ch = lu - pi * cpt;
-      describe<MMAX, false, true>(pi, q, r, a, cn, d, inv_in, d.base);
+      describe<MMAX, false, true, P>(pi, q, r, a, cn, d, one, d.base);
       const uint32_t chunk = batched ? a.chunkB : kChunk;
       const uint32_t t0 = ch * chunk, t1 = min(S, t0 + chunk);
       if (batched) {
         if (b < a.B) {
-          const dd fb = dd_mul(d.f, a.inv_in[b]);
+          const F fb = P::f_mul(d.f, inv_in[b]);
           for (uint32_t tau = t0; tau < t1; ++tau)
-            fin_state(a, fb, r, (size_t)(d.A + tau) * a.B + b, mode, w_in, out_real, out_c, seed, tau);
+            fin_state<P>(a, fb, r, (size_t)(d.A + tau) * a.B + b, mode, w_in, out_real, out_c, seed, tau);
         }
       } else {
-        const dd fb = dd_mul(d.f, a.inv_in[0]);
+        const F fb = P::f_mul(d.f, inv_in[0]);
         for (uint32_t tau = t0 + lane; tau < t1; tau += 32)
-          fin_state(a, fb, r, d.A + tau, mode, w_in, out_real, out_c, seed, tau);
+          fin_state<P>(a, fb, r, d.A + tau, mode, w_in, out_real, out_c, seed, tau);
       }
     } else {
       const uint32_t pi = lu * 32 + lane;
       if (pi < a.npf[r]) {
-        describe<MMAX, false, true>(pi, q, r, a, cn, d, inv_in, d.base);
-        const dd fb = dd_mul(d.f, a.inv_in[0]);
-        for (uint32_t tau = 0; tau < S; ++tau) fin_state(a, fb, r, d.A + tau, mode, w_in, out_real, out_c, seed, tau);
+        describe<MMAX, false, true, P>(pi, q, r, a, cn, d, one, d.base);
+        const F fb = P::f_mul(d.f, inv_in[0]);
+        for (uint32_t tau = 0; tau < S; ++tau)
+          fin_state<P>(a, fb, r, d.A + tau, mode, w_in, out_real, out_c, seed, tau);
       }
     }
   }
@@ -671,21 +672,22 @@ __global__ void __launch_bounds__(256) slos_fin(SlosArgs a, dd inv_in, int mode,
 // Single-circuit finalisation over the forward kernel's units (uoff1 / cpt1 / grp1):
 // large tiles in chunks with one unranking per unit (lane 0, broadcast), smaller tiles
 // in groups unranked by all lanes at once and swept in rank order, one state per lane.
-template <int MMAX>
+template <int MMAX, class P>
 __global__ void __launch_bounds__(256) slos_fin1(SlosArgs a, int mode, const double* __restrict__ w_in,
                                                 double* __restrict__ out_real, double2* __restrict__ out_c,
-                                                cdd* __restrict__ seed) {
+                                                void* __restrict__ seed) {
+  using F = typename P::F;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t* cn = reinterpret_cast<uint32_t*>(smem_raw);
   const int ncn = (a.m + 1) * a.cn_stride;
   for (int i = threadIdx.x; i < ncn; i += blockDim.x) cn[i] = a.cn[i];
-  // per thread: A, f.hi, f.lo of the tile it unranked
+  // per thread: A and the two words of the factor of the tile it unranked
   uint32_t* slots = reinterpret_cast<uint32_t*>(smem_raw + smem_cn_bytes(a.m, a.cn_stride));
   __syncthreads();
   const int lane = threadIdx.x & 31;
   uint32_t* myslot = slots + (size_t)threadIdx.x * 4;
   const uint32_t* wslots = slots + (size_t)(threadIdx.x - lane) * 4;
-  const dd inv0 = a.inv_in[0];
+  const F inv0 = static_cast<const F*>(a.inv_in)[0];
   const uint32_t total = a.uoff1[a.k + 1];
   const uint32_t nw = gridDim.x * kWarps;
   for (uint32_t unit = blockIdx.x * kWarps + (threadIdx.x >> 5); unit < total; unit += nw) {
@@ -697,39 +699,34 @@ __global__ void __launch_bounds__(256) slos_fin1(SlosArgs a, int mode, const dou
       const uint32_t c0 = (lu - pi * cpt) * a.chunk1;
       const uint32_t c1 = min(S, c0 + a.chunk1);
       uint32_t A = 0;
-      float fh = 0.f, fl = 0.f;
+      F f = P::f_from(0.0);
       if (lane == 0) {
-        Desc<MMAX> d;
-        describe<MMAX, false, true>(pi, q, r, a, cn, d, inv0, d.base);
+        Desc<MMAX, F> d;
+        describe<MMAX, false, true, P>(pi, q, r, a, cn, d, inv0, d.base);
         A = d.A;
-        fh = d.f.hi;
-        fl = d.f.lo;
+        f = d.f;
       }
       A = __shfl_sync(0xffffffffu, A, 0);
-      fh = __shfl_sync(0xffffffffu, fh, 0);
-      fl = __shfl_sync(0xffffffffu, fl, 0);
-      const dd f = {fh, fl};
+      f = P::f_shfl(f, 0);
       for (uint32_t tau = c0 + lane; tau < c1; tau += 32)
-        fin_state(a, f, r, A + tau, mode, w_in, out_real, out_c, seed, tau);
+        fin_state<P>(a, f, r, A + tau, mode, w_in, out_real, out_c, seed, tau);
       continue;
     }
     const uint32_t G = a.grp1[r];
     const uint32_t g0 = lu * G;
     const uint32_t ng = min(G, a.npf[r] - g0);
     if ((uint32_t)lane < ng) {
-      Desc<MMAX> d;
-      describe<MMAX, false, true>(g0 + lane, q, r, a, cn, d, inv0, d.base);
+      Desc<MMAX, F> d;
+      describe<MMAX, false, true, P>(g0 + lane, q, r, a, cn, d, inv0, d.base);
       myslot[0] = d.A;
-      myslot[1] = __float_as_uint(d.f.hi);
-      myslot[2] = __float_as_uint(d.f.lo);
+      P::f_pack(d.f, myslot + 1);
     }
     __syncwarp();
     const uint32_t q32 = 32 / S, r32 = 32 - q32 * S;
     uint32_t g = (uint32_t)lane / S, tau = (uint32_t)lane - g * S;
     while (g < ng) {
       const uint32_t* ws = wslots + (size_t)g * 4;
-      const dd f = {__uint_as_float(ws[1]), __uint_as_float(ws[2])};
-      fin_state(a, f, r, ws[0] + tau, mode, w_in, out_real, out_c, seed, tau);
+      fin_state<P>(a, P::f_unpack(ws + 1), r, ws[0] + tau, mode, w_in, out_real, out_c, seed, tau);
       g += q32;
       tau += r32;
       if (tau >= S) {
@@ -742,96 +739,107 @@ __global__ void __launch_bounds__(256) slos_fin1(SlosArgs a, int mode, const dou
 }
 
 // grad[b][j][col[b]] += sum over CTAs of gpart[cta][j][b]  (col: the layer's column per entry)
-__global__ void slos_grad_reduce(const cdd* __restrict__ gpart, int nblk, int m, int B,
+template <class P>
+__global__ void slos_grad_reduce(const typename P::V* __restrict__ gpart, int nblk, int m, int B,
                                  const int32_t* __restrict__ col, double2* __restrict__ grad) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;  // i = j * B + b
   if (i >= m * B) return;
   const int j = i / B, b = i - j * B;
-  cdd s = cdd_zero();
-  for (int q = 0; q < nblk; ++q) s = cdd_add(s, gpart[(size_t)q * m * B + i]);
+  typename P::V s = P::zero();
+  for (int q = 0; q < nblk; ++q) s = P::add(s, gpart[(size_t)q * m * B + i]);
   double2* g = &grad[((size_t)b * m + j) * m + col[b]];
-  g->x += dd_to_double(s.re);
-  g->y += dd_to_double(s.im);
+  g->x += P::re(s);
+  g->y += P::im(s);
 }
 
-// ucols[k][j][b] = U_b[j][col[k][b]] as float-float, for the n layers (ustride: elements
-// between consecutive entries' unitaries; 0 = one unitary shared by every entry)
+// ucols[k][j][b] = U_b[j][col[k][b]] in the plan's arithmetic, for the n layers (ustride:
+// elements between consecutive entries' unitaries; 0 = one unitary shared by every entry)
+template <class P>
 __global__ void slos_convert_u(const double2* __restrict__ u, int m, int n, int B, size_t ustride,
-                               const int32_t* __restrict__ col, cdd* __restrict__ ucols) {
+                               const int32_t* __restrict__ col, typename P::V* __restrict__ ucols) {
   const size_t tot = (size_t)n * m * B;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
     const size_t kj = i / B;
     const int b = (int)(i - kj * B);
     const int k = (int)(kj / m), j = (int)(kj - (size_t)k * m);
     const double2 v = u[(size_t)b * ustride + (size_t)j * m + col[(size_t)k * B + b]];
-    ucols[i] = cdd_from(v.x, v.y);
+    ucols[i] = P::from(v.x, v.y);
   }
 }
 
-__global__ void slos_fill_vacuum(cdd* layer0, int B) {
+template <class P>
+__global__ void slos_fill_vacuum(typename P::V* layer0, int B) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b < B) layer0[b] = cdd_one();
+  if (b < B) layer0[b] = P::one();
 }
 
 enum class Kern { Fwd, FwdProb, Bwd, Fin };
 
-template <int MMAX>
-static int launch_kernel(Kern kind, const SlosArgs& a, int grid, dd inv_in, int mode, const double* w,
-                         double* out_real, double2* out_c, cdd* seed, cudaStream_t s) {
+template <int MMAX, class P>
+static int launch_kernel(Kern kind, const SlosArgs& a, int grid, int mode, const double* w, double* out_real,
+                         double2* out_c, void* seed, cudaStream_t s) {
+  using V = typename P::V;
   const size_t smem = smem_bytes<MMAX>(a.m, a.cn_stride);
   const bool batched = a.B > 1;
   dim3 g(grid, batched ? (a.B + 31) / 32 : 1);
   // the descriptors of 8 warps, u and the rank table may pass 48 KB: allow it
-  cudaFuncSetAttribute(slos_fwdb<MMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaFuncSetAttribute(slos_bwd<MMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaFuncSetAttribute(slos_fin<MMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(slos_fwdb<MMAX, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(slos_bwd<MMAX, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(slos_fin<MMAX, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   switch (kind) {
     case Kern::Fwd:
       if (batched) {
-        slos_fwdb<MMAX><<<g, 256, smem, s>>>(a);
+        slos_fwdb<MMAX, P><<<g, 256, smem, s>>>(a);
       } else {
-        const size_t smem1 = smem_cn_bytes(a.m, a.cn_stride) + (size_t)MMAX * sizeof(cdd) +
+        const size_t smem1 = smem_cn_bytes(a.m, a.cn_stride) + (size_t)MMAX * sizeof(V) +
                              (size_t)256 * fwd1_slot<MMAX, false>() * sizeof(uint32_t);
-        cudaFuncSetAttribute(slos_fwd1<MMAX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
-        slos_fwd1<MMAX, false><<<g, 256, smem1, s>>>(a, nullptr);
+        cudaFuncSetAttribute(slos_fwd1<MMAX, false, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+        slos_fwd1<MMAX, false, P><<<g, 256, smem1, s>>>(a, nullptr);
       }
       break;
     case Kern::FwdProb: {  // single circuit only
-      const size_t smem1 = smem_cn_bytes(a.m, a.cn_stride) + (size_t)MMAX * sizeof(cdd) +
+      const size_t smem1 = smem_cn_bytes(a.m, a.cn_stride) + (size_t)MMAX * sizeof(V) +
                            (size_t)256 * fwd1_slot<MMAX, true>() * sizeof(uint32_t);
-      cudaFuncSetAttribute(slos_fwd1<MMAX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
-      slos_fwd1<MMAX, true><<<g, 256, smem1, s>>>(a, out_real);
+      cudaFuncSetAttribute(slos_fwd1<MMAX, true, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+      slos_fwd1<MMAX, true, P><<<g, 256, smem1, s>>>(a, out_real);
       break;
     }
     case Kern::Bwd:
       if (batched) {
         constexpr int G = kBwdGroups;
         const dim3 gh(grid, (a.B + 32 / G - 1) / (32 / G));
-        const size_t smemh = smem_cn_bytes(a.m, a.cn_stride) + (size_t)MMAX * (32 / G) * sizeof(cdd);
-        slos_bwd_g<MMAX, G><<<gh, 256, smemh, s>>>(a);
+        const size_t smemh = smem_cn_bytes(a.m, a.cn_stride) + (size_t)MMAX * (32 / G) * sizeof(V);
+        slos_bwd_g<MMAX, G, P><<<gh, 256, smemh, s>>>(a);
       } else {
-        slos_bwd<MMAX><<<g, 256, smem, s>>>(a);
+        slos_bwd<MMAX, P><<<g, 256, smem, s>>>(a);
       }
       break;
     case Kern::Fin:
       if (batched) {
-        slos_fin<MMAX><<<g, 256, smem, s>>>(a, inv_in, mode, w, out_real, out_c, seed);
+        slos_fin<MMAX, P><<<g, 256, smem, s>>>(a, mode, w, out_real, out_c, seed);
       } else {
         const size_t smemf = smem_cn_bytes(a.m, a.cn_stride) + (size_t)256 * 4 * sizeof(uint32_t);
-        slos_fin1<MMAX><<<g, 256, smemf, s>>>(a, mode, w, out_real, out_c, seed);
+        slos_fin1<MMAX, P><<<g, 256, smemf, s>>>(a, mode, w, out_real, out_c, seed);
       }
       break;
   }
   return (int)cudaGetLastError();
 }
 
-static int dispatch(Kern kind, const SlosArgs& a, int grid, cudaStream_t s, dd inv_in = dd{0.f, 0.f},
-                    int mode = 0, const double* w = nullptr, double* out_real = nullptr, double2* out_c = nullptr,
-                    cdd* seed = nullptr) {
-  if (a.m <= 8) return launch_kernel<8>(kind, a, grid, inv_in, mode, w, out_real, out_c, seed, s);
-  if (a.m <= 16) return launch_kernel<16>(kind, a, grid, inv_in, mode, w, out_real, out_c, seed, s);
-  if (a.m <= 24) return launch_kernel<24>(kind, a, grid, inv_in, mode, w, out_real, out_c, seed, s);
-  return launch_kernel<32>(kind, a, grid, inv_in, mode, w, out_real, out_c, seed, s);
+template <class P>
+static int dispatch_p(Kern kind, const SlosArgs& a, int grid, cudaStream_t s, int mode, const double* w,
+                      double* out_real, double2* out_c, void* seed) {
+  if (a.m <= 8) return launch_kernel<8, P>(kind, a, grid, mode, w, out_real, out_c, seed, s);
+  if (a.m <= 16) return launch_kernel<16, P>(kind, a, grid, mode, w, out_real, out_c, seed, s);
+  if (a.m <= 24) return launch_kernel<24, P>(kind, a, grid, mode, w, out_real, out_c, seed, s);
+  return launch_kernel<32, P>(kind, a, grid, mode, w, out_real, out_c, seed, s);
+}
+
+static int dispatch(int prec, Kern kind, const SlosArgs& a, int grid, cudaStream_t s, int mode = 0,
+                    const double* w = nullptr, double* out_real = nullptr, double2* out_c = nullptr,
+                    void* seed = nullptr) {
+  if (prec == kPrecFP64) return dispatch_p<Arith64>(kind, a, grid, s, mode, w, out_real, out_c, seed);
+  return dispatch_p<ArithFF>(kind, a, grid, s, mode, w, out_real, out_c, seed);
 }
 
 }  // namespace pcvl
@@ -890,7 +898,7 @@ uint32_t tail_rank(int t, const std::vector<int>& s) {
 // Tail tables for t tail modes and 0..n tail photons (descending-lex order within each
 // photon number): parent ranks rank_t(tau - e_j) (kNone where tau_j = 0), child ranks
 // rank_t(tau + e_j), and the factorial products prod_j tau_j!.
-void tail_tables(int t, int n, std::vector<uint32_t>& tp, std::vector<uint32_t>& tc, std::vector<dd>& ftail,
+void tail_tables(int t, int n, std::vector<uint32_t>& tp, std::vector<uint32_t>& tc, std::vector<double>& ftail,
                  std::vector<uint8_t>& tocc, std::vector<uint32_t>& tail_off, std::vector<uint32_t>& tstate_off,
                  std::vector<uint32_t>& tsize) {
   tail_off.assign(n + 2, 0);
@@ -924,7 +932,7 @@ void tail_tables(int t, int n, std::vector<uint32_t>& tp, std::vector<uint32_t>&
         tc.push_back(tail_rank(t, s));
         s[j] -= 1;
       }
-      ftail.push_back(dd_from_double(f));
+      ftail.push_back(f);
       tocc.push_back(occ);
       int tail = 0;  // next state in descending-lex order
       for (int i = t - 2; i >= 0; --i) {
@@ -938,6 +946,20 @@ void tail_tables(int t, int n, std::vector<uint32_t>& tp, std::vector<uint32_t>&
       }
     }
   }
+}
+
+// factors of the plan's arithmetic as 8-byte words: dd (float-float) or double (FP64)
+std::vector<uint64_t> factor_words(const std::vector<double>& x, int prec) {
+  std::vector<uint64_t> w(x.size());
+  for (size_t i = 0; i < x.size(); ++i) {
+    if (prec == kPrecFP64) {
+      memcpy(&w[i], &x[i], 8);
+    } else {
+      const dd v = dd_from_double(x[i]);
+      memcpy(&w[i], &v, 8);
+    }
+  }
+  return w;
 }
 
 int alloc(void** p, size_t bytes, int64_t& total) {
@@ -1037,13 +1059,20 @@ int grid_for_units(const SlosArgs& a, bool fwd1 = false) {
 
 int pcvl::slos_alloc(void** p, size_t bytes, int64_t& total) { return alloc(p, bytes, total); }
 int pcvl::slos_upload(void* dst, const void* src, size_t bytes) { return upload(dst, src, bytes); }
+std::vector<uint64_t> pcvl::slos_factor_words(const std::vector<double>& x, int prec) {
+  return factor_words(x, prec);
+}
 std::vector<int> pcvl::slos_path_order(const std::vector<int>& input) { return path_order(input); }
 void pcvl::slos_free_plan(pcvl_slos_plan* p) { free_plan(p); }
 
 // Plan for `batch` entries with input states inputs[b * m .. b * m + m - 1].
-static int create_plan(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, int32_t batch, int32_t keep_layers) {
+static int create_plan(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, int32_t batch, int32_t keep_layers,
+                       int32_t precision) {
   PCVL_CHECK(plan && inputs, "null pointer argument");
   *plan = nullptr;
+  PCVL_CHECK(precision == kPrecFP64 || precision == kPrecFloatFloat,
+             "precision must be %d (FP64) or %d (float-float), got %d", (int)kPrecFP64, (int)kPrecFloatFloat,
+             precision);
   PCVL_CHECK(m >= 1 && m <= kSlosMaxM, "m=%d outside [1, %d]", m, kSlosMaxM);
   PCVL_CHECK(batch >= 1, "batch must be >= 1");
   int n = -1;
@@ -1064,10 +1093,11 @@ static int create_plan(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, 
   p->m = m;
   p->n = n;
   p->B = batch;
+  p->prec = precision;
   p->keep = keep_layers != 0;
   p->inputs.assign(inputs, inputs + (size_t)batch * m);
   p->col.assign((size_t)std::max(n, 1) * batch, 0);
-  std::vector<dd> inv_in(batch);
+  std::vector<double> inv_in_v(batch);
   for (int b = 0; b < batch; ++b) {
     const std::vector<int> in(inputs + (size_t)b * m, inputs + (size_t)(b + 1) * m);
     const std::vector<int> order = path_order(in);
@@ -1075,8 +1105,9 @@ static int create_plan(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, 
     double f = 1.0;
     for (int i = 0; i < m; ++i)
       for (int v = 2; v <= in[i]; ++v) f *= v;
-    inv_in[b] = dd_from_double(1.0 / f);
+    inv_in_v[b] = 1.0 / f;
   }
+  const std::vector<uint64_t> inv_in = factor_words(inv_in_v, precision);
   p->sizes.resize(n + 1);
   for (int k = 0; k <= n; ++k) {
     p->sizes[k] = fock_count(m, k);
@@ -1114,9 +1145,10 @@ static int create_plan(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, 
   p->tail_t = t;
   p->tail_p = m - t;
   std::vector<uint32_t> tp, tc;
-  std::vector<dd> ftail;
+  std::vector<double> ftail_v;
   std::vector<uint8_t> tocc;
-  tail_tables(t, n, tp, tc, ftail, tocc, p->tail_off, p->tstate_off, p->tsize);
+  tail_tables(t, n, tp, tc, ftail_v, tocc, p->tail_off, p->tstate_off, p->tsize);
+  const std::vector<uint64_t> ftail = factor_words(ftail_v, precision);
   p->cn_stride = n + 2;
   std::vector<uint32_t> cn((size_t)(m + 1) * p->cn_stride);
   for (int M = 0; M <= m; ++M)
@@ -1132,12 +1164,12 @@ static int create_plan(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, 
   if ((rc = upload(p->tc_d, tc.data(), tc.size() * 4)) != PCVL_OK) goto fail;
   if ((rc = alloc((void**)&p->tocc_d, tocc.size(), p->bytes)) != PCVL_OK) goto fail;
   if ((rc = upload(p->tocc_d, tocc.data(), tocc.size())) != PCVL_OK) goto fail;
-  if ((rc = alloc((void**)&p->ftail_d, ftail.size() * sizeof(dd), p->bytes)) != PCVL_OK) goto fail;
-  if ((rc = upload(p->ftail_d, ftail.data(), ftail.size() * sizeof(dd))) != PCVL_OK) goto fail;
+  if ((rc = alloc((void**)&p->ftail_d, ftail.size() * 8, p->bytes)) != PCVL_OK) goto fail;
+  if ((rc = upload(p->ftail_d, ftail.data(), ftail.size() * 8)) != PCVL_OK) goto fail;
   if ((rc = alloc((void**)&p->col_d, p->col.size() * 4, p->bytes)) != PCVL_OK) goto fail;
   if ((rc = upload(p->col_d, p->col.data(), p->col.size() * 4)) != PCVL_OK) goto fail;
-  if ((rc = alloc((void**)&p->inv_in_d, B * sizeof(dd), p->bytes)) != PCVL_OK) goto fail;
-  if ((rc = upload(p->inv_in_d, inv_in.data(), B * sizeof(dd))) != PCVL_OK) goto fail;
+  if ((rc = alloc((void**)&p->inv_in_d, B * 8, p->bytes)) != PCVL_OK) goto fail;
+  if ((rc = upload(p->inv_in_d, inv_in.data(), B * 8)) != PCVL_OK) goto fail;
   if ((rc = alloc((void**)&p->ucols_d, (size_t)std::max(n, 1) * m * B * sizeof(cdd), p->bytes)) != PCVL_OK)
     goto fail;
   if (p->keep) {
@@ -1167,18 +1199,18 @@ fail:
 }
 
 extern "C" int pcvl_slos_plan_create(pcvl_slos_plan** plan, int32_t m, const int32_t* input_state_h,
-                                     int32_t batch, int32_t keep_layers) {
+                                     int32_t batch, int32_t keep_layers, int32_t precision) {
   PCVL_CHECK(plan && input_state_h, "null pointer argument");
   PCVL_CHECK(m >= 1 && m <= kSlosMaxM, "m=%d outside [1, %d]", m, kSlosMaxM);
   PCVL_CHECK(batch >= 1, "batch must be >= 1");
   std::vector<int32_t> inputs((size_t)batch * m);
   for (int b = 0; b < batch; ++b) std::copy(input_state_h, input_state_h + m, inputs.begin() + (size_t)b * m);
-  return create_plan(plan, m, inputs.data(), batch, keep_layers);
+  return create_plan(plan, m, inputs.data(), batch, keep_layers, precision);
 }
 
 extern "C" int pcvl_slos_plan_create_multi(pcvl_slos_plan** plan, int32_t m, const int32_t* input_states_h,
-                                           int32_t batch, int32_t keep_layers) {
-  return create_plan(plan, m, input_states_h, batch, keep_layers);
+                                           int32_t batch, int32_t keep_layers, int32_t precision) {
+  return create_plan(plan, m, input_states_h, batch, keep_layers, precision);
 }
 
 extern "C" int pcvl_slos_plan_destroy(pcvl_slos_plan* plan) {
@@ -1205,10 +1237,17 @@ static int forward(pcvl_slos_plan* p, const double* u_d, size_t ustride, cudaStr
   if (p->n > 0) {
     const uint64_t tot = (uint64_t)p->n * m * B;
     const int g = (int)std::max<uint64_t>(1, std::min<uint64_t>((tot + 255) / 256, 4096));
-    slos_convert_u<<<g, 256, 0, s>>>((const double2*)u_d, m, p->n, B, ustride, p->col_d, p->ucols_d);
+    if (p->prec == kPrecFP64)
+      slos_convert_u<Arith64><<<g, 256, 0, s>>>((const double2*)u_d, m, p->n, B, ustride, p->col_d,
+                                                (double2*)p->ucols_d);
+    else
+      slos_convert_u<ArithFF><<<g, 256, 0, s>>>((const double2*)u_d, m, p->n, B, ustride, p->col_d, p->ucols_d);
   }
   PCVL_CUDA(cudaGetLastError());
-  slos_fill_vacuum<<<(B + 255) / 256, 256, 0, s>>>(p->layers[0], B);
+  if (p->prec == kPrecFP64)
+    slos_fill_vacuum<Arith64><<<(B + 255) / 256, 256, 0, s>>>((double2*)p->layers[0], B);
+  else
+    slos_fill_vacuum<ArithFF><<<(B + 255) / 256, 256, 0, s>>>(p->layers[0], B);
   PCVL_CUDA(cudaGetLastError());
   if (p->masked) {
     PCVL_TRY(slos_masked_forward(p, s));
@@ -1222,8 +1261,8 @@ static int forward(pcvl_slos_plan* p, const double* u_d, size_t ustride, cudaStr
     a.ucol = p->ucols_d + (size_t)(k - 1) * m * B;
     a.tail = p->tp_d;
     const bool fuse = probs && k == p->n;
-    const int rc = fuse ? dispatch(Kern::FwdProb, a, grid_for_units(a, true), s, dd{0.f, 0.f}, 0, nullptr, probs)
-                        : dispatch(Kern::Fwd, a, grid_for_units(a, B == 1), s);
+    const int rc = fuse ? dispatch(p->prec, Kern::FwdProb, a, grid_for_units(a, true), s, 0, nullptr, probs)
+                        : dispatch(p->prec, Kern::Fwd, a, grid_for_units(a, B == 1), s);
     if (rc != 0) {
       set_error("SLOS layer %d launch failed: %s", k, cudaGetErrorString((cudaError_t)rc));
       return PCVL_ERR_CUDA;
@@ -1243,7 +1282,7 @@ extern "C" int pcvl_slos_forward_shared(pcvl_slos_plan* p, const double* u_d, vo
   return forward(p, u_d, 0, (cudaStream_t)stream);
 }
 
-static int finalize(pcvl_slos_plan* p, int mode, const double* w, double* out_real, double2* out_c, cdd* seed,
+static int finalize(pcvl_slos_plan* p, int mode, const double* w, double* out_real, double2* out_c, void* seed,
                     cudaStream_t s);
 
 extern "C" int pcvl_slos_forward_probabilities(pcvl_slos_plan* p, const double* u_d, double* probs_d, void* stream) {
@@ -1257,14 +1296,13 @@ extern "C" int pcvl_slos_forward_probabilities(pcvl_slos_plan* p, const double* 
   return forward(p, u_d, ustride, s, probs_d);
 }
 
-static int finalize(pcvl_slos_plan* p, int mode, const double* w, double* out_real, double2* out_c, cdd* seed,
+static int finalize(pcvl_slos_plan* p, int mode, const double* w, double* out_real, double2* out_c, void* seed,
                     cudaStream_t s) {
   PCVL_CHECK(p->forwarded, "pcvl_slos_forward has not run on this plan");
   if (p->masked) return slos_masked_finalize(p, mode, w, out_real, out_c, seed, s);
   SlosArgs a = make_args(p, p->n);
   a.in = p->final_layer();
-  const int rc = dispatch(Kern::Fin, a, grid_for_units(a, p->B == 1), s, dd_from_double(1.0),
-                          mode, w, out_real, out_c, seed);
+  const int rc = dispatch(p->prec, Kern::Fin, a, grid_for_units(a, p->B == 1), s, mode, w, out_real, out_c, seed);
   if (rc != 0) {
     set_error("SLOS finalize launch failed: %s", cudaGetErrorString((cudaError_t)rc));
     return PCVL_ERR_CUDA;
@@ -1300,13 +1338,17 @@ extern "C" int pcvl_slos_backward(pcvl_slos_plan* p, const double* weights_d, do
     a.gpart = p->gpart_d;
     a.tail = p->tc_d;
     const int grid = std::min(p->gpart_blocks, grid_for_units(a));
-    const int rc = dispatch(Kern::Bwd, a, grid, s);
+    const int rc = dispatch(p->prec, Kern::Bwd, a, grid, s);
     if (rc != 0) {
       set_error("SLOS adjoint layer %d launch failed: %s", k, cudaGetErrorString((cudaError_t)rc));
       return PCVL_ERR_CUDA;
     }
-    slos_grad_reduce<<<(m * B + 255) / 256, 256, 0, s>>>(p->gpart_d, grid, m, B, p->col_d + (size_t)(k - 1) * B,
-                                                         (double2*)grad_u_d);
+    if (p->prec == kPrecFP64)
+      slos_grad_reduce<Arith64><<<(m * B + 255) / 256, 256, 0, s>>>(
+          (const double2*)p->gpart_d, grid, m, B, p->col_d + (size_t)(k - 1) * B, (double2*)grad_u_d);
+    else
+      slos_grad_reduce<ArithFF><<<(m * B + 255) / 256, 256, 0, s>>>(
+          p->gpart_d, grid, m, B, p->col_d + (size_t)(k - 1) * B, (double2*)grad_u_d);
     PCVL_CUDA(cudaGetLastError());
   }
   return PCVL_OK;

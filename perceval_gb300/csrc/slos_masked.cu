@@ -35,11 +35,15 @@
 // the photons in modes after i,
 //     rank(s)       = sum_{i <= m-2} Cn(m - i, R_{i+1} - 1)
 //     rank(p + e_j) = rank(p) + sum_{i < j} Cn(m - i - 1, R_{i+1}(p)).
+//
+// Arithmetic: the kernels are instantiated for the two policies of arith.cuh (FP64, the
+// default, and float-float), as the full-space kernels of slos.cu.
 #include <algorithm>
 #include <cstring>
 #include <new>
 #include <vector>
 
+#include "arith.cuh"
 #include "common.cuh"
 #include "runtime.cuh"
 #include "slos_plan.cuh"
@@ -223,8 +227,8 @@ constexpr int kParentRun = 16;  // most consecutive kept states per thread of ma
 __global__ void __launch_bounds__(256) mask_parents(MaskSpace sg, int k, const uint64_t* __restrict__ cur,
                                                     uint64_t ncur, const uint64_t* __restrict__ prev,
                                                     uint64_t nprev, uint32_t* __restrict__ occ,
-                                                    uint32_t* __restrict__ par, dd* __restrict__ fact,
-                                                    int* __restrict__ err, int run_len) {
+                                                    uint32_t* __restrict__ par, void* __restrict__ fact,
+                                                    int fact_f64, int* __restrict__ err, int run_len) {
   __shared__ uint64_t cn_s[kCnWords];
   const MaskSpace s = shared_cn(sg, cn_s);
   const uint64_t runs = (ncur + run_len - 1) / run_len;
@@ -261,7 +265,12 @@ __global__ void __launch_bounds__(256) mask_parents(MaskSpace sg, int k, const u
         sub += cnv(s, s.m - j - 1, after - 1);
       }
       occ[i] = om;
-      if (fact) fact[i] = dd_from_double(f);
+      if (fact) {
+        if (fact_f64)
+          static_cast<double*>(fact)[i] = f;
+        else
+          static_cast<dd*>(fact)[i] = dd_from_double(f);
+      }
     }
   }
 }
@@ -282,17 +291,18 @@ __global__ void __launch_bounds__(256) mask_children(const uint32_t* __restrict_
 }
 
 // u_j (conjugated for the adjoint) of one circuit, or of the CTA's 32 circuits as [j][lane]
-template <bool BATCHED, bool CONJ>
-__device__ __forceinline__ void load_u(cdd* us, const cdd* __restrict__ ucol, int m, int B) {
+template <bool BATCHED, bool CONJ, class P>
+__device__ __forceinline__ void load_u(typename P::V* us, const typename P::V* __restrict__ ucol, int m, int B) {
+  using V = typename P::V;
   if (BATCHED) {
     for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) {
       const int j = t >> 5, b = blockIdx.y * 32 + (t & 31);
-      const cdd v = (j < m && b < B) ? ucol[(size_t)j * B + b] : cdd_zero();
-      us[t] = CONJ ? cdd_conj(v) : v;
+      const V v = (j < m && b < B) ? ucol[(size_t)j * B + b] : P::zero();
+      us[t] = CONJ ? P::conj(v) : v;
     }
   } else if (threadIdx.x < 32) {
-    const cdd v = (int)threadIdx.x < m ? ucol[threadIdx.x] : cdd_zero();
-    us[threadIdx.x] = CONJ ? cdd_conj(v) : v;
+    const V v = (int)threadIdx.x < m ? ucol[threadIdx.x] : P::zero();
+    us[threadIdx.x] = CONJ ? P::conj(v) : v;
   }
   __syncthreads();
 }
@@ -300,126 +310,122 @@ __device__ __forceinline__ void load_u(cdd* us, const cdd* __restrict__ ucol, in
 // Layer k: c_k[i] = sum_e u_{j_e} c_{k-1}[par[e][i]] over the occupied modes j_e of kept
 // state i.  One thread per state (one circuit) or one warp per state with the lanes
 // over 32 circuits (blockIdx.y selects the chunk).
-template <bool BATCHED>
-__global__ void __launch_bounds__(256) slos_mfwd(const cdd* __restrict__ in, cdd* __restrict__ out,
+template <bool BATCHED, class P>
+__global__ void __launch_bounds__(256) slos_mfwd(const typename P::V* __restrict__ in, typename P::V* __restrict__ out,
                                                  const uint32_t* __restrict__ occ,
                                                  const uint32_t* __restrict__ par, uint64_t L,
-                                                 const cdd* __restrict__ ucol, int m, int B) {
-  __shared__ cdd us[BATCHED ? 32 * 32 : 32];
-  load_u<BATCHED, false>(us, ucol, m, B);
+                                                 const typename P::V* __restrict__ ucol, int m, int B) {
+  using V = typename P::V;
+  __shared__ V us[BATCHED ? 32 * 32 : 32];
+  load_u<BATCHED, false, P>(us, ucol, m, B);
   if (!BATCHED) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < L; i += stride) {
-      cacc acc = cacc_zero();
+      typename P::Acc acc = P::acc_zero();
       uint64_t e = i;
       for (uint32_t om = __ldg(&occ[i]); om; om &= om - 1, e += L)
-        cacc_fma(acc, ld_cdd(&in[__ldg(&par[e])]), us[__ffs(om) - 1]);
-      out[i] = cacc_finish(acc);
+        P::fma(acc, P::ld(&in[__ldg(&par[e])]), us[__ffs(om) - 1]);
+      out[i] = P::finish(acc);
     }
   } else {
     const int lane = threadIdx.x & 31;
     const int b = blockIdx.y * 32 + lane;
     const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x >> 5);
     for (uint64_t i = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < L; i += nw) {
-      cacc acc = cacc_zero();
+      typename P::Acc acc = P::acc_zero();
       uint64_t e = i;
       for (uint32_t om = __ldg(&occ[i]); om; om &= om - 1, e += L) {
         const uint32_t pidx = __ldg(&par[e]);
-        if (b < B) cacc_fma(acc, ld_cdd(&in[(size_t)pidx * B + b]), us[(__ffs(om) - 1) * 32 + lane]);
+        if (b < B) P::fma(acc, P::ld(&in[(size_t)pidx * B + b]), us[(__ffs(om) - 1) * 32 + lane]);
       }
-      if (b < B) out[i * B + b] = cacc_finish(acc);
+      if (b < B) out[i * B + b] = P::finish(acc);
     }
   }
 }
 
 // Kept outputs -> probabilities (mode 0), amplitudes (mode 1) or the adjoint seed
 // a_n = 2 w F c_n (mode 2), with F = prod(out!) / prod(in_b!).
-__global__ void __launch_bounds__(256) slos_mfin(const cdd* __restrict__ c, const dd* __restrict__ fact,
-                                                 const dd* __restrict__ inv_in, uint64_t L, int B, int mode,
-                                                 const double* __restrict__ w, double* __restrict__ out_real,
-                                                 double2* __restrict__ out_c, cdd* __restrict__ seed) {
+template <class P>
+__global__ void __launch_bounds__(256) slos_mfin(const typename P::V* __restrict__ c,
+                                                 const typename P::F* __restrict__ fact,
+                                                 const typename P::F* __restrict__ inv_in, uint64_t L, int B,
+                                                 int mode, const double* __restrict__ w,
+                                                 double* __restrict__ out_real, double2* __restrict__ out_c,
+                                                 typename P::V* __restrict__ seed) {
   const uint64_t tot = L * (uint64_t)B;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < tot; idx += stride) {
     const uint64_t i = idx / (uint64_t)B;
     const int b = (int)(idx - i * (uint64_t)B);
-    const dd F = dd_mul(fact[i], inv_in[b]);
-    const cdd v = ld_cdd(&c[idx]);
-    if (mode == 0) {
-      const dd c2 = dd_add(dd_mul(v.re, v.re), dd_mul(v.im, v.im));
-      out_real[idx] = dd_to_double_fast(dd_mul(c2, F));
-    } else if (mode == 1) {
-      const double sF = sqrt(dd_to_double_fast(F));
-      out_c[idx] = make_double2(dd_to_double_fast(v.re) * sF, dd_to_double_fast(v.im) * sF);
-    } else {
-      const dd f2 = dd_mul(dd_from_double(2.0 * w[idx]), F);
-      seed[idx] = {dd_mul(v.re, f2), dd_mul(v.im, f2)};
-    }
+    const typename P::F F = P::f_mul(fact[i], inv_in[b]);
+    const typename P::V v = P::ld(&c[idx]);
+    if (mode == 0)
+      out_real[idx] = P::prob(v, F);
+    else if (mode == 1)
+      out_c[idx] = P::amp(v, F);
+    else
+      seed[idx] = P::seed(v, w[idx], F);
   }
 }
 
 // Adjoint step over the kept states of layer k-1: a_{k-1}[i] = sum_j conj(u_j) a_k[child_j(i)]
 // and g_j += conj(c_{k-1}[i]) a_k[child_j(i)] over the kept children; per-CTA partials of
 // g to gpart[cta][j][b].
-template <int MMAX, bool BATCHED>
-__global__ void __launch_bounds__(256) slos_mbwd(const cdd* __restrict__ ain, cdd* __restrict__ aout,
-                                                 const cdd* __restrict__ cpar, const uint32_t* __restrict__ child,
-                                                 uint64_t Lp, const cdd* __restrict__ ucol, int m, int B,
-                                                 cdd* __restrict__ gpart) {
-  __shared__ cdd us[BATCHED ? 32 * 32 : 32];
-  __shared__ cdd red[8][32];
-  load_u<BATCHED, true>(us, ucol, m, B);
+template <int MMAX, bool BATCHED, class P>
+__global__ void __launch_bounds__(256) slos_mbwd(const typename P::V* __restrict__ ain,
+                                                 typename P::V* __restrict__ aout,
+                                                 const typename P::V* __restrict__ cpar,
+                                                 const uint32_t* __restrict__ child, uint64_t Lp,
+                                                 const typename P::V* __restrict__ ucol, int m, int B,
+                                                 typename P::V* __restrict__ gpart) {
+  using V = typename P::V;
+  __shared__ V us[BATCHED ? 32 * 32 : 32];
+  __shared__ V red[8][32];
+  load_u<BATCHED, true, P>(us, ucol, m, B);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int b = BATCHED ? blockIdx.y * 32 + lane : 0;
-  cacc g[MMAX];
+  typename P::Acc g[MMAX];
 #pragma unroll
-  for (int j = 0; j < MMAX; ++j) g[j] = cacc_zero();
+  for (int j = 0; j < MMAX; ++j) g[j] = P::acc_zero();
   const uint64_t per = BATCHED ? (blockDim.x >> 5) : blockDim.x;
   const uint64_t first = (uint64_t)blockIdx.x * per + (BATCHED ? wid : threadIdx.x);
   const uint64_t stride = (uint64_t)gridDim.x * per;
   for (uint64_t i = first; i < Lp; i += stride) {
     if (BATCHED && b >= B) continue;
     const size_t pidx = BATCHED ? (size_t)i * B + b : (size_t)i;
-    const cdd cp = cdd_conj(ld_cdd(&cpar[pidx]));
-    cacc acc = cacc_zero();
+    const V cp = P::conj(P::ld(&cpar[pidx]));
+    typename P::Acc acc = P::acc_zero();
 #pragma unroll
     for (int j = 0; j < MMAX; ++j) {
       if (j < m) {
         const uint32_t ci = __ldg(&child[(uint64_t)j * Lp + i]);
         if (ci != kNoIdx) {
-          const cdd v = ld_cdd(&ain[BATCHED ? (size_t)ci * B + b : (size_t)ci]);
-          cacc_fma(acc, v, us[BATCHED ? j * 32 + lane : j]);
-          cacc_fma(g[j], v, cp);
+          const V v = P::ld(&ain[BATCHED ? (size_t)ci * B + b : (size_t)ci]);
+          P::fma(acc, v, us[BATCHED ? j * 32 + lane : j]);
+          P::fma(g[j], v, cp);
         }
       }
     }
-    aout[pidx] = cacc_finish(acc);
+    aout[pidx] = P::finish(acc);
   }
 #pragma unroll
   for (int j = 0; j < MMAX; ++j) {
     if (j >= m) break;
-    cdd v = cacc_finish(g[j]);
+    V v = P::finish(g[j]);
     if (!BATCHED) {
 #pragma unroll
-      for (int dlt = 16; dlt > 0; dlt >>= 1) {
-        cdd o;
-        o.re.hi = __shfl_down_sync(0xffffffffu, v.re.hi, dlt);
-        o.re.lo = __shfl_down_sync(0xffffffffu, v.re.lo, dlt);
-        o.im.hi = __shfl_down_sync(0xffffffffu, v.im.hi, dlt);
-        o.im.lo = __shfl_down_sync(0xffffffffu, v.im.lo, dlt);
-        v = cdd_add(v, o);
-      }
+      for (int dlt = 16; dlt > 0; dlt >>= 1) v = P::add(v, P::shfl_down(v, dlt));
     }
     red[wid][lane] = v;
     __syncthreads();
     if (wid == 0) {
       if (BATCHED) {
-        cdd s2 = red[0][lane];
-        for (int q = 1; q < 8; ++q) s2 = cdd_add(s2, red[q][lane]);
+        V s2 = red[0][lane];
+        for (int q = 1; q < 8; ++q) s2 = P::add(s2, red[q][lane]);
         if (b < B) gpart[((size_t)blockIdx.x * m + j) * B + b] = s2;
       } else if (lane == 0) {
-        cdd s2 = red[0][0];
-        for (int q = 1; q < 8; ++q) s2 = cdd_add(s2, red[q][0]);
+        V s2 = red[0][0];
+        for (int q = 1; q < 8; ++q) s2 = P::add(s2, red[q][0]);
         gpart[(size_t)blockIdx.x * m + j] = s2;
       }
     }
@@ -428,16 +434,17 @@ __global__ void __launch_bounds__(256) slos_mbwd(const cdd* __restrict__ ain, cd
 }
 
 // grad[b][j][col[b]] += sum over CTAs of gpart[cta][j][b]
-__global__ void slos_mgrad_reduce(const cdd* __restrict__ gpart, int nblk, int m, int B,
+template <class P>
+__global__ void slos_mgrad_reduce(const typename P::V* __restrict__ gpart, int nblk, int m, int B,
                                   const int32_t* __restrict__ col, double2* __restrict__ grad) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m * B) return;
   const int j = i / B, b = i - j * B;
-  cdd s = cdd_zero();
-  for (int q = 0; q < nblk; ++q) s = cdd_add(s, gpart[(size_t)q * m * B + i]);
+  typename P::V s = P::zero();
+  for (int q = 0; q < nblk; ++q) s = P::add(s, gpart[(size_t)q * m * B + i]);
   double2* g = &grad[((size_t)b * m + j) * m + col[b]];
-  g->x += dd_to_double(s.re);
-  g->y += dd_to_double(s.im);
+  g->x += P::re(s);
+  g->y += P::im(s);
 }
 
 // device buffer released at scope exit unless taken
@@ -465,13 +472,29 @@ int grid_for(uint64_t threads, int per_sm) {
   return (int)std::max<uint64_t>(g, 1);
 }
 
-template <int MMAX>
-void launch_mbwd(bool batched, dim3 grid, const cdd* ain, cdd* aout, const cdd* cpar, const uint32_t* child,
-                 uint64_t Lp, const cdd* ucol, int m, int B, cdd* gpart, cudaStream_t s) {
+template <int MMAX, class P>
+void launch_mbwd(bool batched, dim3 grid, const void* ain, void* aout, const void* cpar, const uint32_t* child,
+                 uint64_t Lp, const void* ucol, int m, int B, void* gpart, cudaStream_t s) {
+  using V = typename P::V;
   if (batched)
-    slos_mbwd<MMAX, true><<<grid, 256, 0, s>>>(ain, aout, cpar, child, Lp, ucol, m, B, gpart);
+    slos_mbwd<MMAX, true, P><<<grid, 256, 0, s>>>((const V*)ain, (V*)aout, (const V*)cpar, child, Lp,
+                                                  (const V*)ucol, m, B, (V*)gpart);
   else
-    slos_mbwd<MMAX, false><<<grid, 256, 0, s>>>(ain, aout, cpar, child, Lp, ucol, m, B, gpart);
+    slos_mbwd<MMAX, false, P><<<grid, 256, 0, s>>>((const V*)ain, (V*)aout, (const V*)cpar, child, Lp,
+                                                   (const V*)ucol, m, B, (V*)gpart);
+}
+
+template <class P>
+void launch_mbwd_m(bool batched, dim3 grid, const void* ain, void* aout, const void* cpar, const uint32_t* child,
+                   uint64_t Lp, const void* ucol, int m, int B, void* gpart, cudaStream_t s) {
+  if (m <= 8)
+    launch_mbwd<8, P>(batched, grid, ain, aout, cpar, child, Lp, ucol, m, B, gpart, s);
+  else if (m <= 16)
+    launch_mbwd<16, P>(batched, grid, ain, aout, cpar, child, Lp, ucol, m, B, gpart, s);
+  else if (m <= 24)
+    launch_mbwd<24, P>(batched, grid, ain, aout, cpar, child, Lp, ucol, m, B, gpart, s);
+  else
+    launch_mbwd<32, P>(batched, grid, ain, aout, cpar, child, Lp, ucol, m, B, gpart, s);
 }
 
 }  // namespace
@@ -491,9 +514,12 @@ void slos_masked_free(pcvl_slos_plan* p) {
 
 int slos_masked_create(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, int32_t batch,
                        int32_t keep_layers, int32_t n_masks, const int8_t* digits, uint32_t at_least,
-                       int32_t mask_n) {
+                       int32_t mask_n, int32_t precision) {
   PCVL_CHECK(plan && inputs && digits, "null pointer argument");
   *plan = nullptr;
+  PCVL_CHECK(precision == kPrecFP64 || precision == kPrecFloatFloat,
+             "precision must be %d (FP64) or %d (float-float), got %d", (int)kPrecFP64, (int)kPrecFloatFloat,
+             precision);
   PCVL_CHECK(m >= 1 && m <= kMaskMaxM, "m=%d outside [1, %d]", m, kMaskMaxM);
   PCVL_CHECK(batch >= 1, "batch must be >= 1");
   PCVL_CHECK(n_masks >= 1 && n_masks <= kMaxMasks, "n_masks=%d outside [1, %d]", n_masks, kMaxMasks);
@@ -516,13 +542,14 @@ int slos_masked_create(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, 
   auto* p = new (std::nothrow) pcvl_slos_plan();
   PCVL_CHECK(p, "host allocation failed");
   p->masked = true;
+  p->prec = precision;
   p->m = m;
   p->n = n;
   p->B = batch;
   p->keep = keep_layers != 0;
   p->inputs.assign(inputs, inputs + (size_t)batch * m);
   p->col.assign((size_t)std::max(n, 1) * batch, 0);
-  std::vector<dd> inv_in(batch);
+  std::vector<double> inv_in_v(batch);
   for (int b = 0; b < batch; ++b) {
     const std::vector<int> in(inputs + (size_t)b * m, inputs + (size_t)(b + 1) * m);
     const std::vector<int> order = slos_path_order(in);
@@ -530,8 +557,9 @@ int slos_masked_create(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, 
     double f = 1.0;
     for (int i = 0; i < m; ++i)
       for (int v = 2; v <= in[i]; ++v) f *= v;
-    inv_in[b] = dd_from_double(1.0 / f);
+    inv_in_v[b] = 1.0 / f;
   }
+  const std::vector<uint64_t> inv_in = slos_factor_words(inv_in_v, precision);
   p->sizes.assign(n + 1, 0);
   p->sizes[0] = 1;
   p->mocc_d.assign(n + 1, nullptr);
@@ -614,13 +642,13 @@ int slos_masked_create(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, 
     const uint64_t width = (uint64_t)std::min(k, m);
     if ((rc = slos_alloc((void**)&p->mocc_d[k], total * 4, p->bytes)) != PCVL_OK) goto fail;
     if ((rc = slos_alloc((void**)&p->mpar_d[k], width * total * 4, p->bytes)) != PCVL_OK) goto fail;
-    if (k == n && (rc = slos_alloc((void**)&p->mfact_d, total * sizeof(dd), p->bytes)) != PCVL_OK) goto fail;
+    if (k == n && (rc = slos_alloc((void**)&p->mfact_d, total * 8, p->bytes)) != PCVL_OK) goto fail;
     if (total > 0) {
       const int run_len = (int)std::max<uint64_t>(
           1, std::min<uint64_t>(kParentRun, total / ((uint64_t)num_sms() * 4096)));
       mask_parents<<<grid_for((total + run_len - 1) / run_len, 8), 256>>>(
           sp, k, (const uint64_t*)cur.p, total, (const uint64_t*)prev_d.p, nprev, p->mocc_d[k], p->mpar_d[k],
-          k == n ? p->mfact_d : nullptr, (int*)err_d.p, run_len);
+          k == n ? p->mfact_d : nullptr, precision == kPrecFP64, (int*)err_d.p, run_len);
       if (cudaGetLastError() != cudaSuccess) goto cuda_fail;
     }
     if (p->keep) {
@@ -644,9 +672,9 @@ int slos_masked_create(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, 
       vac = miss <= mask_n;
     }
     if (!vac) p->sizes[0] = 0;
-    if ((rc = slos_alloc((void**)&p->mfact_d, sizeof(dd), p->bytes)) != PCVL_OK) goto fail;
-    const dd one = dd_from_double(1.0);
-    if ((rc = slos_upload(p->mfact_d, &one, sizeof(dd))) != PCVL_OK) goto fail;
+    if ((rc = slos_alloc((void**)&p->mfact_d, 8, p->bytes)) != PCVL_OK) goto fail;
+    const std::vector<uint64_t> one = slos_factor_words({1.0}, precision);
+    if ((rc = slos_upload(p->mfact_d, one.data(), 8)) != PCVL_OK) goto fail;
   }
   if (cudaMemcpy(&err_h, err_d.p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) goto cuda_fail;
   if (err_h != 0) {
@@ -682,8 +710,8 @@ int slos_masked_create(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, 
     }
     if ((rc = slos_alloc((void**)&p->col_d, p->col.size() * 4, p->bytes)) != PCVL_OK) goto fail;
     if ((rc = slos_upload(p->col_d, p->col.data(), p->col.size() * 4)) != PCVL_OK) goto fail;
-    if ((rc = slos_alloc((void**)&p->inv_in_d, B * sizeof(dd), p->bytes)) != PCVL_OK) goto fail;
-    if ((rc = slos_upload(p->inv_in_d, inv_in.data(), B * sizeof(dd))) != PCVL_OK) goto fail;
+    if ((rc = slos_alloc((void**)&p->inv_in_d, B * 8, p->bytes)) != PCVL_OK) goto fail;
+    if ((rc = slos_upload(p->inv_in_d, inv_in.data(), B * 8)) != PCVL_OK) goto fail;
     if ((rc = slos_alloc((void**)&p->ucols_d, (size_t)std::max(n, 1) * m * B * sizeof(cdd), p->bytes)) != PCVL_OK)
       goto fail;
     if (p->keep) {
@@ -726,12 +754,22 @@ int slos_masked_forward(pcvl_slos_plan* p, cudaStream_t s) {
     const cdd* in = p->keep ? p->layers[k - 1] : p->layers[(k - 1) % 2];
     cdd* out = p->keep ? p->layers[k] : p->layers[k % 2];
     const cdd* ucol = p->ucols_d + (size_t)(k - 1) * m * B;
+    const bool f64 = p->prec == kPrecFP64;
     if (B == 1) {
-      slos_mfwd<false><<<grid_for(L, 8), 256, 0, s>>>(in, out, p->mocc_d[k], p->mpar_d[k], L, ucol, m, B);
+      if (f64)
+        slos_mfwd<false, Arith64><<<grid_for(L, 8), 256, 0, s>>>((const double2*)in, (double2*)out, p->mocc_d[k],
+                                                                 p->mpar_d[k], L, (const double2*)ucol, m, B);
+      else
+        slos_mfwd<false, ArithFF><<<grid_for(L, 8), 256, 0, s>>>(in, out, p->mocc_d[k], p->mpar_d[k], L, ucol, m,
+                                                                 B);
     } else {
       const dim3 grid((unsigned)std::max<uint64_t>(1, std::min<uint64_t>((L + 7) / 8, (uint64_t)num_sms() * 16)),
                       (unsigned)((B + 31) / 32));
-      slos_mfwd<true><<<grid, 256, 0, s>>>(in, out, p->mocc_d[k], p->mpar_d[k], L, ucol, m, B);
+      if (f64)
+        slos_mfwd<true, Arith64><<<grid, 256, 0, s>>>((const double2*)in, (double2*)out, p->mocc_d[k],
+                                                      p->mpar_d[k], L, (const double2*)ucol, m, B);
+      else
+        slos_mfwd<true, ArithFF><<<grid, 256, 0, s>>>(in, out, p->mocc_d[k], p->mpar_d[k], L, ucol, m, B);
     }
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -742,12 +780,17 @@ int slos_masked_forward(pcvl_slos_plan* p, cudaStream_t s) {
   return PCVL_OK;
 }
 
-int slos_masked_finalize(pcvl_slos_plan* p, int mode, const double* w, double* out_real, double2* out_c, cdd* seed,
-                         cudaStream_t s) {
+int slos_masked_finalize(pcvl_slos_plan* p, int mode, const double* w, double* out_real, double2* out_c,
+                         void* seed, cudaStream_t s) {
   const uint64_t L = p->sizes[p->n];
   if (L == 0) return PCVL_OK;
-  slos_mfin<<<grid_for(L * p->B, 8), 256, 0, s>>>(p->final_layer(), p->mfact_d, p->inv_in_d, L, p->B, mode, w,
-                                                  out_real, out_c, seed);
+  if (p->prec == kPrecFP64)
+    slos_mfin<Arith64><<<grid_for(L * p->B, 8), 256, 0, s>>>(
+        (const double2*)p->final_layer(), (const double*)p->mfact_d, (const double*)p->inv_in_d, L, p->B, mode, w,
+        out_real, out_c, (double2*)seed);
+  else
+    slos_mfin<ArithFF><<<grid_for(L * p->B, 8), 256, 0, s>>>(p->final_layer(), p->mfact_d, p->inv_in_d, L, p->B,
+                                                             mode, w, out_real, out_c, (cdd*)seed);
   PCVL_CUDA(cudaGetLastError());
   return PCVL_OK;
 }
@@ -766,21 +809,23 @@ int slos_masked_backward(pcvl_slos_plan* p, const double* weights_d, double* gra
     const cdd* ain = p->adj_d[k % 2];
     cdd* aout = p->adj_d[(k - 1) % 2];
     const cdd* ucol = p->ucols_d + (size_t)(k - 1) * m * B;
-    if (m <= 8)
-      launch_mbwd<8>(batched, grid, ain, aout, p->layers[k - 1], p->mchild_d[k], Lp, ucol, m, B, p->gpart_d, s);
-    else if (m <= 16)
-      launch_mbwd<16>(batched, grid, ain, aout, p->layers[k - 1], p->mchild_d[k], Lp, ucol, m, B, p->gpart_d, s);
-    else if (m <= 24)
-      launch_mbwd<24>(batched, grid, ain, aout, p->layers[k - 1], p->mchild_d[k], Lp, ucol, m, B, p->gpart_d, s);
+    if (p->prec == kPrecFP64)
+      launch_mbwd_m<Arith64>(batched, grid, ain, aout, p->layers[k - 1], p->mchild_d[k], Lp, ucol, m, B,
+                             p->gpart_d, s);
     else
-      launch_mbwd<32>(batched, grid, ain, aout, p->layers[k - 1], p->mchild_d[k], Lp, ucol, m, B, p->gpart_d, s);
+      launch_mbwd_m<ArithFF>(batched, grid, ain, aout, p->layers[k - 1], p->mchild_d[k], Lp, ucol, m, B,
+                             p->gpart_d, s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
       set_error("masked SLOS adjoint layer %d launch failed: %s", k, cudaGetErrorString(e));
       return PCVL_ERR_CUDA;
     }
-    slos_mgrad_reduce<<<(m * B + 255) / 256, 256, 0, s>>>(p->gpart_d, gx, m, B, p->col_d + (size_t)(k - 1) * B,
-                                                          (double2*)grad_u_d);
+    if (p->prec == kPrecFP64)
+      slos_mgrad_reduce<Arith64><<<(m * B + 255) / 256, 256, 0, s>>>(
+          (const double2*)p->gpart_d, gx, m, B, p->col_d + (size_t)(k - 1) * B, (double2*)grad_u_d);
+    else
+      slos_mgrad_reduce<ArithFF><<<(m * B + 255) / 256, 256, 0, s>>>(
+          p->gpart_d, gx, m, B, p->col_d + (size_t)(k - 1) * B, (double2*)grad_u_d);
     PCVL_CUDA(cudaGetLastError());
   }
   return PCVL_OK;
@@ -792,8 +837,10 @@ using namespace pcvl;
 
 extern "C" int pcvl_slos_plan_create_masked(pcvl_slos_plan** plan, int32_t m, const int32_t* input_states_h,
                                             int32_t batch, int32_t keep_layers, int32_t n_masks,
-                                            const int8_t* digits_h, uint32_t at_least_modes, int32_t mask_n) {
-  return slos_masked_create(plan, m, input_states_h, batch, keep_layers, n_masks, digits_h, at_least_modes, mask_n);
+                                            const int8_t* digits_h, uint32_t at_least_modes, int32_t mask_n,
+                                            int32_t precision) {
+  return slos_masked_create(plan, m, input_states_h, batch, keep_layers, n_masks, digits_h, at_least_modes, mask_n,
+                            precision);
 }
 
 extern "C" int pcvl_slos_output_ranks(const pcvl_slos_plan* plan, uint64_t* ranks_h) {

@@ -6,8 +6,12 @@
 
 #include "common.cuh"
 
+// Device arrays of complex values are typed cdd but hold the plan's arithmetic: float-float
+// pairs (cdd) or double2 (FP64), both 16 bytes; factor arrays (dd) hold dd or double, both
+// 8 bytes.  Kernels reinterpret them through the arithmetic policies of arith.cuh.
 struct pcvl_slos_plan {
   int m = 0, n = 0, B = 0;
+  int prec = pcvl::kPrecFP64;    // kPrecFP64 or kPrecFloatFloat
   bool keep = false;
   std::vector<int> inputs;        // B x m input states (same photon count)
   std::vector<int32_t> col;       // n x B: input mode of photon k of entry b -> col[(k-1) * B + b]
@@ -48,16 +52,18 @@ namespace pcvl {
 // shared host helpers (slos.cu)
 int slos_alloc(void** p, size_t bytes, int64_t& total);
 int slos_upload(void* dst, const void* src, size_t bytes);
+// factors of the plan's arithmetic as 8-byte words: dd (float-float) or double (FP64)
+std::vector<uint64_t> slos_factor_words(const std::vector<double>& x, int prec);
 std::vector<int> slos_path_order(const std::vector<int>& input);
 void slos_free_plan(pcvl_slos_plan* p);
 
 // masked plans (slos_masked.cu)
 int slos_masked_create(pcvl_slos_plan** plan, int32_t m, const int32_t* inputs, int32_t batch,
                        int32_t keep_layers, int32_t n_masks, const int8_t* digits, uint32_t at_least,
-                       int32_t mask_n);
+                       int32_t mask_n, int32_t precision);
 int slos_masked_forward(pcvl_slos_plan* p, cudaStream_t s);
 int slos_masked_finalize(pcvl_slos_plan* p, int mode, const double* w, double* out_real, double2* out_c,
-                         cdd* seed, cudaStream_t s);
+                         void* seed, cudaStream_t s);
 int slos_masked_backward(pcvl_slos_plan* p, const double* weights_d, double* grad_u_d, cudaStream_t s);
 void slos_masked_free(pcvl_slos_plan* p);
 

@@ -67,8 +67,11 @@ def test_argument_errors_are_reported_without_device_work(lib):
     assert rc == 1 and "overlap" in _native.last_error()
     h = ctypes.c_void_p()
     inp = np.array([1] * 40, dtype=np.int32)
-    rc = L.pcvl_slos_plan_create(ctypes.byref(h), 40, inp.ctypes.data, 1, 0)
+    rc = L.pcvl_slos_plan_create(ctypes.byref(h), 40, inp.ctypes.data, 1, 0, 2)
     assert rc == 1 and "outside" in _native.last_error()
+    inp = np.array([1] * 4, dtype=np.int32)
+    rc = L.pcvl_slos_plan_create(ctypes.byref(h), 4, inp.ctypes.data, 1, 0, 1)
+    assert rc == 1 and "precision" in _native.last_error()
 
 
 def test_masked_slap_and_mask_ranks_refuse_bad_arguments(lib):
@@ -82,13 +85,16 @@ def test_masked_slap_and_mask_ranks_refuse_bad_arguments(lib):
     h = ctypes.c_void_p()
     inp = np.array([1, 1, 0, 0], dtype=np.int32)
     digits = np.array([[-1, -1, 0, 0]], dtype=np.int8)
-    assert L.pcvl_slos_plan_create_masked(ctypes.byref(h), 4, inp.ctypes.data, 1, 0, 0, digits.ctypes.data, 0, 2) == 1
+    assert L.pcvl_slos_plan_create_masked(ctypes.byref(h), 4, inp.ctypes.data, 1, 0, 0, digits.ctypes.data, 0, 2,
+                                          2) == 1
     assert "n_masks" in _native.last_error()
     bad = np.array([[-1, -2, 0, 0]], dtype=np.int8)
-    assert L.pcvl_slos_plan_create_masked(ctypes.byref(h), 4, inp.ctypes.data, 1, 0, 1, bad.ctypes.data, 0, 2) == 1
+    assert L.pcvl_slos_plan_create_masked(ctypes.byref(h), 4, inp.ctypes.data, 1, 0, 1, bad.ctypes.data, 0, 2,
+                                          2) == 1
     assert "digit" in _native.last_error()
     two = np.array([1, 1, 0, 0, 1, 0, 0, 0], dtype=np.int32)
-    assert L.pcvl_slos_plan_create_masked(ctypes.byref(h), 4, two.ctypes.data, 2, 0, 1, digits.ctypes.data, 0, 2) == 1
+    assert L.pcvl_slos_plan_create_masked(ctypes.byref(h), 4, two.ctypes.data, 2, 0, 1, digits.ctypes.data, 0, 2,
+                                          2) == 1
     assert "photon count" in _native.last_error()
     kept = ctypes.c_int64()
     assert L.pcvl_fock_mask_ranks(0, 2, 1, digits.ctypes.data, None, 2, None, 0, ctypes.byref(kept)) == 1

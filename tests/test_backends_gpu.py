@@ -111,20 +111,23 @@ def test_slos_equals_naive_on_random_circuit(native):
     assert s.prob_amplitude(BasicState([1] * 7)) == 0
 
 
-def test_naive_batched_collision_free_outputs(native, oracle):
-    # the small-configuration second half: Naive amplitudes of collision-free outputs
+@pytest.mark.parametrize("prec", ["fp64", "float-float"])
+def test_naive_batched_collision_free_outputs(native, oracle, prec):
+    # the small configuration's second half: Naive amplitudes of its 1000 random
+    # collision-free outputs (6 of 12 modes, default_rng(0)), every one against the oracle
     U = random_unitary(12, seed=0)
     inp = BasicState([1] * 6 + [0] * 6)
     rng = np.random.default_rng(0)
     outs = []
-    for _ in range(50):
+    for _ in range(1000):
         o = np.zeros(12, dtype=int)
         o[rng.choice(12, 6, replace=False)] = 1
         outs.append(BasicState(o))
-    b = BackendFactory.get_backend("Naive")
+    b = BackendFactory.get_backend("Naive", precision=prec)
     b.set_circuit(U)
     b.set_input_state(inp)
     got = b.prob_amplitudes(outs)
+    assert len(got) == 1000
     _, ref = oracle.slos(U, list(inp))
     from perceval_gb300.utils import fock_rank
     want = np.array([ref[fock_rank(o)] for o in outs])

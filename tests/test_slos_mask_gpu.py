@@ -37,13 +37,14 @@ def close(a, b):
     return a.shape == b.shape and (a.size == 0 or np.abs(a - b).max() <= RTOL * scale)
 
 
+@pytest.mark.parametrize("prec", ["fp64", "float-float"])
 @pytest.mark.parametrize("case", CASES, ids=[str(i) for i in range(len(CASES))])
-def test_masked_plan_against_oracle(native, oracle, case):
+def test_masked_plan_against_oracle(native, oracle, case, prec):
     m, inp, masks, at_least, mask_n = case
     n = sum(inp)
     mask = FSMask(m, mask_n or n, masks, at_least)
     U = random_unitary(m, seed=m + n)
-    plan = native.SlosPlan(m, inp, mask=mask)
+    plan = native.SlosPlan(m, inp, mask=mask, precision=prec)
     sel = kept_ranks(m, n, mask)
     assert plan.count == len(sel)
     assert np.array_equal(plan.output_ranks().astype(np.int64), sel)
