@@ -403,7 +403,7 @@ def run_ours(args):
             "max_rel_diff_vs_fp64": float(((ff_out - ref64).abs() / ref64.abs()).max()),
             "step_tflops_fp64_equiv": flops_total / (ff_ms * 1e-3) / 1e12}
         del ff_plan
-        sec.update(secondary(torch, _native, random_unitary, dev, flush))
+        sec.update(secondary(torch, _native, random_unitary, dev, flush, fp64_peak))
         line["secondary"] = sec
     if rank == 0 and ws == 1 and not args.skip_cpu:
         line["cpu_baseline"] = cpu_perm_baseline()
@@ -415,7 +415,7 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def secondary(torch, _native, random_unitary, dev, flush):
+def secondary(torch, _native, random_unitary, dev, flush, fp64_peak_tflops):
     res = {}
 
     def timed(fn, reps=3):
@@ -437,30 +437,41 @@ def secondary(torch, _native, random_unitary, dev, flush):
         hbm = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]
     except (OSError, ValueError, KeyError):
         hbm = 6800.0
-    # SLOS m=24, n=12
+    # SLOS m=24, n=12 in both arithmetics
     m, n = 24, 12
-    plan = _native.SlosPlan(m, [1] * n + [0] * (m - n))
     Ud = torch.from_numpy(random_unitary(m, seed=0)).to(dev)
-    t_fwd = timed(lambda: plan.forward(Ud), reps=2)
-    probs = plan.probabilities()
-    t_prob = timed(lambda: plan.probabilities(probs), reps=2)
-    # every probability without storing the last layer (its probabilities written directly)
-    t_fused = timed(lambda: plan.forward_probabilities(Ud, probs), reps=2)
     Ls = [math.comb(m + k - 1, k) for k in range(n + 1)]
     alg_bytes = 16 * sum(Ls[k - 1] + Ls[k] for k in range(1, n + 1))
-    # the arithmetic floor: layer k has m L_{k-1} (state, occupied mode) terms (the states with
-    # mode 0 occupied number L_{k-1}); a float-float complex multiply-add is 48 FP32 operations,
-    # at the 36.8 T FP32 operations/s measured on this part
+    # the arithmetic floors: layer k has m L_{k-1} (state, occupied mode) terms (the states with
+    # mode 0 occupied number L_{k-1}); an FP64 complex multiply-add is 4 DFMA (8 flops), at the
+    # FP64 rate measured in this run; a float-float one is 48 FP32 operations, at the 36.8 T
+    # FP32 operations/s measured on this part
     terms = m * sum(Ls[k - 1] for k in range(1, n + 1))
+    fp64_floor_ms = terms * 8 / (fp64_peak_tflops * 1e12) * 1e3
     fp32_floor_ms = terms * 48 / 36.8e12 * 1e3
-    res["slos_m24_n12"] = {"amps_per_s": Ls[n] / (t_fwd * 1e-3), "forward_ms": t_fwd, "probabilities_ms": t_prob,
-                           "forward_probabilities_ms": t_fused, "multiply_add_terms": terms,
-                           "fp32_floor_ms": fp32_floor_ms, "fp32_frac": fp32_floor_ms / t_fwd,
-                           "algorithmic_gb": alg_bytes / 1e9,
-                           "hbm_frac": alg_bytes / (t_fwd * 1e-3) / 1e9 / hbm, "hbm_peak_gbs": hbm,
-                           "sum_p": float(probs.sum())}
-    del plan, probs
-    torch.cuda.empty_cache()
+    p64 = None
+    for prec, key in (("fp64", "slos_m24_n12"), ("float-float", "slos_m24_n12_float_float")):
+        plan = _native.SlosPlan(m, [1] * n + [0] * (m - n), precision=prec)
+        t_fwd = timed(lambda: plan.forward(Ud), reps=2)
+        probs = plan.probabilities()
+        t_prob = timed(lambda: plan.probabilities(probs), reps=2)
+        # every probability without storing the last layer (its probabilities written directly)
+        t_fused = timed(lambda: plan.forward_probabilities(Ud, probs), reps=2)
+        row = {"arithmetic": prec, "amps_per_s": Ls[n] / (t_fwd * 1e-3), "forward_ms": t_fwd,
+               "probabilities_ms": t_prob, "forward_probabilities_ms": t_fused, "multiply_add_terms": terms,
+               "algorithmic_gb": alg_bytes / 1e9, "hbm_frac": alg_bytes / (t_fwd * 1e-3) / 1e9 / hbm,
+               "hbm_peak_gbs": hbm, "sum_p": float(probs.sum())}
+        if prec == "fp64":
+            row.update({"fp64_floor_ms": fp64_floor_ms, "fp64_frac": fp64_floor_ms / t_fwd,
+                        "fp64_peak_tflops": fp64_peak_tflops})
+            p64 = probs[::997].clone()
+        else:
+            row.update({"fp32_floor_ms": fp32_floor_ms, "fp32_frac": fp32_floor_ms / t_fwd,
+                        "max_abs_diff_vs_fp64_sampled": float((probs[::997] - p64).abs().max())})
+        res[key] = row
+        del plan, probs
+        torch.cuda.empty_cache()
+    t_fwd = res["slos_m24_n12"]["forward_ms"]
     # the same circuit heralded: modes 20..23 detected as 1, 1, 0, 0 (a masked plan keeps only
     # the states that can still end with that pattern)
     from perceval_gb300.utils import FSMask
@@ -517,15 +528,20 @@ def secondary(torch, _native, random_unitary, dev, flush):
     from perceval_gb300.components.mesh import clements_mesh_unitary
     ph = torch.from_numpy(np.random.default_rng(0).uniform(0, 2 * math.pi, (256, 240)))
     Um = clements_mesh_unitary(ph, 16).contiguous().to(dev)
-    plan = _native.SlosPlan(16, [1] * 8 + [0] * 8, batch=256, keep_layers=True)
-    w = torch.from_numpy(np.random.default_rng(1).normal(size=plan.count * 256)).to(dev)
-    t_f = timed(lambda: plan.forward(Um), reps=2)
-    t_b = timed(lambda: plan.backward(w), reps=2)
     Ls = [math.comb(16 + k - 1, k) for k in range(9)]
     fb = 16 * 256 * sum(Ls[k - 1] + Ls[k] for k in range(1, 9))
-    res["slos_grad_m16_n8_b256"] = {"forward_ms": t_f, "backward_ms": t_b, "circuits_per_s": 256 / ((t_f + t_b) * 1e-3),
-                                    "forward_hbm_frac": fb / (t_f * 1e-3) / 1e9 / hbm}
-    del plan
+    fterms = 256 * 16 * sum(Ls[k - 1] for k in range(1, 9))  # forward complex multiply-adds
+    for prec, key in (("fp64", "slos_grad_m16_n8_b256"), ("float-float", "slos_grad_m16_n8_b256_float_float")):
+        plan = _native.SlosPlan(16, [1] * 8 + [0] * 8, batch=256, keep_layers=True, precision=prec)
+        w = torch.from_numpy(np.random.default_rng(1).normal(size=plan.count * 256)).to(dev)
+        t_f = timed(lambda: plan.forward(Um), reps=2)
+        t_b = timed(lambda: plan.backward(w), reps=2)
+        row = {"arithmetic": prec, "forward_ms": t_f, "backward_ms": t_b,
+               "circuits_per_s": 256 / ((t_f + t_b) * 1e-3), "forward_hbm_frac": fb / (t_f * 1e-3) / 1e9 / hbm}
+        if prec == "fp64":
+            row["forward_fp64_frac"] = fterms * 8 / (t_f * 1e-3) / (fp64_peak_tflops * 1e12)
+        res[key] = row
+        del plan
     torch.cuda.empty_cache()
     # single large permanents spread over the whole chip (Haar submatrices of a 1024x1024
     # unitary), Glynn and Ryser, with their relative difference
@@ -851,16 +867,17 @@ def profile_case(name: str):
     _native.load()
     autotune.load()  # the launch shapes the headline run tuned and cached, if any
     dev = torch.device("cuda")
-    if name == "perm24":
-        # 64 matrices of the n = 24 bin (one perm_bin_kernel<24> launch)
+    if name in ("perm24", "perm24ff"):
+        # 64 matrices of the n = 24 bin (one perm_bin_f64<24> or perm_bin_kernel<24> launch)
         mats, flat, offs, sizes = make_batch(seed=0)
         sel = [i for i in range(N_MATS) if sizes[i] == 24][:64]
         sub = torch.from_numpy(np.concatenate([mats[i].reshape(-1) for i in sel])).to(dev)
         out = torch.empty(len(sel), dtype=torch.complex128, device=dev)
-        _native.permanent_batch(sub, np.arange(len(sel), dtype=np.int64) * 576, np.full(len(sel), 24, np.int32), out)
-    elif name == "slos20":
+        _native.permanent_batch(sub, np.arange(len(sel), dtype=np.int64) * 576, np.full(len(sel), 24, np.int32), out,
+                                precision="fp64" if name == "perm24" else "float-float")
+    elif name in ("slos20", "slos20ff"):
         # SLOS m = 20, n = 10: last layer 20,030,010 states (320 MB, above L2)
-        plan = _native.SlosPlan(20, [1] * 10 + [0] * 10)
+        plan = _native.SlosPlan(20, [1] * 10 + [0] * 10, precision="fp64" if name == "slos20" else "float-float")
         plan.forward(torch.from_numpy(random_unitary(20, seed=0)).to(dev))
         plan.probabilities()
     elif name == "slos20p":
@@ -919,7 +936,7 @@ def main():
                     help="run the learned-proposal sampler workload (n=30, m=900 and n=8, m=64) and exit")
     ap.add_argument("--learned-train", type=int, default=2048, help="exact training samples at n=30")
     ap.add_argument("--large-perm", action="store_true", help="one n = 40 permanent (about a minute)")
-    ap.add_argument("--profile-case", choices=["perm24", "slos20", "slos20p", "slosmask22", "slap1024", "slos16b256",
+    ap.add_argument("--profile-case", choices=["perm24", "perm24ff", "slos20", "slos20ff", "slos20p", "slosmask22", "slap1024", "slos16b256",
                                                "cc2017", "gurvits20", "gemm"],
                     help="run one small untimed case of a single kernel (for ncu) and exit")
     args = ap.parse_args()

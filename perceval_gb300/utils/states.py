@@ -6,9 +6,15 @@ The reference aliases these to closed native types (perceval/utils/states.py:42-
 same observable behaviour that the backend API relies on:
 
 * ``FockState`` is an immutable, hashable occupation vector with ``m``, ``n``,
-  ``prodnfact()``, indexing, iteration and the ``|a,b,c>`` text form.
+  ``prodnfact()``, indexing (a slice is a ``FockState``), iteration, the ``|a,b,c>``
+  text form, ``merge`` (mode-wise sum of two states' photons, what the simulators'
+  recombination of distinguishable parts calls, perceval/simulators/
+  _simulator_utils.py:77,164) and ``set_slice`` (perceval/simulators/stepper.py:94).
 * ``StateVector`` maps ``FockState`` to complex amplitudes, supports ``+``, ``-``
-  and scalar ``*`` and ``normalize()``.
+  and scalar ``*`` and ``normalize()``; iterating it yields (state, amplitude) pairs,
+  as the reference's does (perceval/simulators/stepper.py:92,
+  _simulator_utils.py:132), and so does ``unnormalized_iterator()``; ``keys()`` gives
+  the states.
 * ``BSDistribution`` maps ``FockState`` to probabilities (``add`` accumulates).
 * ``BSSamples`` is a list of ``FockState``; ``BSCount`` counts them.
 
@@ -103,6 +109,25 @@ class FockState(tuple):
             return FockState(res)
         return res
 
+    def merge(self, other: "FockState") -> "FockState":
+        """The state holding both states' photons: counts added mode by mode (the two
+        states have the same number of modes)."""
+        other = FockState(other)
+        if len(other) != len(self):
+            raise ValueError(f"cannot merge states of {len(self)} and {len(other)} modes")
+        return FockState._trusted(tuple(a + b for a, b in zip(self, other)))
+
+    def set_slice(self, sl: slice, state: "FockState") -> "FockState":
+        """A copy whose modes ``sl`` are replaced by the occupations of ``state``."""
+        vals = list(self)
+        idx = range(*sl.indices(len(vals)))
+        state = FockState(state)
+        if len(idx) != len(state):
+            raise ValueError("the replacement state does not have the slice's number of modes")
+        for i, v in zip(idx, state):
+            vals[i] = v
+        return FockState._trusted(tuple(vals))
+
 
 BasicState = FockState
 
@@ -133,7 +158,15 @@ class StateVector(dict):
 
     @property
     def m(self) -> int:
-        return next(iter(self)).m if self else 0
+        return next(iter(self.keys())).m if self else 0
+
+    def __iter__(self):
+        """(state, amplitude) pairs, as the reference's StateVector iterates."""
+        return iter(self.items())
+
+    def unnormalized_iterator(self):
+        """(state, amplitude) pairs without normalisation."""
+        return iter(self.items())
 
     def __add__(self, other):
         res = StateVector(dict(self))
@@ -164,7 +197,7 @@ class StateVector(dict):
             del self[k]
         norm = math.sqrt(sum(abs(v) ** 2 for v in self.values()))
         if norm > 0:
-            for k in self:
+            for k in list(self.keys()):
                 self[k] /= norm
         return self
 
@@ -177,6 +210,11 @@ class BSDistribution(dict):
     distribution has exactly its two non-zero outputs,
     tests/backends/test_backends.py:203-218).
     """
+
+    def __missing__(self, key):
+        # a state absent from the distribution has probability 0, so ``d[s] += p``
+        # accumulates (perceval/simulators/simulator.py:497)
+        return 0.0
 
     def add(self, state: FockState, p: float):
         p = float(p)
@@ -330,7 +368,7 @@ def allstate_iterator(input_state, mask=None) -> Iterator[FockState]:
     """
     m = input_state.m
     if isinstance(input_state, StateVector):
-        ns = sorted({s.n for s in input_state})
+        ns = sorted({s.n for s in input_state.keys()})
     else:
         ns = [input_state.n]
     for n in ns:

@@ -81,7 +81,7 @@ def test_kat_amplitudes_and_evolve(native, kats, name):
         b.set_input_state(BasicState(case["input"]))
         sv = b.evolve()
         sv.normalize()
-        assert {str(k) for k in sv} == set(case["expected"])
+        assert {str(k) for k in sv.keys()} == set(case["expected"])
         for s, v in case["expected"].items():
             assert sv[BasicState(s)] == pytest.approx(complex(*v))
 

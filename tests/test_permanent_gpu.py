@@ -164,8 +164,10 @@ def test_all_ones_and_equal_rows(native, n, method, prec):
     (all ones: the all-ones matrix J_n): perm = n! prod(r) (3 + 4i)^n exactly.  Their
     term magnitudes span the widest exponent range the row scaling must keep inside
     FP32 (float-float) and FP64.  The check is the rounding bound of the sum:
-    |gpu - perm| <= max(1e-10, 4 n u cond) |perm|, with cond = sum |terms| / |sum|
-    computed exactly (u: the arithmetic's unit roundoff)."""
+    |gpu - perm| <= max(1e-10, 16 n u cond) |perm|, with cond = sum |terms| / |sum|
+    computed exactly (u: the arithmetic's unit roundoff; a term is a product of n row
+    sums, each rounded, and float-float's lazy pairs lose about one more bit per
+    operation than u).  At n = 40 in float-float the bound is 7e-6 relative."""
     rng = np.random.default_rng(1000 + n)
     for r in (np.ones(n, dtype=np.int64), rng.integers(1, 4, n)):
         a = np.tile(r.astype(float), (n, 1)) * (3 + 4j)
@@ -177,7 +179,7 @@ def test_all_ones_and_equal_rows(native, n, method, prec):
         terms = _abs_term_sum([int(v) for v in r], method == 1)
         denom = exact_int * (2 ** (n - 1) if method == 0 else 1)
         cond = terms / denom
-        tol = max(RTOL, 4 * n * UNIT[prec] * cond)
+        tol = max(RTOL, 16 * n * UNIT[prec] * cond)
         got = gpu_perms(native, [np.ascontiguousarray(a)], method, prec)[0]
         assert np.isfinite(got.real) and np.isfinite(got.imag)
         assert abs(got - ref) <= tol * abs(ref), (abs(got - ref) / abs(ref), tol, cond)
