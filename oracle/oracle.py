@@ -48,6 +48,8 @@ def lib():
         L.oracle_perm_glynn.argtypes = [i32, vp, vp]
         L.oracle_perm_ryser.argtypes = [i32, vp, vp]
         L.oracle_perm_batch.argtypes = [vp, vp, vp, i32, i32, vp]
+        L.oracle_perm_batch_fast.argtypes = [vp, vp, vp, i32, vp]
+        L.oracle_cc2017_fast.argtypes = [vp, i32, vp, i64, u64, u64, vp]
         L.oracle_slos_order.restype = i32
         L.oracle_slos_order.argtypes = [i32, vp, vp]
         L.oracle_slos_coefs.restype = i32
@@ -98,6 +100,31 @@ def perm_batch(mats: np.ndarray, offsets, sizes, method: str = "glynn") -> np.nd
     out = np.zeros(len(sizes), dtype=np.complex128)
     lib().oracle_perm_batch(mats.ctypes.data, offsets.ctypes.data, sizes.ctypes.data, len(sizes),
                             1 if method == "ryser" else 0, out.ctypes.data)
+    return out
+
+
+def perm_batch_fast(mats: np.ndarray, offsets, sizes) -> np.ndarray:
+    """Glynn permanents of a packed batch by the host-tuned path (the CPU baseline):
+    vectorisable row-sum updates, four product chains, one OpenMP task per 2^12-step
+    chunk of every matrix, chunks added in order with compensation (FP64)."""
+    mats = _c128(mats)
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    sizes = _i32(sizes)
+    out = np.zeros(len(sizes), dtype=np.complex128)
+    lib().oracle_perm_batch_fast(mats.ctypes.data, offsets.ctypes.data, sizes.ctypes.data, len(sizes),
+                                 out.ctypes.data)
+    return out
+
+
+def cc2017_fast(U, input_state, count: int, seed: int, first: int = 0) -> np.ndarray:
+    """Clifford & Clifford samples drawn in parallel over samples, the k sub-permanents of
+    a step from one Glynn sum (the CPU baseline; same Philox stream and draws as cc2017)."""
+    U = _c128(U)
+    m = U.shape[0]
+    inp = _i32(input_state)
+    out = np.zeros((count, m), dtype=np.int32)
+    lib().oracle_cc2017_fast(U.ctypes.data, m, inp.ctypes.data, int(count), int(seed) & (2**64 - 1), int(first),
+                             out.ctypes.data)
     return out
 
 

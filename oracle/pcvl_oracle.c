@@ -537,3 +537,243 @@ void oracle_set_threads(int t) {
   (void)t;
 #endif
 }
+
+/* ---------------------------------------------------------------- CPU baseline paths
+ * The same formulas, arranged to run fast on the host (this is what the benchmark's CPU
+ * baseline times; the functions above stay the plain restatement the tests pin).
+ *
+ * Batched Glynn: the sign vectors of every matrix are cut into chunks of 2^12 consecutive
+ * Gray-code steps; one OpenMP task per (matrix, chunk), so small matrices use every core
+ * too.  Within a chunk the row sums live as separate real and imaginary arrays, so the
+ * update of a step (one column, +-2 a_ij for every row) is one vectorisable loop, and
+ * the product of the n row sums runs as four independent chains.  A chunk's terms are
+ * summed plainly; the chunks of a matrix are added in order with Neumaier compensation,
+ * so results do not depend on the thread count.  FP64 throughout. */
+/* Multiply-adds may fuse (FMA) here: this is the timed baseline, not the pinned restatement. */
+__attribute__((optimize("fp-contract=fast")))
+static void glynn_chunk(int n, const double* ar, const double* ai, uint64_t g0, uint64_t g1, double* rr, double* ri,
+                        double* out) {
+  /* ar, ai: column-major 2 a (ar[j * n + i] = 2 Re a_ij); row sums at Gray code g0 */
+  uint64_t gc = g0 ^ (g0 >> 1);
+  for (int i = 0; i < n; ++i) {
+    double vr = 0.5 * ar[i], vi = 0.5 * ai[i];
+    for (int j = 1; j < n; ++j) {
+      const double s = ((gc >> (j - 1)) & 1) ? -0.5 : 0.5;
+      vr += s * ar[j * n + i];
+      vi += s * ai[j * n + i];
+    }
+    rr[i] = vr;
+    ri[i] = vi;
+  }
+  int sign = __builtin_popcountll(gc) & 1;
+  double sr = 0, si = 0;
+  for (uint64_t k = g0; k < g1; ++k) {
+    if (k > g0) {
+      const int t = __builtin_ctzll(k);
+      gc ^= 1ull << t;
+      const double c = ((gc >> t) & 1) ? -1.0 : 1.0;
+      const double* xr = ar + (size_t)(t + 1) * n;
+      const double* xi = ai + (size_t)(t + 1) * n;
+      for (int i = 0; i < n; ++i) {
+        rr[i] += c * xr[i];
+        ri[i] += c * xi[i];
+      }
+      sign ^= 1;
+    }
+    double pr[4] = {1, 1, 1, 1}, pi[4] = {0, 0, 0, 0};
+    int i = 0;
+    for (; i + 4 <= n; i += 4)
+      for (int q = 0; q < 4; ++q) {
+        const double x = pr[q], y = pi[q], u = rr[i + q], v = ri[i + q];
+        pr[q] = x * u - y * v;
+        pi[q] = x * v + y * u;
+      }
+    for (; i < n; ++i) {
+      const double x = pr[0], y = pi[0], u = rr[i], v = ri[i];
+      pr[0] = x * u - y * v;
+      pi[0] = x * v + y * u;
+    }
+    const double ar01 = pr[0] * pr[1] - pi[0] * pi[1], ai01 = pr[0] * pi[1] + pi[0] * pr[1];
+    const double ar23 = pr[2] * pr[3] - pi[2] * pi[3], ai23 = pr[2] * pi[3] + pi[2] * pr[3];
+    const double p_r = ar01 * ar23 - ai01 * ai23, p_i = ar01 * ai23 + ai01 * ar23;
+    if (sign) {
+      sr -= p_r;
+      si -= p_i;
+    } else {
+      sr += p_r;
+      si += p_i;
+    }
+  }
+  out[0] = sr;
+  out[1] = si;
+}
+
+void oracle_perm_batch_fast(const double* mats, const int64_t* offs, const int32_t* sizes, int count, double* out) {
+  const uint64_t chunk = 1ull << 12;
+  int64_t* first = (int64_t*)malloc(sizeof(int64_t) * (count + 1));
+  first[0] = 0;
+  for (int i = 0; i < count; ++i) {
+    const int n = sizes[i];
+    const uint64_t total = n > 0 ? 1ull << (n - 1) : 0;
+    first[i + 1] = first[i] + (int64_t)((total + chunk - 1) / chunk);
+  }
+  const int64_t ntasks = first[count];
+  double* part = (double*)malloc(sizeof(double) * 2 * (ntasks > 0 ? ntasks : 1));
+#pragma omp parallel
+  {
+    double* buf = (double*)malloc(sizeof(double) * (4 * 40 + 4 * 40 * 40));
+    int cur = -1;
+    double *ar = buf + 160, *ai = ar + 1600, *rr = buf, *ri = buf + 40;
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t q = 0; q < ntasks; ++q) {
+      int lo = 0, hi = count;  /* matrix of task q: first[mat] <= q < first[mat + 1] */
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) / 2;
+        if (first[mid] <= q) lo = mid; else hi = mid;
+      }
+      while (first[lo + 1] <= q) ++lo;
+      const int mat = lo, n = sizes[mat];
+      if (mat != cur) {
+        const double* a = mats + 2 * offs[mat];
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < n; ++j) {
+            ar[j * n + i] = 2.0 * a[2 * (i * n + j)];
+            ai[j * n + i] = 2.0 * a[2 * (i * n + j) + 1];
+          }
+        cur = mat;
+      }
+      const uint64_t total = 1ull << (n - 1);
+      const uint64_t g0 = (uint64_t)(q - first[mat]) * chunk;
+      const uint64_t g1 = g0 + chunk < total ? g0 + chunk : total;
+      glynn_chunk(n, ar, ai, g0, g1, rr, ri, part + 2 * q);
+    }
+    free(buf);
+  }
+  for (int i = 0; i < count; ++i) {
+    const int n = sizes[i];
+    if (n == 0) {
+      out[2 * i] = 1;
+      out[2 * i + 1] = 0;
+      continue;
+    }
+    double sr = 0, cr = 0, si = 0, ci = 0;
+    for (int64_t q = first[i]; q < first[i + 1]; ++q) {
+      neumaier(&sr, &cr, part[2 * q]);
+      neumaier(&si, &ci, part[2 * q + 1]);
+    }
+    out[2 * i] = ldexp(sr + cr, -(n - 1));
+    out[2 * i + 1] = ldexp(si + ci, -(n - 1));
+  }
+  free(part);
+  free(first);
+}
+
+/* Clifford & Clifford algorithm B, samples in parallel (the same Philox stream and draw
+ * procedure as oracle_cc2017), with the k sub-permanents of a step from one Glynn sum over
+ * the signs of the k - 1 chosen rows: for each sign vector d the k column sums
+ * c_j = sum_i d_i U[row_i, col_j], and the sub-permanent without column l is
+ * 2^(2-k) sum_d (prod d) prod_{j != l} c_j, the leave-one-out products taken from prefix
+ * and suffix products.  O(k 2^(k-2)) per step instead of O(k^2 2^(k-2)). */
+static void sub_perms_all(int k, const cplx* U, int m, const int* rows, const int* cols, cplx* sub) {
+  if (k == 1) {
+    sub[0] = 1;
+    return;
+  }
+  const int d = k - 1;  /* rows; sign of row 0 fixed to +1 */
+  cplx c[64], pre[65], suf[65];
+  double accr[64], acci[64];
+  for (int l = 0; l < k; ++l) accr[l] = acci[l] = 0;
+  const uint64_t total = 1ull << (d - 1);
+  uint64_t gc = 0;
+  for (int j = 0; j < k; ++j) {
+    cplx v = 0;
+    for (int i = 0; i < d; ++i) v += U[rows[i] * m + cols[j]];
+    c[j] = v;
+  }
+  int sign = 0;
+  for (uint64_t t = 0; t < total; ++t) {
+    if (t > 0) {
+      const int b = __builtin_ctzll(t);
+      gc ^= 1ull << b;
+      const int neg = (gc >> b) & 1;  /* row b + 1 flips */
+      for (int j = 0; j < k; ++j) {
+        const cplx x = 2.0 * U[rows[b + 1] * m + cols[j]];
+        c[j] += neg ? -x : x;
+      }
+      sign ^= 1;
+    }
+    pre[0] = 1;
+    for (int j = 0; j < k; ++j) pre[j + 1] = pre[j] * c[j];
+    suf[k] = 1;
+    for (int j = k - 1; j >= 0; --j) suf[j] = suf[j + 1] * c[j];
+    for (int l = 0; l < k; ++l) {
+      const cplx p = pre[l] * suf[l + 1];
+      if (sign) {
+        accr[l] -= creal(p);
+        acci[l] -= cimag(p);
+      } else {
+        accr[l] += creal(p);
+        acci[l] += cimag(p);
+      }
+    }
+  }
+  for (int l = 0; l < k; ++l) sub[l] = ldexp(accr[l], -(d - 1)) + I * ldexp(acci[l], -(d - 1));
+}
+
+void oracle_cc2017_fast(const double* U_, int m, const int* in, int64_t count, uint64_t seed, uint64_t first,
+                        int32_t* out) {
+  const cplx* U = (const cplx*)U_;
+  int n = 0;
+  for (int i = 0; i < m; ++i) n += in[i];
+  int cols0[64];
+  for (int i = 0, q = 0; i < m; ++i)
+    for (int v = 0; v < in[i]; ++v) cols0[q++] = i;
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+#pragma omp parallel
+  {
+    double* w = (double*)malloc(sizeof(double) * m);
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t s = 0; s < count; ++s) {
+      const uint64_t sid = first + (uint64_t)s;
+      const uint32_t slo = (uint32_t)sid, shi = (uint32_t)(sid >> 32);
+      int cols[64], rows[64];
+      cplx sub[64];
+      for (int l = 0; l < n; ++l) cols[l] = cols0[l];
+      for (int q = n - 1; q >= 1; --q) {
+        const u4 r = philox((u4){slo, shi, 0xffffffffu, (uint32_t)q}, k0, k1);
+        const int j = (int)(((uint64_t)r.x * (uint64_t)(q + 1)) >> 32);
+        const int t = cols[q];
+        cols[q] = cols[j];
+        cols[j] = t;
+      }
+      for (int k = 1; k <= n; ++k) {
+        sub_perms_all(k, U, m, rows, cols, sub);
+        double W = 0;
+        for (int i = 0; i < m; ++i) {
+          cplx z = 0;
+          for (int l = 0; l < k; ++l) z += U[i * m + cols[l]] * sub[l];
+          w[i] = creal(z) * creal(z) + cimag(z) * cimag(z);
+          W += w[i];
+        }
+        const u4 r = philox((u4){slo, shi, (uint32_t)k, 0u}, k0, k1);
+        const uint64_t v = ((uint64_t)(r.x >> 5) << 26) | (uint64_t)(r.y >> 6);
+        const double target = (double)v * (1.0 / 9007199254740992.0) * W;
+        double run = 0;
+        int pick = -1, last_pos = 0;
+        for (int i = 0; i < m; ++i) {
+          if (w[i] > 0) last_pos = i;
+          run += w[i];
+          if (run > target) {
+            pick = i;
+            break;
+          }
+        }
+        rows[k - 1] = pick >= 0 ? pick : last_pos;
+      }
+      int32_t* o = out + s * m;
+      for (int i = 0; i < m; ++i) o[i] = 0;
+      for (int k = 0; k < n; ++k) o[rows[k]]++;
+    }
+    free(w);
+  }
+}
