@@ -351,13 +351,16 @@ def run_ours(args):
     fp64_peak = measured_fp64_peak(torch)
     achieved = len(sel) * glynn_flops(24) / (k_ms * 1e-3) / 1e12
     roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": achieved / fp64_peak, "traffic": traffic_from_profile("perm_bin_f64_n24"),
-                "kernel": "perm_bin_f64<24> (the n=24 bin of the batch)",
+                "frac": achieved / fp64_peak, "traffic": traffic_from_profile("perm_bin_fx_n24"),
+                "kernel": "perm_bin_fx<24> (the n=24 bin of the batch)",
                 "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 on this GPU (the measured peaks file "
                                "has no FP64 entry)",
                 "algorithmic_flops_per_permanent": "2^(n-1) (8n - 4)",
-                "note": "native FP64 arithmetic; the kernel issues 6n - 4 FP64 instructions per sign vector "
-                        "for 8n - 4 algorithmic flops, so frac <= (8n-4)/(2(6n-4)) = 0.67 at n = 24",
+                "note": "FP64 arithmetic with exact fixed-point row sums on the integer pipe (one rounding "
+                        "to FP64 each); per sign vector the FP64 pipe issues 4n - 4 instructions (products "
+                        "and the accumulation) for 8n - 4 algorithmic flops, so frac can reach "
+                        "(8n-4)/(2(4n-4)) = 1.02 at n = 24; with FP64 row sums (secondary "
+                        "perm_batch_fp64_dadd) 6n - 4 instructions, frac <= 0.67",
                 "step_tflops": flops_total / (ms / args.steps * 1e-3) / 1e12}
 
     line = {"metric": METRIC, "value": value, "unit": "perms/s", "n_gpus": ws, "steps": args.steps,
@@ -386,30 +389,31 @@ def run_ours(args):
             kb.append(s.elapsed_time(e))
         sec["perm_batch_call_8192"] = {"ms": statistics.median(kb), "arithmetic": "fp64",
                                        "perms_per_s": N_MATS / (statistics.median(kb) * 1e-3)}
-        # the same batch in float-float (opt-in): a plan of its own, its own tuned shapes
-        autotune.ensure_tuned(range(8, 25), log=lambda s: print(s, file=sys.stderr), precision="float-float")
+        # the same batch in float-float (opt-in) and in FP64 with FP64 row sums: plans of
+        # their own, their own tuned shapes
         ref64 = out_d.clone()
-        ff_plan = _native.PermPlan(offs, sizes, precision="float-float")
-        ff_out = torch.empty_like(out_d)
-        for _ in range(args.warmup):
-            ff_plan(flat_d, ff_out)
-        torch.cuda.synchronize()
-        kf = []
-        for _ in range(args.steps):
-            flush.zero_()
-            s, e = torch.cuda.Event(True), torch.cuda.Event(True)
-            s.record()
-            ff_plan(flat_d, ff_out)
-            e.record()
-            e.synchronize()
-            kf.append(s.elapsed_time(e))
-        ff_ms = statistics.mean(kf)
-        sec["perm_batch_float_float"] = {
-            "ms_per_step": ff_ms, "perms_per_s": N_MATS / (ff_ms * 1e-3),
-            "speedup_vs_fp64": (ms / args.steps) / ff_ms,
-            "max_rel_diff_vs_fp64": float(((ff_out - ref64).abs() / ref64.abs()).max()),
-            "step_tflops_fp64_equiv": flops_total / (ff_ms * 1e-3) / 1e12}
-        del ff_plan
+        for prec, key in (("float-float", "perm_batch_float_float"), ("fp64-dadd", "perm_batch_fp64_dadd")):
+            autotune.ensure_tuned(range(8, 25), log=lambda s: print(s, file=sys.stderr), precision=prec)
+            o_plan = _native.PermPlan(offs, sizes, precision=prec)
+            o_out = torch.empty_like(out_d)
+            for _ in range(args.warmup):
+                o_plan(flat_d, o_out)
+            torch.cuda.synchronize()
+            kf = []
+            for _ in range(args.steps):
+                flush.zero_()
+                s, e = torch.cuda.Event(True), torch.cuda.Event(True)
+                s.record()
+                o_plan(flat_d, o_out)
+                e.record()
+                e.synchronize()
+                kf.append(s.elapsed_time(e))
+            o_ms = statistics.mean(kf)
+            sec[key] = {"arithmetic": prec, "ms_per_step": o_ms, "perms_per_s": N_MATS / (o_ms * 1e-3),
+                        "speedup_vs_fp64": (ms / args.steps) / o_ms,
+                        "max_rel_diff_vs_fp64": float(((o_out - ref64).abs() / ref64.abs()).max()),
+                        "step_tflops": flops_total / (o_ms * 1e-3) / 1e12}
+            del o_plan
         sec.update(secondary(torch, _native, random_unitary, dev, flush, fp64_peak))
         line["secondary"] = sec
     if rank == 0 and ws == 1 and not args.skip_cpu:
@@ -608,6 +612,12 @@ def secondary(torch, _native, random_unitary, dev, flush, fp64_peak_tflops):
     t_loop = timed(loop, reps=2)
     res["cc2017_64_inputs_m64_n6"] = {"samples": 64000, "one_wavefront_ms": t_many, "per_input_loop_ms": t_loop,
                                       "samples_per_s": 64000 / (t_many * 1e-3)}
+    # the learned-proposal sampler, bounded for the default run: n = 30, m = 900 trained on
+    # 1024 exact samples (FP32 sampler), 8 chains x 8 steps of FP64-permanent acceptances
+    # against 96 exact float-float samples; and the n = 8, m = 64 companion
+    res["learned_mis_n30_m900"] = learned_case(torch, _native, random_unitary, 900, 30, 1024, 4, 8, 8, 96,
+                                               tvd=False)
+    res["learned_mis_n8_m64"] = learned_case(torch, _native, random_unitary, 64, 8, 20000, 10, 64, 200, 25600)
     # small case: SLOS m=12, n=6 and 1000 Naive amplitudes (latency-bound)
     from perceval_gb300 import BackendFactory, BasicState
     U12 = random_unitary(12, seed=0)
@@ -754,67 +764,91 @@ def secondary(torch, _native, random_unitary, dev, flush, fp64_peak_tflops):
     return res
 
 
-def run_learned(args):
-    """Learned-proposal Metropolised sampler vs the plain GPU exact sampler at
-    n = 30, m = 900 (Haar seed 0, input modes 0..29), plus the n = 8, m = 64 companion.
+def learned_case(torch, _native, random_unitary, m, n, n_train, epochs, chains, steps, n_ref, tvd=True,
+                 marginal_modes=8):
+    """Learned-proposal Metropolised sampler against the plain GPU exact sampler on one
+    Haar unitary (seed 0, input photons in modes 0..n-1).
 
-    Training data: exact Clifford & Clifford samples drawn by this library's sampler in
-    its FP32 mode (the float-float mode is the baseline it is compared with).  ESS: Geyer's initial
-    positive sequence estimator on each chain's log pi trace, summed over chains; the
-    exact sampler's samples are independent (ESS = N).  Marginals: sample means of n_i
-    and n_i n_j against the closed forms."""
-    import torch
-    from perceval_gb300 import _native
+    Training data: exact Clifford & Clifford samples from this library's sampler in its
+    FP32 mode.  Acceptance ratios: exact FP64 permanents (permanent plans, FP64 arithmetic).
+    ESS: Geyer's initial positive sequence on each chain's log pi trace, summed over
+    chains; the exact sampler's samples are independent (ESS = N).  Marginals: the exact
+    one-mode distributions P(n_i = a) of the most occupied modes and two-mode
+    distributions P(n_i = a, n_j = b) of pairs among them (generating-function
+    permanents, perceval_gb300.marginals) against each sampler's empirical ones, with
+    the binomial standard error of the largest probability at that sample count."""
     from perceval_gb300.learned import ProposalMLP, ess, exact_moments, run_mis, tvd_estimate
-    from perceval_gb300.utils.matrix import random_unitary
-    _native.load()
-    out = {}
-    for (m, n, n_train, epochs, chains, steps, n_ref) in ((900, 30, args.learned_train, 6, 16, 32, 152),
-                                                           (64, 8, 20000, 10, 64, 400, 25600)):
-        U = random_unitary(m, seed=0)
-        inp = [1] * n + [0] * (m - n)
-        Ud = torch.from_numpy(U).cuda()
-        # exact training samples (FP32 sampler)
-        t0 = time.perf_counter()
-        train = _native.cc2017_sample(Ud, inp, n_train, seed=101, precision=1).cpu().numpy()
-        t_train_samples = time.perf_counter() - t0
-        net = ProposalMLP(m, n, D=128, H=512, layers=3, seed=0)
-        t0 = time.perf_counter()
-        n_val = max(1, len(train) // 10)  # held-out tenth: early stopping on its NLL
-        losses = net.train(train[n_val:], epochs=epochs, batch=256, lr=1e-3, val=train[:n_val])
-        torch.cuda.synchronize()
-        t_fit = time.perf_counter() - t0
-        # Metropolised independence sampler (proposal sampling + exact permanents + scan)
-        res = run_mis(net, U, inp, chains=chains, steps=steps, seed=7, batch=512)
-        ess_mis = float(sum(ess(x) for x in res.log_pi))
-        # plain exact sampler (float-float), same unitary
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ref = _native.cc2017_sample(Ud, inp, n_ref, seed=202, precision=0).cpu().numpy()
-        t_ref = time.perf_counter() - t0
-        A, E2 = exact_moments(U, inp)
-        st = res.samples.reshape(-1, m).astype(np.float64)
-        refs = ref.astype(np.float64)
-        row = {"m": m, "n": n, "train_samples": n_train, "train_sampling_s": t_train_samples,
-               "fit_s": t_fit, "nll_first_last": [losses[0], losses[-1]],
-               "held_out_nll": net.val_nll, "kept_epoch": net.best_epoch,
-               "mis": {"chains": chains, "steps": steps, "proposals": res.proposals, "seconds": res.seconds,
-                       "accept_rate": res.accept_rate, "ess": ess_mis, "ess_per_s": ess_mis / res.seconds,
-                       "max_abs_err_E_n": float(np.abs(st.mean(0) - A).max()),
-                       "max_abs_err_E_nn": float(np.abs(st.T @ st / len(st) - E2).max())},
-               "exact_sampler": {"samples": n_ref, "seconds": t_ref, "ess_per_s": n_ref / t_ref,
-                                 "max_abs_err_E_n": float(np.abs(refs.mean(0) - A).max()),
-                                 "max_abs_err_E_nn": float(np.abs(refs.T @ refs / len(refs) - E2).max())}}
-        row["ess_per_s_ratio"] = row["mis"]["ess_per_s"] / row["exact_sampler"]["ess_per_s"]
+    from perceval_gb300.marginals import (empirical_one_mode, empirical_two_mode, one_mode_marginal,
+                                          two_mode_marginal)
+    U = random_unitary(m, seed=0)
+    inp = [1] * n + [0] * (m - n)
+    Ud = torch.from_numpy(U).cuda()
+    t0 = time.perf_counter()
+    train = _native.cc2017_sample(Ud, inp, n_train, seed=101, precision=1).cpu().numpy()
+    t_train_samples = time.perf_counter() - t0
+    net = ProposalMLP(m, n, D=128, H=512, layers=3, seed=0)
+    t0 = time.perf_counter()
+    n_val = max(1, len(train) // 10)  # held-out tenth: early stopping on its NLL
+    losses = net.train(train[n_val:], epochs=epochs, batch=256, lr=1e-3, val=train[:n_val])
+    torch.cuda.synchronize()
+    t_fit = time.perf_counter() - t0
+    res = run_mis(net, U, inp, chains=chains, steps=steps, seed=7, batch=512)
+    ess_mis = float(sum(ess(x) for x in res.log_pi))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ref = _native.cc2017_sample(Ud, inp, n_ref, seed=202, precision=0).cpu().numpy()
+    t_ref = time.perf_counter() - t0
+    A, E2 = exact_moments(U, inp)
+    st = res.samples.reshape(-1, m)
+    modes = [int(i) for i in np.argsort(-A)[:marginal_modes]]
+    one = {i: one_mode_marginal(U, inp, i) for i in modes}
+    pairs = [(modes[a], modes[b]) for a in range(len(modes)) for b in range(a + 1, len(modes))][:12]
+    two = {p: two_mode_marginal(U, inp, *p) for p in pairs}
+
+    def marg_err(samples):
+        e1 = max(float(np.abs(empirical_one_mode(samples, i, n) - one[i]).max()) for i in modes)
+        e2 = max(float(np.abs(empirical_two_mode(samples, i, j, n) - two[(i, j)]).max()) for i, j in pairs)
+        pmax = max(float(one[i].max()) for i in modes)
+        return {"max_abs_err_one_mode": e1, "max_abs_err_two_mode": e2, "samples": int(len(samples)),
+                "binomial_stderr_at_max_p": math.sqrt(pmax * (1 - pmax) / len(samples))}
+    row = {"m": m, "n": n, "train_samples": n_train, "train_sampling_s": t_train_samples,
+           "fit_s": t_fit, "nll_first_last": [losses[0], losses[-1]],
+           "held_out_nll": net.val_nll, "kept_epoch": net.best_epoch,
+           "mis": {"chains": chains, "steps": steps, "proposals": res.proposals, "seconds": res.seconds,
+                   "acceptance_arithmetic": "fp64 permanents",
+                   "accept_rate": res.accept_rate, "ess": ess_mis, "ess_per_s": ess_mis / res.seconds,
+                   "max_abs_err_E_n": float(np.abs(st.astype(float).mean(0) - A).max()),
+                   "marginals": marg_err(st)},
+           "exact_sampler": {"samples": n_ref, "seconds": t_ref, "ess_per_s": n_ref / t_ref,
+                             "arithmetic": "float-float",
+                             "max_abs_err_E_n": float(np.abs(ref.astype(float).mean(0) - A).max()),
+                             "marginals": marg_err(ref)},
+           "marginal_modes": modes, "marginal_pairs": [list(p) for p in pairs]}
+    row["ess_per_s_ratio"] = row["mis"]["ess_per_s"] / row["exact_sampler"]["ess_per_s"]
+    if tvd:
         # TVD(q, pi) on photon sequences from the exact samples: trained vs untrained network
         untrained = ProposalMLP(m, n, D=128, H=512, layers=3, seed=0)
         t, te = tvd_estimate(net, U, inp, ref, seed=5)
         u0, ue = tvd_estimate(untrained, U, inp, ref, seed=5)
         row["tvd_q_pi_sequences"] = {"samples": int(len(ref)), "trained": t, "trained_stderr": te,
                                      "untrained": u0, "untrained_stderr": ue}
-        out[f"n{n}_m{m}"] = row
-    # tensor-pipe rate of the network's GEMM kernel (pcvl_gemm_bf16, mma.sync BF16, FP32
-    # accumulation) at the training shapes of n = 30, m = 900 (256 sequences x 30 steps)
+    return row
+
+
+def run_learned(args):
+    """Learned-proposal Metropolised sampler vs the plain GPU exact sampler at
+    n = 30, m = 900, plus the n = 8, m = 64 companion (``learned_case``), and the
+    tensor-pipe rate of the network's GEMM kernel."""
+    import torch
+    from perceval_gb300 import _native
+    from perceval_gb300.utils.matrix import random_unitary
+    _native.load()
+    out = {}
+    for (m, n, n_train, epochs, chains, steps, n_ref) in ((900, 30, args.learned_train, 6, 16, 32, 152),
+                                                           (64, 8, 20000, 10, 64, 400, 25600)):
+        out[f"n{n}_m{m}"] = learned_case(torch, _native, random_unitary, m, n, n_train, epochs, chains, steps, n_ref)
+    # tensor-pipe rate of the network's GEMM kernel (pcvl_gemm_bf16: tcgen05 MMA from TMA-staged
+    # tiles, FP32 accumulation in tensor memory) at the training shapes of n = 30, m = 900 (256 sequences x 30 steps)
     # and at 8192^3, against the measured cuBLAS BF16 burst peak
     try:
         peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"]
@@ -874,14 +908,15 @@ def profile_case(name: str):
     _native.load()
     autotune.load()  # the launch shapes the headline run tuned and cached, if any
     dev = torch.device("cuda")
-    if name in ("perm24", "perm24ff"):
-        # 64 matrices of the n = 24 bin (one perm_bin_f64<24> or perm_bin_kernel<24> launch)
+    if name in ("perm24", "perm24dadd", "perm24ff"):
+        # 64 matrices of the n = 24 bin (one perm_bin_fx<24>, perm_bin_f64<24> or
+        # perm_bin_kernel<24> launch)
         mats, flat, offs, sizes = make_batch(seed=0)
         sel = [i for i in range(N_MATS) if sizes[i] == 24][:64]
         sub = torch.from_numpy(np.concatenate([mats[i].reshape(-1) for i in sel])).to(dev)
         out = torch.empty(len(sel), dtype=torch.complex128, device=dev)
         _native.permanent_batch(sub, np.arange(len(sel), dtype=np.int64) * 576, np.full(len(sel), 24, np.int32), out,
-                                precision="fp64" if name == "perm24" else "float-float")
+                                precision={"perm24": "fp64", "perm24dadd": "fp64-dadd"}.get(name, "float-float"))
     elif name in ("slos20", "slos20ff"):
         # SLOS m = 20, n = 10: last layer 20,030,010 states (320 MB, above L2)
         plan = _native.SlosPlan(20, [1] * 10 + [0] * 10, precision="fp64" if name == "slos20" else "float-float")
@@ -943,7 +978,7 @@ def main():
                     help="run the learned-proposal sampler workload (n=30, m=900 and n=8, m=64) and exit")
     ap.add_argument("--learned-train", type=int, default=2048, help="exact training samples at n=30")
     ap.add_argument("--large-perm", action="store_true", help="one n = 40 permanent (about a minute)")
-    ap.add_argument("--profile-case", choices=["perm24", "perm24ff", "slos20", "slos20ff", "slos20p", "slosmask22", "slap1024", "slos16b256",
+    ap.add_argument("--profile-case", choices=["perm24", "perm24dadd", "perm24ff", "slos20", "slos20ff", "slos20p", "slosmask22", "slap1024", "slos16b256",
                                                "cc2017", "gurvits20", "gemm"],
                     help="run one small untimed case of a single kernel (for ncu) and exit")
     args = ap.parse_args()

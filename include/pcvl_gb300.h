@@ -28,13 +28,17 @@ extern "C" {
 
 /* Arithmetic of the permanent, SLOS and sampler kernels (`precision` arguments).
  * PCVL_PREC_FP64: native FP64, the reference's own arithmetic (complex128 in
- * exqalibur); the default of the Python layer.  PCVL_PREC_FLOAT_FLOAT: every value an
- * unevaluated pair of FP32 numbers (~48 significant bits) on the FP32 pipe, several
- * times faster on GB300, whose FP64 rate is a small fraction of its FP32 rate.
- * PCVL_PREC_FP32: FP32 with compensated sums (sampler only). */
+ * exqalibur); the default of the Python layer.  For permanents every row sum is exact
+ * (64-bit fixed point on the integer pipe, rounded once to FP64) and every product and
+ * sum is an FP64 operation.  PCVL_PREC_FP64_DADD (permanents only): the same with the
+ * row sums too in FP64 additions, one rounding per addition.  PCVL_PREC_FLOAT_FLOAT:
+ * every value an unevaluated pair of FP32 numbers (~48 significant bits) on the FP32
+ * pipe, several times faster on GB300, whose FP64 rate is a small fraction of its FP32
+ * rate.  PCVL_PREC_FP32: FP32 with compensated sums (sampler only). */
 #define PCVL_PREC_FLOAT_FLOAT 0
 #define PCVL_PREC_FP32 1
 #define PCVL_PREC_FP64 2
+#define PCVL_PREC_FP64_DADD 3
 
 /* ------------------------------------------------------------------ errors */
 /* Library version string, e.g. "pcvl_gb300 0.2.0 sm_103a". */
@@ -57,7 +61,7 @@ int pcvl_release_workspace(void);
  * every thread enumerates from a shared-memory table of row-sum parts and "hi" bits
  * spread over threads and CTAs (walked in Gray-code order in FP64), so one large
  * matrix uses every SM; matrices are binned by size, one launch per size.  precision:
- * PCVL_PREC_FP64 or PCVL_PREC_FLOAT_FLOAT.  The matrices must not overlap in mats_d,
+ * PCVL_PREC_FP64, PCVL_PREC_FP64_DADD or PCVL_PREC_FLOAT_FLOAT.  The matrices must not overlap in mats_d,
  * except as identical entries (same offset and size): each is rescaled in place in
  * the library's scratch at its own offsets.  offsets_h and sizes_h are host arrays.
  * Scratch comes from a stream-ordered pool per call, so concurrent calls on
@@ -105,7 +109,8 @@ int pcvl_permanent_estimate_batch(const double* mats_d, const int64_t* offsets_h
 
 /* Launch-shape tuning of the permanent kernels (no reference counterpart; written by the
  * autotuner in perceval_gb300/autotune.py).  For method (0 Glynn, 1 Ryser), precision
- * (PCVL_PREC_FP64 or PCVL_PREC_FLOAT_FLOAT: each arithmetic has its own table) and size n:
+ * (PCVL_PREC_FP64, PCVL_PREC_FP64_DADD or PCVL_PREC_FLOAT_FLOAT: each arithmetic has its
+ * own table) and size n:
  * lo_bits = sign bits every thread enumerates from the shared-memory table (-1: built-in
  * min(7, max(0, F - 7)) with F the free bits), ctas_per_sm = target CTAs per SM over a
  * size bin (0: built-in 8).  Applies to later calls and plans on every device; results

@@ -136,13 +136,14 @@ def check(status: int, what: str):
 
 
 # precision codes of the C ABI (PCVL_PREC_*)
-PREC_FLOAT_FLOAT, PREC_FP32, PREC_FP64 = 0, 1, 2
+PREC_FLOAT_FLOAT, PREC_FP32, PREC_FP64, PREC_FP64_DADD = 0, 1, 2, 3
 _PREC_NAMES = {"fp64": PREC_FP64, "float64": PREC_FP64, "float-float": PREC_FLOAT_FLOAT,
-               "ff": PREC_FLOAT_FLOAT, "fp32": PREC_FP32}
+               "ff": PREC_FLOAT_FLOAT, "fp32": PREC_FP32, "fp64-dadd": PREC_FP64_DADD}
 
 
 def precision_code(precision) -> int:
-    """ABI code of a precision given as a code or a name ("fp64", "float-float", "fp32")."""
+    """ABI code of a precision given as a code or a name ("fp64", "float-float", "fp32";
+    permanents also take "fp64-dadd": FP64 with the row sums in FP64 additions too)."""
     if isinstance(precision, str):
         try:
             return _PREC_NAMES[precision.lower()]

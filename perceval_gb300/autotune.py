@@ -97,9 +97,9 @@ def tune_permanents(sizes=range(8, 27), method: int = 0, target_ms: float = 20.0
     """Tunes every size in ``sizes`` for one arithmetic and installs the winners; returns
     the table {"key": device_key(), "method": method, "precision": name, "entries": {n: {...}}}."""
     code = _native.precision_code(precision)
-    name = "fp64" if code == _native.PREC_FP64 else "float-float"
+    name = _prec_name(code)
     if rate_flops is None:  # work per candidate run: about target_ms at the expected rate
-        rate_flops = 0.7e12 if code == _native.PREC_FP64 else 3.5e12
+        rate_flops = 3.5e12 if code == _native.PREC_FLOAT_FLOAT else 0.7e12
     entries = {}
     for n in sizes:
         n = int(n)
@@ -132,6 +132,10 @@ def tune_permanents(sizes=range(8, 27), method: int = 0, target_ms: float = 20.0
             log(f"{name} n={n}: lo={eff_lo} ctas/SM={eff_c} {t:.3f} ms (built-in {t_default:.3f} ms, "
                 f"{count} matrices)")
     return {"key": device_key(), "method": method, "precision": name, "entries": entries}
+
+
+def _prec_name(code: int) -> str:
+    return {_native.PREC_FP64: "fp64", _native.PREC_FP64_DADD: "fp64-dadd"}.get(code, "float-float")
 
 
 def _tables(doc: dict) -> list[dict]:
@@ -200,7 +204,7 @@ def ensure_tuned(sizes=range(8, 27), method: int = 0, path: Path | None = None, 
     """Loads the cached table of (method, arithmetic) for this device, or tunes ``sizes``
     and caches the result."""
     path = Path(path) if path else default_cache_path()
-    name = "fp64" if _native.precision_code(precision) == _native.PREC_FP64 else "float-float"
+    name = _prec_name(_native.precision_code(precision))
     tables = _cached(path, device_key())
     for t in tables:
         if int(t.get("method", 0)) == method and t.get("precision", "float-float") == name:

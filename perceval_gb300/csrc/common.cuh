@@ -19,7 +19,7 @@
 namespace pcvl {
 
 // Arithmetic of the permanent, SLOS and sampler kernels (the ABI's PCVL_PREC_* codes).
-enum Precision : int { kPrecFloatFloat = 0, kPrecFP32 = 1, kPrecFP64 = 2 };
+enum Precision : int { kPrecFloatFloat = 0, kPrecFP32 = 1, kPrecFP64 = 2, kPrecFP64Dadd = 3 };
 
 // ------------------------------------------------------------------ df64 scalars
 struct dd {

@@ -31,8 +31,14 @@ struct PermDesc {
   int32_t n;
 };
 
-__device__ __forceinline__ void store_prepared(cdd* dst, double re, double im) { *dst = cdd_from(re, im); }
-__device__ __forceinline__ void store_prepared(double2* dst, double re, double im) { *dst = make_double2(re, im); }
+__device__ __forceinline__ void store_prepared(cdd* dst, double re, double im, int) { *dst = cdd_from(re, im); }
+__device__ __forceinline__ void store_prepared(double2* dst, double re, double im, int) {
+  *dst = make_double2(re, im);
+}
+// fixed point with F fraction bits (the exact-row-sum FP64 kernel): |value| < 2^c, F = 62 - c
+__device__ __forceinline__ void store_prepared(longlong2* dst, double re, double im, int F) {
+  *dst = make_longlong2(__double2ll_rn(ldexp(re, F)), __double2ll_rn(ldexp(im, F)));
+}
 
 template <typename E>
 __global__ void perm_prepare(const double2* __restrict__ src, const int64_t* __restrict__ offs,
@@ -64,7 +70,7 @@ __global__ void perm_prepare(const double2* __restrict__ src, const int64_t* __r
     esum += e;
     for (int j = 0; j < n; ++j) {
       const double2 v = src[off + (int64_t)i * n + j];
-      store_prepared(&dst[off + (int64_t)i * n + j], ldexp(v.x, e), ldexp(v.y, e));
+      store_prepared(&dst[off + (int64_t)i * n + j], ldexp(v.x, e), ldexp(v.y, e), 62 - c);
     }
   }
 #pragma unroll
@@ -118,23 +124,27 @@ static int launch_bin(int n, const PermBinArgs& a, PermNode* node = nullptr) {
   return launch_perm_bin_37_40(n, a, node);
 }
 
-// Tuning table: per arithmetic (0 float-float, 1 FP64), method and size, the lo bits and
-// the target CTAs per SM of a bin, packed as (L + 1) | ctas << 8 (0 in a field: the
-// built-in choice).  Written by pcvl_perm_set_tuning (the autotuner), read without locks
-// by every launch.
-static std::atomic<uint32_t> g_tune[2][2][kPermMaxN + 1];
+// Tuning table: per arithmetic (0 float-float, 1 FP64, 2 FP64 with FP64 row sums), method
+// and size, the lo bits and the target CTAs per SM of a bin, packed as (L + 1) | ctas << 8
+// (0 in a field: the built-in choice).  Written by pcvl_perm_set_tuning (the autotuner),
+// read without locks by every launch.
+static std::atomic<uint32_t> g_tune[3][2][kPermMaxN + 1];
 
-static int prec_slot(int prec) { return prec == kPrecFP64 ? 1 : 0; }
+static int prec_slot(int prec) { return prec == kPrecFP64 ? 1 : prec == kPrecFP64Dadd ? 2 : 0; }
 
-// prepare kernel of an arithmetic (prepared elements: double2 for FP64, cdd otherwise)
+// prepare kernel of an arithmetic (prepared elements: fixed-point longlong2 for FP64,
+// double2 for FP64 with FP64 row sums, cdd for float-float)
 static void* prepare_func(int prec) {
-  return prec == kPrecFP64 ? reinterpret_cast<void*>(perm_prepare<double2>)
-                           : reinterpret_cast<void*>(perm_prepare<cdd>);
+  if (prec == kPrecFP64) return reinterpret_cast<void*>(perm_prepare<longlong2>);
+  if (prec == kPrecFP64Dadd) return reinterpret_cast<void*>(perm_prepare<double2>);
+  return reinterpret_cast<void*>(perm_prepare<cdd>);
 }
 
 static void launch_prepare(int prec, unsigned blocks, cudaStream_t stream, const double2* src, const int64_t* offs,
                            const int32_t* sizes, int32_t count, void* prep, int32_t* exps) {
   if (prec == kPrecFP64)
+    perm_prepare<longlong2><<<blocks, 256, 0, stream>>>(src, offs, sizes, count, (longlong2*)prep, exps);
+  else if (prec == kPrecFP64Dadd)
     perm_prepare<double2><<<blocks, 256, 0, stream>>>(src, offs, sizes, count, (double2*)prep, exps);
   else
     perm_prepare<cdd><<<blocks, 256, 0, stream>>>(src, offs, sizes, count, (cdd*)prep, exps);
@@ -293,10 +303,10 @@ static PermBinArgs bin_args(const BatchLayout& L, unsigned char* base, int n, in
 
 using namespace pcvl;
 
-#define PCVL_CHECK_PERM_PREC(p)                                                                        \
-  PCVL_CHECK((p) == PCVL_PREC_FP64 || (p) == PCVL_PREC_FLOAT_FLOAT,                                       \
-             "precision must be %d (FP64) or %d (float-float), got %d", PCVL_PREC_FP64, PCVL_PREC_FLOAT_FLOAT, \
-             (p))
+#define PCVL_CHECK_PERM_PREC(p)                                                                           \
+  PCVL_CHECK((p) == PCVL_PREC_FP64 || (p) == PCVL_PREC_FP64_DADD || (p) == PCVL_PREC_FLOAT_FLOAT,          \
+             "precision must be %d (FP64), %d (FP64 with FP64 row sums) or %d (float-float), got %d",       \
+             PCVL_PREC_FP64, PCVL_PREC_FP64_DADD, PCVL_PREC_FLOAT_FLOAT, (p))
 
 extern "C" int pcvl_permanent_batch(const double* mats_d, const int64_t* offsets_h, const int32_t* sizes_h,
                                     int32_t count, double* out_d, int32_t method, int32_t precision, void* stream_) {

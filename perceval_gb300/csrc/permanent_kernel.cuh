@@ -20,15 +20,16 @@
 // matrix with compensation and applies the 2^{1-n} (or (-1)^n) and row-scaling
 // factors.
 //
-// Two arithmetics share this layout (16 bytes per prepared element either way):
-//  * FP64 (perm_bin_f64, the default, the reference's own arithmetic): row sums by
-//    DADD, the product tree by DMUL/DFMA with the last product fused into the signed
-//    accumulation, each hi pattern's lo sweep added to a Neumaier-compensated sum.
-//    The hi patterns of a thread are walked in Gray-code order, so consecutive
-//    patterns differ in one column and H_i moves by one DFMA per component (H is
-//    rebuilt exactly every 32 patterns).
+// Three arithmetics share this layout (16 bytes per prepared element in each):
+//  * FP64 (perm_bin_fx, the default): exact fixed-point row sums on the integer pipe,
+//    each converted once to FP64; the product tree by DMUL/DFMA with the last product
+//    fused into the signed accumulation; each hi pattern's lo sweep added to a
+//    Neumaier-compensated FP64 sum.  The hi patterns of a thread are walked in
+//    Gray-code order, so consecutive patterns differ in one column.
+//  * FP64 with FP64 row sums (perm_bin_f64): the same with the row sums and their
+//    Gray-code updates in DADD / DFMA (H rebuilt exactly every 32 patterns).
 //  * float-float (perm_bin_kernel): every value an unevaluated pair of FP32 numbers on
-//    the FP32 pipe (~48 significant bits), about 4x faster on GB300, opt-in.
+//    the FP32 pipe (~48 significant bits), several times faster on GB300, opt-in.
 #pragma once
 #include "common.cuh"
 
@@ -44,7 +45,7 @@ struct PermBinArgs {
   int64_t P;              // hi patterns per thread per item
   int64_t items_per_mat;  // CTAs per matrix
   int32_t ryser;          // 0 Glynn, 1 Ryser
-  int32_t prec;           // kPrecFloatFloat or kPrecFP64
+  int32_t prec;           // kPrecFP64 (exact row sums), kPrecFP64Dadd or kPrecFloatFloat
   double2* partials;      // one per item, bin-local indexing
   cudaStream_t stream;
 };
@@ -364,6 +365,192 @@ __global__ void __launch_bounds__(kPermThreads) perm_bin_f64(PermBinArgs a) {
   }
 }
 
+// ------------------------------------------------------------------ exact row sums
+// The FP64 default (perm_bin_fx) keeps every row sum exact: the prepared matrix holds
+// each scaled element as a 64-bit fixed-point integer (value 2^F x element, F = 62 - c,
+// so every row sum, |r| < 2^c, stays below 2^62), the lo table, the hi parts and their
+// Gray-code updates are integer additions on the integer pipe, and each row sum is
+// converted to FP64 once, rounded to nearest even, by integer operations on its bits.
+// The product tree and the compensated accumulation are the FP64 ones above, so every
+// rounding of the sum is an FP64 rounding and the row sums carry none (FP64 row sums
+// round at every addition).  Per sign vector the FP64 pipe then issues 4n - 4
+// instructions instead of 6n - 4.
+template <int N>
+struct FixedPoint {
+  static constexpr int c = 20 < 120 / N ? 20 : 120 / N;  // row l1 norms in [2^(c-1), 2^c)
+  static constexpr int F = 62 - c;                        // fixed-point fraction bits
+};
+
+// x 2^-F as a double, rounded to nearest even, from the binary64 format's definition
+// (sign, 11-bit biased exponent, 52 stored mantissa bits) with integer operations only.
+__device__ __forceinline__ double fx_to_f64(long long x, int F) {
+  const unsigned long long ux = (unsigned long long)x;
+  const unsigned long long sgn = ux & 0x8000000000000000ull;
+  const unsigned long long ax = x < 0 ? 0ull - ux : ux;
+  const int lz = __clzll((long long)ax);                 // 64 when ax == 0
+  const unsigned long long mn = ax << (lz & 63);         // leading one at bit 63
+  unsigned long long mant = mn >> 11;                    // 53 bits, leading one at bit 52
+  const unsigned int rem = (unsigned int)mn & 0x7ffu;    // the 11 bits rounded away
+  mant += (rem + (unsigned int)(mant & 1ull) + 0x3ffu) >> 11;  // up when rem > half, or = half and odd
+  const unsigned long long e = (unsigned long long)(1023 + 63 - F - lz);
+  const unsigned long long bits = sgn | ((e << 52) + mant - (1ull << 52));  // a carry out of mant bumps e
+  return ax == 0 ? 0.0 : __longlong_as_double((long long)bits);
+}
+
+template <int LO, int HI, int F>
+struct RowProdFX {
+  static __device__ __forceinline__ double2 run(const longlong2* H, const longlong2* Tb) {
+    if constexpr (HI - LO == 1) {
+      const longlong2 t = Tb[LO];
+      return make_double2(fx_to_f64(H[LO].x + t.x, F), fx_to_f64(H[LO].y + t.y, F));
+    } else {
+      constexpr int MID = (LO + HI) / 2;
+      const double2 x = RowProdFX<LO, MID, F>::run(H, Tb);
+      const double2 y = RowProdFX<MID, HI, F>::run(H, Tb);
+      return cmul64(x, y);
+    }
+  }
+};
+
+template <int N>
+__device__ __forceinline__ void lo_sweep_fx(const longlong2* H, const longlong2* T, int nsteps, uint32_t hsign,
+                                            double& sr, double& si) {
+  constexpr int F = FixedPoint<N>::F;
+  for (int b = 0; b < nsteps; ++b) {
+    const longlong2* Tb = T + b * N;
+    const uint32_t s = (((uint32_t)__popc(b) ^ hsign) & 1u) << 31;
+    if constexpr (N == 1) {
+      sr += flip64(fx_to_f64(H[0].x + Tb[0].x, F), s);
+      si += flip64(fx_to_f64(H[0].y + Tb[0].y, F), s);
+    } else {
+      constexpr int MID = N / 2;
+      double2 x = RowProdFX<0, MID, F>::run(H, Tb);
+      const double2 y = RowProdFX<MID, N, F>::run(H, Tb);
+      x.x = flip64(x.x, s);
+      x.y = flip64(x.y, s);
+      sr = fma(x.x, y.x, sr);
+      sr = fma(-x.y, y.y, sr);
+      si = fma(x.x, y.y, si);
+      si = fma(x.y, y.x, si);
+    }
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(kPermThreads) perm_bin_fx(PermBinArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  longlong2* As = reinterpret_cast<longlong2*>(smem_raw);  // N x N fixed-point elements
+  longlong2* T = As + N * N;                               // (1 << L) x N
+  __shared__ double red[4][kPermThreads / 32];
+
+  const int64_t item = blockIdx.x;
+  const int64_t mat_local = item / a.items_per_mat;
+  const int64_t chunk = item - mat_local * a.items_per_mat;
+  const int mid = a.mids[mat_local];
+  const longlong2* A = static_cast<const longlong2*>(a.A) + a.offs[mid];
+  const int L = a.L;
+  const int ryser = a.ryser;
+  const int tid = threadIdx.x;
+
+  for (int e = tid; e < N * N; e += blockDim.x) As[e] = A[e];
+  __syncthreads();
+
+  const int lo_col0 = ryser ? 0 : 1;
+  for (int i = tid; i < N; i += blockDim.x) {
+    longlong2 t0 = make_longlong2(0, 0);
+    if (!ryser)
+      for (int l = 0; l < L; ++l) {
+        t0.x += As[i * N + lo_col0 + l].x;
+        t0.y += As[i * N + lo_col0 + l].y;
+      }
+    T[i] = t0;
+  }
+  __syncthreads();
+  for (int l = 0; l < L; ++l) {
+    const int half = 1 << l;
+    for (int e = tid; e < half * N; e += blockDim.x) {
+      const int b = e / N, i = e - b * N;
+      const longlong2 d = As[i * N + lo_col0 + l];
+      const longlong2 t = T[b * N + i];
+      T[(b + half) * N + i] = ryser ? make_longlong2(t.x + d.x, t.y + d.y) : make_longlong2(t.x - 2 * d.x, t.y - 2 * d.y);
+    }
+    __syncthreads();
+  }
+
+  const uint64_t nhi = 1ull << a.Hbits;
+  const uint64_t h0 = (uint64_t)chunk * (uint64_t)(kPermThreads * a.P) + (uint64_t)tid * a.P;
+  const int hi_col0 = ryser ? L : 1 + L;
+  const int nsteps = 1 << L;
+  double Sr = 0.0, Cr = 0.0, Si = 0.0, Ci = 0.0;
+  longlong2 H[N];
+  for (int64_t p = 0; p < a.P; ++p) {
+    const uint64_t h = h0 + p;
+    if (h >= nhi) break;
+    const uint64_t g = h ^ (h >> 1);  // Gray code: g(h) and g(h - 1) differ in bit ctz(h)
+    if (p == 0) {                     // integer updates are exact: one build per thread
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        longlong2 v = ryser ? make_longlong2(0, 0) : As[i * N];
+        for (int t = 0; t < a.Hbits; ++t) {
+          const longlong2 x = As[i * N + hi_col0 + t];
+          const bool bit = (g >> t) & 1ull;
+          if (ryser) {
+            if (bit) {
+              v.x += x.x;
+              v.y += x.y;
+            }
+          } else {
+            v.x += bit ? -x.x : x.x;
+            v.y += bit ? -x.y : x.y;
+          }
+        }
+        H[i] = v;
+      }
+    } else {
+      const int t = __ffsll((long long)h) - 1;
+      const bool set = (g >> t) & 1ull;
+      const long long c = ryser ? (set ? 1 : -1) : (set ? -2 : 2);
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const longlong2 x = As[i * N + hi_col0 + t];
+        H[i].x += c * x.x;
+        H[i].y += c * x.y;
+      }
+    }
+    double sr = 0.0, si = 0.0;
+    lo_sweep_fx<N>(H, T, nsteps, (uint32_t)(__popcll(g) & 1), sr, si);
+    comp_add(Sr, Cr, sr);
+    comp_add(Si, Ci, si);
+  }
+
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    const double or_ = __shfl_down_sync(0xffffffffu, Sr, d), oc = __shfl_down_sync(0xffffffffu, Cr, d);
+    const double oi = __shfl_down_sync(0xffffffffu, Si, d), od = __shfl_down_sync(0xffffffffu, Ci, d);
+    Cr += oc;
+    comp_add(Sr, Cr, or_);
+    Ci += od;
+    comp_add(Si, Ci, oi);
+  }
+  if ((tid & 31) == 0) {
+    red[0][tid >> 5] = Sr;
+    red[1][tid >> 5] = Cr;
+    red[2][tid >> 5] = Si;
+    red[3][tid >> 5] = Ci;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double sr = red[0][0], cr = red[1][0], si = red[2][0], ci = red[3][0];
+    for (int w = 1; w < kPermThreads / 32; ++w) {
+      cr += red[1][w];
+      comp_add(sr, cr, red[0][w]);
+      ci += red[3][w];
+      comp_add(si, ci, red[2][w]);
+    }
+    a.partials[item] = make_double2(sr + cr, si + ci);
+  }
+}
+
 // Launch shape of one bin, for callers that build a CUDA graph node instead of launching.
 struct PermNode {
   void* func;
@@ -376,7 +563,9 @@ template <int N>
 int launch_perm_bin_n(const PermBinArgs& a, PermNode* node) {
   static_assert(sizeof(cdd) == sizeof(double2), "both arithmetics use 16-byte elements");
   const size_t smem = (size_t)(N * N + (1 << a.L) * N) * sizeof(double2);
-  void (*kern)(PermBinArgs) = a.prec == kPrecFP64 ? perm_bin_f64<N> : perm_bin_kernel<N>;
+  void (*kern)(PermBinArgs) = a.prec == kPrecFP64       ? perm_bin_fx<N>
+                              : a.prec == kPrecFP64Dadd ? perm_bin_f64<N>
+                                                        : perm_bin_kernel<N>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;

@@ -9,8 +9,9 @@ r = (r_1..r_n) of modes (one per photon, order kept) gets
     pi(r) = |Perm(U[r, in])|^2 / n!
 
 so that the multiset of r has the boson-sampling probability |Perm|^2 / prod s!: every
-ordering of a multiset is equally likely.  The permanent is the exact float-float
-Glynn kernel (pcvl_permanent_batch).
+ordering of a multiset is equally likely.  The permanent is the exact Glynn kernel in
+native FP64 (permanent plans, pcvl_perm_plan_*), so the acceptance ratios are FP64
+throughout.
 
 Proposal.  An autoregressive network q(r) = prod_k q(r_k | r_<k): the input row of
 step k is pos_emb[k] + sum_{l<k} mode_emb[r_l] (mode embedding dim D), followed by
@@ -240,13 +241,13 @@ def _perm_plan(S: int, n: int) -> "_native.PermPlan":
     if plan is None:
         if len(_PERM_PLANS) >= 8:
             _PERM_PLANS.pop(next(iter(_PERM_PLANS))).close()
-        plan = _native.PermPlan(np.arange(S, dtype=np.int64) * n * n, np.full(S, n, np.int32))
+        plan = _native.PermPlan(np.arange(S, dtype=np.int64) * n * n, np.full(S, n, np.int32), precision="fp64")
         _PERM_PLANS[key] = plan
     return plan
 
 
 def log_abs_perm2(U_dev: torch.Tensor, cols: np.ndarray, seq: torch.Tensor) -> np.ndarray:
-    """log |Perm(U[seq_s, cols])|^2 for every sequence (exact float-float permanents)."""
+    """log |Perm(U[seq_s, cols])|^2 for every sequence (exact FP64 permanents)."""
     S, n = seq.shape
     colsd = torch.as_tensor(cols, dtype=torch.long, device=U_dev.device)
     mats = U_dev[seq.long()][:, :, colsd].contiguous()  # S x n x n
@@ -308,7 +309,7 @@ def tvd_estimate(proposal: "ProposalMLP", U: np.ndarray, input_state, exact_coun
     """Total-variation distance between the proposal q and the target pi on photon
     sequences, TVD = E_{r ~ pi}[max(0, 1 - q(r) / pi(r))], estimated without bias from
     exact samples (counts) given a uniformly random photon order (a draw from pi); exact
-    pi(r) = |Perm|^2 / n! from the float-float permanents.  Returns (estimate, standard
+    pi(r) = |Perm|^2 / n! from FP64 permanents.  Returns (estimate, standard
     error).  It bounds the distance between the two laws on output multisets from above."""
     rng = np.random.default_rng(seed)
     m = U.shape[0]

@@ -1,5 +1,6 @@
 """GPU permanents against the FP64 oracle, the mpmath golden vectors and exact
-identities, in both arithmetics (native FP64, the default, and float-float).
+identities, in every arithmetic (FP64 with exact row sums, the default; FP64 with FP64
+row sums; float-float).
 Tolerance: 1e-10 relative (|gpu - ref| <= 1e-10 |ref|) wherever the problem's own
 conditioning allows it; the all-ones and equal-row cases state their rounding bound."""
 import json
@@ -14,8 +15,8 @@ from perceval_gb300.utils.matrix import random_unitary
 
 pytestmark = pytest.mark.gpu
 RTOL = 1e-10
-PRECS = ["fp64", "float-float"]
-UNIT = {"fp64": 2.0 ** -53, "float-float": 2.0 ** -47}  # unit roundoff of each arithmetic
+PRECS = ["fp64", "fp64-dadd", "float-float"]
+UNIT = {"fp64": 2.0 ** -53, "fp64-dadd": 2.0 ** -53, "float-float": 2.0 ** -47}  # unit roundoff
 
 
 def pack(mats):
@@ -85,7 +86,7 @@ def test_batched_haar_vs_oracle(native, oracle, prec):
     got = gpu_perms(native, mats, 1, prec)
     rel = np.abs(got - ref) / np.abs(ref)
     assert rel[sizes <= 12].max() <= RTOL
-    assert rel.max() <= (1e-10 if prec == "fp64" else 1e-8)
+    assert rel.max() <= (1e-8 if prec == "float-float" else 1e-10)
 
 
 @pytest.mark.parametrize("prec", PRECS)
@@ -124,7 +125,7 @@ def test_n32_against_committed_oracle_value(native, prec):
         ref = complex(*case["perm_glynn"])
         g = gpu_perms(native, [a], 0, prec)[0]
         assert abs(g - ref) <= RTOL * abs(ref), abs(g - ref) / abs(ref)
-        if prec == "fp64":
+        if prec != "float-float":
             r = gpu_perms(native, [a], 1, prec)[0]
             assert abs(r - ref) <= 1e-6 * abs(ref)
 
@@ -154,7 +155,8 @@ def _abs_term_sum(r, ryser):
 
 # (n, method, arithmetics): Ryser is conditioned like n^n / n! on these matrices, so it is
 # checked only where its rounding bound stays small; FP64 n = 40 would take ~5 minutes
-EQUAL_ROW_CASES = [(n, 0, p) for n in (20, 24, 28, 32, 36) for p in PRECS] + [(40, 0, "float-float")] + \
+EQUAL_ROW_CASES = [(n, 0, p) for n in (20, 24, 28, 32) for p in PRECS] + \
+                  [(36, 0, "fp64"), (36, 0, "float-float"), (40, 0, "float-float")] + \
                   [(n, 1, p) for n in (20, 24) for p in PRECS]
 
 
@@ -251,3 +253,19 @@ def test_block_diagonal_identity(native, oracle, prec):
     got = gpu_perms(native, mats, 0, prec)
     for g, r in zip(got, refs):
         assert abs(g - r) <= RTOL * abs(r)
+
+
+def test_fixed_point_conversion_rounding(native):
+    """The FP64 default converts each exact integer row sum to FP64 with integer operations:
+    matrices whose row sums are exactly representable at every sign vector (dyadic
+    entries) give exactly the same permanent in both FP64 kernels, and products of
+    diagonal entries near the rounding boundary are rounded to nearest."""
+    rng = np.random.default_rng(77)
+    for n in (3, 9, 17):
+        a = (rng.integers(-64, 65, (n, n)) + 1j * rng.integers(-64, 65, (n, n))) / 64.0
+        fx = gpu_perms(native, [a], 0, "fp64")[0]
+        dd = gpu_perms(native, [a], 0, "fp64-dadd")[0]
+        assert abs(fx - dd) <= 1e-13 * abs(dd)
+    d = 1.0 + np.array([2.0 ** -52, 3 * 2.0 ** -53, 2.0 ** -30, -2.0 ** -40])
+    got = gpu_perms(native, [np.diag(d).astype(complex)], 0, "fp64")[0]
+    assert abs(got - np.prod(d)) <= 4 * 2.0 ** -53
