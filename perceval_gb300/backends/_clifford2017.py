@@ -1,7 +1,9 @@
 """Exact boson sampling on the GPU (restating perceval/backends/_clifford2017.py:36-61).
 
-``samples(count)`` draws all samples in one ``pcvl_cc2017_sample`` launch (one CTA
-per sample, Clifford & Clifford 2018 algorithm B).  Randomness comes from
+``samples(count)`` draws all samples in one ``pcvl_cc2017_sample`` call (Clifford &
+Clifford 2018 algorithm B): up to 32768 samples advance together photon by photon, two
+kernels per photon over all of them (the sub-permanents, spread over lane groups and
+CTAs, then the weights and the draw).  Randomness comes from
 Philox4x32-10 keyed by the seed of ``perceval_gb300.utils.random_seed``; every
 sample has its own counter, so a fixed seed gives the same samples however the
 launch is scheduled, and successive calls continue the stream.

@@ -25,6 +25,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "common.cuh"
 #include "runtime.cuh"
@@ -435,6 +436,179 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tma_kernel(const __grid_const
   }
 }
 
+// Persistent variant for plain layouts: one CTA per SM walks the output tiles
+// t = blockIdx.x, blockIdx.x + gridDim.x, ... (tile t = row block t / ntn, column block
+// t % ntn, so neighbouring CTAs share their A rows in L2).  Six warps: warp 0 (one thread)
+// issues the TMA loads into a kPStages-deep ring, warp 1 (one thread) the tcgen05.mma into
+// one of two 128-column accumulators in tensor memory, and warps 2..5 read an accumulator
+// back (warp w reads TMEM lanes 32 (w % 4) .. +31) and store it while the MMAs of the next
+// tile run into the other one.  The ring and the accumulators are handed over by mbarriers:
+// full / empty per stage, acc_full (MMA commit) and acc_empty (the four epilogue warps)
+// per accumulator.  The loads of the next tile start while the last tile's epilogue runs,
+// so tensor-memory allocation, barrier set-up and pipeline fill are paid once per CTA.
+// Every wait is bounded; after one gives up the CTA stops issuing, waits (bounded) for the
+// loads and MMAs it issued, and writes NaN to the tiles it had not finished.
+constexpr int kPStages = 4;
+constexpr int kPThreads = 192;
+constexpr uint32_t kPTmemCols = 256;
+
+__global__ void __launch_bounds__(kPThreads, 1) gemm_tma_persistent(const __grid_constant__ CUtensorMap mapA,
+                                                                    const __grid_constant__ CUtensorMap mapB,
+                                                                    GemmArgs g, int ntn, int ntiles) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full[kPStages], empty[kPStages], accf[2], acce[2], done;
+  __shared__ uint32_t tmem_base_s;
+  __shared__ volatile int fail;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nk = (g.K + TBK - 1) / TBK;
+  const uint32_t sbase = (smem_u32(smem_raw) + 1023u) & ~1023u;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                 "r"(kPTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int i = 0; i < kPStages; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[i])));
+    }
+    for (int i = 0; i < 2; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&accf[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(smem_u32(&acce[i])));
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done)));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    fail = 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_base_s;
+
+  if (warp == 0) {
+    if (lane == 0 && nk > 0) {
+      // producer: global step it -> stage it % S, phase it / S of full[] and empty[]
+      int it = 0;
+      for (int t = blockIdx.x; t < ntiles && !fail; t += gridDim.x) {
+        const int m0 = (t / ntn) * TBM, n0 = (t % ntn) * TBN;
+        for (int kt = 0; kt < nk; ++kt, ++it) {
+          const int st = it % kPStages, round = it / kPStages;
+          if (it >= kPStages && !mbar_wait(smem_u32(&empty[st]), (round - 1) & 1)) {
+            fail = 1;
+            break;
+          }
+          if (fail) break;
+          const uint32_t fb = smem_u32(&full[st]);
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kStageBytes)
+                       : "memory");
+          const uint32_t a_dst = sbase + st * kStageBytes;
+          tma_load_2d(a_dst, &mapA, kt * TBK, m0, fb);
+          tma_load_2d(a_dst + kTileBytes, &mapB, kt * TBK, n0, fb);
+        }
+      }
+      // the last load into each stage has landed before the CTA moves on
+      for (int q = (it > kPStages ? it - kPStages : 0); q < it; ++q)
+        if (!mbar_wait(smem_u32(&full[q % kPStages]), (q / kPStages) & 1)) fail = 1;
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && nk > 0) {
+      const uint32_t idesc = umma_idesc();
+      int it = 0, lt = 0;
+      for (int t = blockIdx.x; t < ntiles && !fail; t += gridDim.x, ++lt) {
+        const int buf = lt & 1, use = lt >> 1;
+        if (lt >= 2 && !mbar_wait(smem_u32(&acce[buf]), (use - 1) & 1)) {
+          fail = 1;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t acc_addr = tmem + (uint32_t)(buf * TBN);
+        bool stop = false;
+        for (int kt = 0; kt < nk; ++kt, ++it) {
+          const int st = it % kPStages;
+          if (!mbar_wait(smem_u32(&full[st]), (it / kPStages) & 1)) {
+            fail = 1;
+            stop = true;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t a0 = sbase + st * kStageBytes, b0 = a0 + kTileBytes;
+#pragma unroll
+          for (int kk = 0; kk < TBK / 16; ++kk) {
+            const uint64_t ad = umma_desc_sw128(a0 + kk * 32), bd = umma_desc_sw128(b0 + kk * 32);
+            const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
+            asm volatile(
+                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc_addr),
+                "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+          }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                           smem_u32(&empty[st]))
+                       : "memory");
+        }
+        if (stop) break;
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_u32(&accf[buf]))
+                     : "memory");
+      }
+      // every MMA issued has completed before tensor memory is released
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&done))
+                   : "memory");
+      if (!mbar_wait(smem_u32(&done), 0)) fail = 1;
+    }
+  } else {
+    // epilogue warps 2..5: warp w owns the accumulator rows 32 (w % 4) .. +31
+    const int quad = warp & 3;
+    const bool vec = (g.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(g.C) & 15) == 0 &&
+                     (reinterpret_cast<uintptr_t>(g.Cpre) & 15) == 0 &&
+                     (reinterpret_cast<uintptr_t>(g.Cb) & 7) == 0;
+    int lt = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
+      const int m0 = (t / ntn) * TBM, n0 = (t % ntn) * TBN;
+      const int buf = lt & 1, use = lt >> 1;
+      bool ok = nk > 0 && !fail;
+      if (ok && !mbar_wait(smem_u32(&accf[buf]), use & 1)) {
+        fail = 1;
+        ok = false;
+      }
+      ok = __all_sync(0xffffffffu, ok);
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const int row = m0 + quad * 32 + lane;
+      const uint32_t taddr = tmem + (uint32_t)(buf * TBN) + ((uint32_t)(quad * 32) << 16);
+#pragma unroll 1
+      for (int c0 = 0; c0 < TBN; c0 += 32) {
+        uint32_t r[32];
+        if (ok) {
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+              "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+              : "r"(taddr + (uint32_t)c0));
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        } else {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) r[i] = 0u;
+        }
+        if (row < g.M) store_row32(g, r, row, n0 + c0, ok, vec);
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acce[buf])) : "memory");
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kPTmemCols));
+  }
+}
+
 // ---------------------------------------------------------------- elementwise kernels
 __global__ void k_gelu_backward(const float* __restrict__ dy, const float* __restrict__ pre, int64_t n,
                                 __nv_bfloat16* __restrict__ dxb, float* __restrict__ dx) {
@@ -610,6 +784,59 @@ static int make_tile_map(CUtensorMap* map, const void* base, int k, int rows, in
 
 static int grid1(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 65536)); }
 
+// The training loop calls the same few GEMM shapes on the same buffers every step: tensor
+// maps are kept in a small table keyed by (device, base, k, rows, ld) instead of encoded per
+// call, and each kernel's shared-memory limit is raised once per device.
+struct MapKey {
+  int dev;
+  const void* base;
+  int k, rows, ld;
+};
+struct MapEntry {
+  MapKey key;
+  CUtensorMap map;
+};
+static MapEntry g_maps[64];
+static int g_nmaps = 0, g_next_map = 0;
+static std::mutex g_maps_mu;
+
+static int cached_tile_map(CUtensorMap* map, const void* base, int k, int rows, int ld) {
+  int dev = 0;
+  PCVL_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(g_maps_mu);
+  for (int i = 0; i < g_nmaps; ++i) {
+    const MapKey& q = g_maps[i].key;
+    if (q.dev == dev && q.base == base && q.k == k && q.rows == rows && q.ld == ld) {
+      *map = g_maps[i].map;
+      return PCVL_OK;
+    }
+  }
+  PCVL_TRY(make_tile_map(map, base, k, rows, ld));
+  MapEntry& e = g_maps[g_next_map];
+  e.key = {dev, base, k, rows, ld};
+  e.map = *map;
+  g_next_map = (g_next_map + 1) % 64;
+  g_nmaps = std::min(g_nmaps + 1, 64);
+  return PCVL_OK;
+}
+
+static int allow_smem(const void* func, int bytes) {
+  static std::mutex mu;
+  static const void* done_func[2][64] = {};
+  static int done_bytes[2][64] = {};
+  int dev = 0;
+  PCVL_CUDA(cudaGetDevice(&dev));
+  PCVL_CHECK(dev >= 0 && dev < 64, "device index %d out of range", dev);
+  std::lock_guard<std::mutex> lock(mu);
+  for (int i = 0; i < 2; ++i)
+    if (done_func[i][dev] == func && done_bytes[i][dev] >= bytes) return PCVL_OK;
+  PCVL_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  const int slot = done_func[0][dev] == nullptr || done_func[0][dev] == func ? 0 : 1;
+  done_func[slot][dev] = func;
+  done_bytes[slot][dev] = bytes;
+  return PCVL_OK;
+}
+
 }  // namespace pcvl
 
 using namespace pcvl;
@@ -633,14 +860,17 @@ extern "C" int pcvl_gemm_bf16(const void* A, const void* B, int32_t M, int32_t N
                    (reinterpret_cast<uintptr_t>(A) & 15) == 0 && (reinterpret_cast<uintptr_t>(B) & 15) == 0;
   if (tma) {
     CUtensorMap mapA, mapB;
-    PCVL_TRY(make_tile_map(&mapA, A, K, M, lda));
-    PCVL_TRY(make_tile_map(&mapB, B, K, N, ldb));
-    const int smem = kTmaStages * (int)kStageBytes + 1024;
-    PCVL_CUDA(cudaFuncSetAttribute(gemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    gemm_tma_kernel<<<grid, kTcThreads, smem, (cudaStream_t)stream>>>(mapA, mapB, g);
+    PCVL_TRY(cached_tile_map(&mapA, A, K, M, lda));
+    PCVL_TRY(cached_tile_map(&mapB, B, K, N, ldb));
+    // persistent: one CTA per SM over every tile of the output
+    const int ntiles = (int)grid.x * (int)grid.y;
+    const int ctas = std::min(ntiles, num_sms());
+    const int smem = kPStages * (int)kStageBytes + 1024;
+    PCVL_TRY(allow_smem(reinterpret_cast<const void*>(gemm_tma_persistent), smem));
+    gemm_tma_persistent<<<ctas, kPThreads, smem, (cudaStream_t)stream>>>(mapA, mapB, g, (int)grid.x, ntiles);
   } else {
     const int smem = kStages * 2 * (int)kTileBytes;
-    PCVL_CUDA(cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    PCVL_TRY(allow_smem(reinterpret_cast<const void*>(gemm_tc_kernel), smem));
     gemm_tc_kernel<<<grid, kTcThreads, smem, (cudaStream_t)stream>>>(g);
   }
   PCVL_CUDA(cudaGetLastError());

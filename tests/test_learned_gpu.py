@@ -21,7 +21,10 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("M,N,K,ta,tb,epi", [(200, 96, 64, 0, 0, 0), (130, 257, 100, 0, 0, 2), (64, 128, 300, 0, 1, 0),
                                              (96, 72, 333, 1, 1, 0), (1, 900, 512, 0, 0, 1),
-                                             (512, 384, 1024, 0, 0, 0), (300, 200, 136, 0, 0, 2)])
+                                             (512, 384, 1024, 0, 0, 0), (300, 200, 136, 0, 0, 2),
+                                             # more tiles than SMs: every persistent CTA walks several
+                                             # tiles through both accumulators and wraps the load ring
+                                             (7680, 900, 512, 0, 0, 2), (4096, 1024, 1024, 0, 0, 0)])
 def test_gemm_bf16(native, M, N, K, ta, tb, epi):
     g = torch.Generator().manual_seed(M + N + K)
     A = torch.randn(K, M, generator=g) if ta else torch.randn(M, K, generator=g)
