@@ -50,6 +50,7 @@
 #include <algorithm>
 #include <cstring>
 #include <new>
+#include <type_traits>
 #include <vector>
 
 #include "arith.cuh"
@@ -245,8 +246,50 @@ __device__ __forceinline__ typename P::V fwd_value(const SlosArgs& a, const Desc
   return P::finish(acc);
 }
 
+// Two consecutive states of one tile for circuit b: the same sums as fwd_value, in the same
+// order for each state, as two independent chains (FP64: a complex multiply-add is four
+// dependent DFMA per component pair, so one chain per lane leaves the FP64 pipe idle).
+template <int MMAX, class P>
+__device__ __forceinline__ void fwd_value2(const SlosArgs& a, const Desc<MMAX, typename P::F>& d, int r,
+                                           uint32_t tau, bool two, const typename P::V* __restrict__ x,
+                                           const typename P::V* u, int b, typename P::V& v0, typename P::V& v1) {
+  using V = typename P::V;
+  const int p = a.p;
+  typename P::Acc acc0 = P::acc_zero(), acc1 = P::acc_zero();
+#pragma unroll
+  for (int j = 0; j < MMAX; ++j) {
+    if (j < p && ((d.mask >> j) & 1u)) {
+      const uint32_t ad = d.base[j] + tau;
+      const V uj = u[j * 32];
+      P::fma(acc0, P::ld(&x[(size_t)ad * a.B + b]), uj);
+      if (two) P::fma(acc1, P::ld(&x[(size_t)(ad + 1) * a.B + b]), uj);
+    }
+  }
+  if (r > 0) {
+    const uint32_t* row0 = a.tail + a.tail_off[r] + (size_t)tau * a.t;
+    uint32_t occ0 = __ldg(&a.tocc[a.tstate_off[r] + tau]);
+    uint32_t occ1 = two ? __ldg(&a.tocc[a.tstate_off[r] + tau + 1]) : 0u;
+    const uint32_t* row1 = row0 + a.t;
+    while (occ0 | occ1) {
+      if (occ0) {
+        const int jl = __ffs(occ0) - 1;
+        occ0 &= occ0 - 1;
+        P::fma(acc0, P::ld(&x[(size_t)(d.tb + __ldg(&row0[jl])) * a.B + b]), u[(p + jl) * 32]);
+      }
+      if (occ1) {
+        const int jl = __ffs(occ1) - 1;
+        occ1 &= occ1 - 1;
+        P::fma(acc1, P::ld(&x[(size_t)(d.tb + __ldg(&row1[jl])) * a.B + b]), u[(p + jl) * 32]);
+      }
+    }
+  }
+  v0 = P::finish(acc0);
+  v1 = P::finish(acc1);
+}
+
 // Batched forward layer: a warp takes a unit (one tile, up to kChunkB states) and its
-// lanes 32 circuits; the parent offsets are warp-uniform, the loads coalesced.
+// lanes 32 circuits; the parent offsets are warp-uniform, the loads coalesced.  In FP64
+// a lane carries two states at a time (fwd_value2).
 template <int MMAX, class P>
 __global__ void __launch_bounds__(256, 4) slos_fwdb(SlosArgs a) {
   using V = typename P::V;
@@ -267,9 +310,20 @@ __global__ void __launch_bounds__(256, 4) slos_fwdb(SlosArgs a) {
     Desc<MMAX, typename P::F> d;
     describe<MMAX, false, false, P>(pi, a.k - r, r, a, cn, d, P::f_from(0.0), d.base);
     const uint32_t t0 = ch * a.chunkB, t1 = min(S, t0 + a.chunkB);
-    if (b < a.B)
-      for (uint32_t tau = t0; tau < t1; ++tau)
-        xout[(size_t)(d.A + tau) * a.B + b] = fwd_value<MMAX, P>(a, d, r, tau, xin, u, 32, b);
+    if (b < a.B) {
+      if constexpr (std::is_same<P, Arith64>::value) {
+        for (uint32_t tau = t0; tau < t1; tau += 2) {
+          const bool two = tau + 1 < t1;
+          V v0, v1;
+          fwd_value2<MMAX, P>(a, d, r, tau, two, xin, u, b, v0, v1);
+          xout[(size_t)(d.A + tau) * a.B + b] = v0;
+          if (two) xout[(size_t)(d.A + tau + 1) * a.B + b] = v1;
+        }
+      } else {
+        for (uint32_t tau = t0; tau < t1; ++tau)
+          xout[(size_t)(d.A + tau) * a.B + b] = fwd_value<MMAX, P>(a, d, r, tau, xin, u, 32, b);
+      }
+    }
   }
 }
 
