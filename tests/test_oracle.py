@@ -197,3 +197,24 @@ def test_mlp_reference_gradient_finite_differences():
             assert (lp - lm) / (2 * h) == pytest.approx(g["W"][i][1, 2], rel=1e-5, abs=1e-8)
     finally:
         mlp_ref.bf16 = saved
+
+
+def test_host_tuned_paths_equal_the_restatements(oracle):
+    """The CPU baseline's batched Glynn and parallel sampler compute what the plain
+    restatements compute: permanents to 1e-12 relative, samples one for one."""
+    from perceval_gb300.utils.matrix import random_unitary
+    U = random_unitary(64, seed=3)
+    rng = np.random.default_rng(3)
+    mats = [np.zeros((0, 0), complex)] + [np.ascontiguousarray(U[np.ix_(rng.choice(64, n, False),
+                                                                          rng.choice(64, n, False))])
+                                          for n in (1, 2, 3, 7, 12, 14)]
+    sizes = np.array([a.shape[0] for a in mats], dtype=np.int32)
+    offs = np.concatenate([[0], np.cumsum([a.size for a in mats])[:-1]]).astype(np.int64)
+    flat = np.concatenate([a.reshape(-1) for a in mats] + [np.zeros(1, complex)])
+    ref = oracle.perm_batch(flat, offs, sizes)
+    got = oracle.perm_batch_fast(flat, offs, sizes)
+    assert got[0] == 1
+    assert np.max(np.abs(got[1:] - ref[1:]) / np.abs(ref[1:])) < 1e-12
+    V = random_unitary(12, seed=4)
+    inp = [1, 0, 1, 1, 0, 0, 1, 0, 1, 0, 0, 0]
+    assert np.array_equal(oracle.cc2017_fast(V, inp, 300, seed=5, first=7), oracle.cc2017(V, inp, 300, seed=5, first=7))
