@@ -22,9 +22,12 @@ from ._abstract_backends import ASamplingBackend
 class Clifford2017Backend(ASamplingBackend):
     def __init__(self, precision: str = "double"):
         super().__init__()
-        if precision not in ("double", "single"):
-            raise ValueError("precision must be 'double' (float-float) or 'single' (FP32)")
-        self._precision = 0 if precision == "double" else 1
+        names = {"double": _native.PREC_FLOAT_FLOAT, "float-float": _native.PREC_FLOAT_FLOAT,
+                 "fp64": _native.PREC_FP64, "single": _native.PREC_FP32, "fp32": _native.PREC_FP32}
+        if precision not in names:
+            raise ValueError("precision must be 'double' / 'float-float' (FP64-class pairs, the default), "
+                             "'fp64' (native FP64) or 'single' / 'fp32'")
+        self._precision = names[precision]
         self._u_dev = None
 
     @property

@@ -136,6 +136,37 @@ struct ArF32 {  // FP32 with Kahan-compensated accumulation
   }
 };
 
+struct Ar64 {  // native FP64: row sums, products and the sums of the sign patterns
+  using C = double2;
+  struct Acc {
+    double r, i;
+  };
+  static __device__ __forceinline__ C zero() { return make_double2(0.0, 0.0); }
+  static __device__ __forceinline__ C one() { return make_double2(1.0, 0.0); }
+  static __device__ __forceinline__ C add(C a, C b) { return make_double2(a.x + b.x, a.y + b.y); }
+  static __device__ __forceinline__ C add_n(C a, C b) { return add(a, b); }
+  static __device__ __forceinline__ C sub_n(C a, C b) { return make_double2(a.x - b.x, a.y - b.y); }
+  static __device__ __forceinline__ C mul(C a, C b) {
+    return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+  }
+  static __device__ __forceinline__ C neg(C a) { return make_double2(-a.x, -a.y); }
+  static __device__ __forceinline__ C twice(C a) { return make_double2(2.0 * a.x, 2.0 * a.y); }
+  static __device__ __forceinline__ C from(double2 v) { return v; }
+  static __device__ __forceinline__ C scale(C a, int e) { return make_double2(ldexp(a.x, e), ldexp(a.y, e)); }
+  static __device__ __forceinline__ float mag(C a) { return (float)(fabs(a.x) + fabs(a.y)); }
+  static __device__ __forceinline__ double shd(double v, int mask) { return __shfl_xor_sync(0xffffffffu, v, mask); }
+  static __device__ __forceinline__ C shfl(C v, int mask) { return make_double2(shd(v.x, mask), shd(v.y, mask)); }
+  static __device__ __forceinline__ Acc acc_zero() { return {0.0, 0.0}; }
+  static __device__ __forceinline__ void acc_add(Acc& a, C x) {
+    a.r += x.x;
+    a.i += x.y;
+  }
+  static __device__ __forceinline__ void acc_fold(Acc&) {}
+  static __device__ __forceinline__ Acc acc_merge(Acc a, Acc b) { return {a.r + b.r, a.i + b.i}; }
+  static __device__ __forceinline__ Acc acc_shfl(Acc v, int mask) { return {shd(v.r, mask), shd(v.i, mask)}; }
+  static __device__ __forceinline__ double2 acc_value(Acc a) { return make_double2(a.r, a.i); }
+};
+
 constexpr int kCCThreads = 128;
 constexpr int kMaxPhotons = 32;
 
@@ -534,7 +565,9 @@ static int cc2017_run(const double* u_d, int32_t m, int32_t nstates, const int32
   PCVL_CHECK(u_d && input_states_h && counts_h && out_counts_d, "null pointer argument");
   PCVL_CHECK(m >= 1 && m <= 2048, "m=%d outside [1, 2048]", m);
   PCVL_CHECK(nstates >= 1 && nstates <= (1 << 20), "nstates=%d outside [1, 2^20]", nstates);
-  PCVL_CHECK(precision == 0 || precision == 1, "precision must be 0 (float-float) or 1 (FP32)");
+  PCVL_CHECK(precision == kPrecFloatFloat || precision == kPrecFP32 || precision == kPrecFP64,
+             "precision must be %d (float-float), %d (FP32) or %d (FP64), got %d", (int)kPrecFloatFloat,
+             (int)kPrecFP32, (int)kPrecFP64, precision);
   std::vector<int32_t> cols((size_t)nstates * kMaxPhotons, 0);
   std::vector<int64_t> state_off(nstates + 1, 0);
   int n = -1;
@@ -570,7 +603,8 @@ static int cc2017_run(const double* u_d, int32_t m, int32_t nstates, const int32
   const int64_t last = count - (waves - 1) * W;
   for (int k = 2; k <= n; ++k) max_chunks = std::max(max_chunks, plan_step(k, last, target_ctas).chunks);
 
-  const size_t csz = precision == 0 ? sizeof(cdd) : sizeof(float2);
+  const size_t csz = precision == kPrecFloatFloat ? sizeof(cdd) : precision == kPrecFP64 ? sizeof(double2)
+                                                                                          : sizeof(float2);
   const size_t o_cols0 = align_up((size_t)m * m * csz, 256);
   const size_t o_soff = o_cols0 + align_up(cols.size() * sizeof(int32_t), 256);
   const size_t o_cols = o_soff + align_up(state_off.size() * sizeof(int64_t), 256);
@@ -591,8 +625,10 @@ static int cc2017_run(const double* u_d, int32_t m, int32_t nstates, const int32
     PCVL_TRY(stage_h2d(up.data(), up.size(), base + o_cols0, s));
   }
   const int cgrid = std::max(1, std::min(1024, (m * m + 255) / 256));
-  if (precision == 0)
+  if (precision == kPrecFloatFloat)
     cc_convert<ArDD><<<cgrid, 256, 0, s>>>((const double2*)u_d, m, (cdd*)base);
+  else if (precision == kPrecFP64)
+    cc_convert<Ar64><<<cgrid, 256, 0, s>>>((const double2*)u_d, m, (double2*)base);
   else
     cc_convert<ArF32><<<cgrid, 256, 0, s>>>((const double2*)u_d, m, (float2*)base);
   PCVL_CUDA(cudaGetLastError());
@@ -636,7 +672,9 @@ static int cc2017_run(const double* u_d, int32_t m, int32_t nstates, const int32
         sa.L = p.L;
         sa.Hb = p.Hb;
         sa.chunks = p.chunks;
-        const int rc = precision == 0 ? sub_dispatch<ArDD>(p, sa, s) : sub_dispatch<ArF32>(p, sa, s);
+        const int rc = precision == kPrecFloatFloat ? sub_dispatch<ArDD>(p, sa, s)
+                       : precision == kPrecFP64     ? sub_dispatch<Ar64>(p, sa, s)
+                                                    : sub_dispatch<ArF32>(p, sa, s);
         if (rc != 0) {
           set_error("CC2017 sub-permanent launch failed: %s", cudaGetErrorString((cudaError_t)rc));
           return PCVL_ERR_CUDA;
