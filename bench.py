@@ -614,9 +614,10 @@ def secondary(torch, _native, random_unitary, dev, flush, fp64_peak_tflops):
                                       "samples_per_s": 64000 / (t_many * 1e-3)}
     # the learned-proposal sampler, bounded for the default run: n = 30, m = 900 trained on
     # 1024 exact samples (FP32 sampler), 8 chains x 8 steps of FP64-permanent acceptances
-    # against 96 exact float-float samples; and the n = 8, m = 64 companion
+    # against 96 exact float-float samples and 32 exact FP64 samples; and the n = 8, m = 64
+    # companion
     res["learned_mis_n30_m900"] = learned_case(torch, _native, random_unitary, 900, 30, 1024, 4, 8, 8, 96,
-                                               tvd=False)
+                                               tvd=False, n_ref64=32)
     res["learned_mis_n8_m64"] = learned_case(torch, _native, random_unitary, 64, 8, 20000, 10, 64, 200, 25600)
     # small case: SLOS m=12, n=6 and 1000 Naive amplitudes (latency-bound)
     from perceval_gb300 import BackendFactory, BasicState
@@ -765,7 +766,7 @@ def secondary(torch, _native, random_unitary, dev, flush, fp64_peak_tflops):
 
 
 def learned_case(torch, _native, random_unitary, m, n, n_train, epochs, chains, steps, n_ref, tvd=True,
-                 marginal_modes=8):
+                 marginal_modes=8, n_ref64=None):
     """Learned-proposal Metropolised sampler against the plain GPU exact sampler on one
     Haar unitary (seed 0, input photons in modes 0..n-1).
 
@@ -798,6 +799,11 @@ def learned_case(torch, _native, random_unitary, m, n, n_train, epochs, chains, 
     t0 = time.perf_counter()
     ref = _native.cc2017_sample(Ud, inp, n_ref, seed=202, precision=0).cpu().numpy()
     t_ref = time.perf_counter() - t0
+    # the same sampler with native FP64 sub-permanent sums, the acceptance's arithmetic
+    n_ref64 = n_ref if n_ref64 is None else n_ref64
+    t0 = time.perf_counter()
+    ref64 = _native.cc2017_sample(Ud, inp, n_ref64, seed=303, precision=2).cpu().numpy()
+    t_ref64 = time.perf_counter() - t0
     A, E2 = exact_moments(U, inp)
     st = res.samples.reshape(-1, m)
     modes = [int(i) for i in np.argsort(-A)[:marginal_modes]]
@@ -823,8 +829,13 @@ def learned_case(torch, _native, random_unitary, m, n, n_train, epochs, chains, 
                              "arithmetic": "float-float",
                              "max_abs_err_E_n": float(np.abs(ref.astype(float).mean(0) - A).max()),
                              "marginals": marg_err(ref)},
+           "exact_sampler_fp64": {"samples": n_ref64, "seconds": t_ref64, "ess_per_s": n_ref64 / t_ref64,
+                                  "arithmetic": "fp64",
+                                  "max_abs_err_E_n": float(np.abs(ref64.astype(float).mean(0) - A).max()),
+                                  "marginals": marg_err(ref64)},
            "marginal_modes": modes, "marginal_pairs": [list(p) for p in pairs]}
     row["ess_per_s_ratio"] = row["mis"]["ess_per_s"] / row["exact_sampler"]["ess_per_s"]
+    row["ess_per_s_ratio_vs_fp64_exact"] = row["mis"]["ess_per_s"] / row["exact_sampler_fp64"]["ess_per_s"]
     if tvd:
         # TVD(q, pi) on photon sequences from the exact samples: trained vs untrained network
         untrained = ProposalMLP(m, n, D=128, H=512, layers=3, seed=0)
@@ -871,7 +882,34 @@ def run_learned(args):
             e0.synchronize()
             best = min(best, s0.elapsed_time(e0))
         tf = 2.0 * M * N * K / (best * 1e-3) / 1e12
-        gemm[f"{M}x{N}x{K}"] = {"ms": best, "tflops": tf, "frac_of_bf16_peak": tf / peak}
+        row = {"ms": best, "tflops": tf, "frac_of_bf16_peak": tf / peak,
+               "timing": "one call between two events (includes the host's launch latency)"}
+        # 20 back-to-back calls captured in one CUDA graph: the device time per call
+        reps = 20 if M * N * K < 1 << 33 else 4
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(side):
+            f()
+            with torch.cuda.graph(graph, stream=side):
+                for _ in range(reps):
+                    f()
+        torch.cuda.current_stream().wait_stream(side)
+        graph.replay()
+        torch.cuda.synchronize()
+        gbest = float("inf")
+        for _ in range(5):
+            s0, e0 = torch.cuda.Event(True), torch.cuda.Event(True)
+            s0.record()
+            graph.replay()
+            e0.record()
+            e0.synchronize()
+            gbest = min(gbest, s0.elapsed_time(e0) / reps)
+        gtf = 2.0 * M * N * K / (gbest * 1e-3) / 1e12
+        row.update({"graph_ms_per_call": gbest, "graph_tflops": gtf, "graph_frac_of_bf16_peak": gtf / peak,
+                    "graph_calls": reps})
+        del graph
+        gemm[f"{M}x{N}x{K}"] = row
     print(json.dumps({"learned_proposal": out, "mlp_gemm": gemm, "bf16_peak_tflops": peak}), flush=True)
 
 

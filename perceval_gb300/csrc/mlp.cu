@@ -295,20 +295,35 @@ __global__ void __launch_bounds__(kTcThreads) gemm_tc_kernel(GemmArgs g) {
   }
 }
 
-// ---------------------------------------------------------------- TMA-fed variant
-// For A and B in the plain layout (k contiguous, 16-byte aligned rows) the tiles come by
-// TMA (cp.async.bulk.tensor, 128-byte swizzle) into a ring of kTmaStages stages; one
-// thread issues the loads (mbarrier transaction counts), one thread issues the MMAs and
-// releases each stage through tcgen05.commit, and all four warps run the epilogue.  The
-// shared-memory descriptors use the 128-byte swizzled K-major layout (8 rows x 128 B per
-// swizzle atom, 1024 B between 8-row groups); a K slice of 16 elements is 32 B further.
-constexpr int kTmaStages = 3;
+// ---------------------------------------------------------------- TMA-fed kernel
+// Operands whose rows start on 16-byte boundaries come by TMA (cp.async.bulk.tensor,
+// 128-byte swizzle).  A K-major operand tile (k contiguous) uses the 128-byte swizzled
+// K-major layout (8 rows x 128 B per swizzle atom, 1024 B between 8-row groups); a K slice
+// of 16 elements is 32 B further.
 constexpr uint32_t kStageBytes = 2 * kTileBytes;  // A and B tiles of one stage
 
 __device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr) {
   const uint64_t lbo = 16, sbo = 1024;
   return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((lbo >> 4) << 16) | ((sbo >> 4) << 32) | (1ull << 46) |
          (2ull << 61);
+}
+
+// MN-major operand (a transposed A or B: the tile's 128 rows contiguous in memory): two TMA
+// boxes of 64 rows (128 B) x 64 k, the second 8 KB after the first.  In the 128-byte swizzled
+// MN-major layout a swizzle atom is 64 rows x 8 k (8 lines of 128 B, one line per k); atoms
+// adjacent in the row direction are LBO = 8 KB apart (the two boxes), atoms adjacent in k
+// SBO = 1024 B apart, so a K slice of 16 elements starts 2048 B further.
+constexpr uint32_t kMnBoxBytes = 64 * TBK * 2;  // one 64-row x 64-k box, 8 KB
+
+__device__ __forceinline__ uint64_t umma_desc_sw128_mn(uint32_t saddr) {
+  const uint64_t lbo = kMnBoxBytes, sbo = 1024;
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((lbo >> 4) << 16) | ((sbo >> 4) << 32) | (1ull << 46) |
+         (2ull << 61);
+}
+
+// instruction descriptor with the operands' major-ness (bit 15: A MN-major, bit 16: B)
+__device__ __forceinline__ uint32_t umma_idesc_t(bool ta, bool tb) {
+  return umma_idesc() | ((ta ? 1u : 0u) << 15) | ((tb ? 1u : 0u) << 16);
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t mbar) {
@@ -319,142 +334,30 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
-__global__ void __launch_bounds__(kTcThreads) gemm_tma_kernel(const __grid_constant__ CUtensorMap mapA,
-                                                              const __grid_constant__ CUtensorMap mapB, GemmArgs g) {
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t full[kTmaStages], empty[kTmaStages], done;
-  __shared__ uint32_t tmem_base_s;
-  __shared__ int fail;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int m0 = blockIdx.y * TBM, n0 = blockIdx.x * TBN;
-  const int nk = (g.K + TBK - 1) / TBK;
-  // stages start on a 1024-byte boundary (the swizzle atom)
-  const uint32_t sbase = (smem_u32(smem_raw) + 1023u) & ~1023u;
-
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
-                 "r"(kTmemCols));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  if (tid == 0) {
-    for (int i = 0; i < kTmaStages; ++i) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[i])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[i])));
-    }
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done)));
-    asm volatile("fence.mbarrier_init.release.cluster;");
-    fail = 0;
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;");
-  const uint32_t tmem = tmem_base_s;
-
-  if (warp == 0 && lane == 0 && nk > 0) {
-    // producer: step kt -> stage kt % S, phase kt / S of full[] and empty[]
-    int issued = 0;
-    for (int kt = 0; kt < nk; ++kt) {
-      const int st = kt % kTmaStages, round = kt / kTmaStages;
-      if (kt >= kTmaStages && !mbar_wait(smem_u32(&empty[st]), (round - 1) & 1)) {
-        fail = 1;
-        break;
-      }
-      const uint32_t fb = smem_u32(&full[st]);
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kStageBytes) : "memory");
-      const uint32_t a_dst = sbase + st * kStageBytes;
-      tma_load_2d(a_dst, &mapA, kt * TBK, m0, fb);
-      tma_load_2d(a_dst + kTileBytes, &mapB, kt * TBK, n0, fb);
-      issued = kt + 1;
-    }
-    // every load issued has landed before the CTA moves on
-    for (int kt = (issued > kTmaStages ? issued - kTmaStages : 0); kt < issued; ++kt)
-      if (!mbar_wait(smem_u32(&full[kt % kTmaStages]), (kt / kTmaStages) & 1)) fail = 1;
-  } else if (warp == 1 && lane == 0 && nk > 0) {
-    // MMA issuer
-    const uint32_t idesc = umma_idesc();
-    for (int kt = 0; kt < nk; ++kt) {
-      const int st = kt % kTmaStages;
-      if (!mbar_wait(smem_u32(&full[st]), (kt / kTmaStages) & 1)) {
-        fail = 1;
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t a0 = sbase + st * kStageBytes, b0 = a0 + kTileBytes;
-#pragma unroll
-      for (int kk = 0; kk < TBK / 16; ++kk) {
-        const uint64_t ad = umma_desc_sw128(a0 + kk * 32), bd = umma_desc_sw128(b0 + kk * 32);
-        const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
-        asm volatile(
-            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-      }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       smem_u32(&empty[st]))
-                   : "memory");
-    }
-    // completion of every MMA issued (a commit covers all earlier ones of this thread)
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                     smem_u32(&done))
-                 : "memory");
-  }
-  __syncwarp();
-  bool ok = true;
-  if (nk > 0) ok = mbar_wait(smem_u32(&done), 0);
-  __syncthreads();
-  ok = __syncthreads_and(ok && fail == 0);
-  asm volatile("tcgen05.fence::after_thread_sync;");
-
-  const int row = m0 + warp * 32 + lane;
-  const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-  const bool vec = (g.ldc & 3) == 0 && (reinterpret_cast<uintptr_t>(g.C) & 15) == 0 &&
-                   (reinterpret_cast<uintptr_t>(g.Cpre) & 15) == 0 && (reinterpret_cast<uintptr_t>(g.Cb) & 7) == 0;
-#pragma unroll 1
-  for (int c0 = 0; c0 < TBN; c0 += 32) {
-    uint32_t r[32];
-    if (nk > 0 && ok) {
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-          "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-          : "r"(taddr + (uint32_t)c0));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-    } else {
-#pragma unroll
-      for (int i = 0; i < 32; ++i) r[i] = 0u;
-    }
-    if (row < g.M) store_row32(g, r, row, n0 + c0, ok, vec);
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;");
-  __syncthreads();
-  if (warp == 0) {
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
-  }
-}
-
-// Persistent variant for plain layouts: one CTA per SM walks the output tiles
-// t = blockIdx.x, blockIdx.x + gridDim.x, ... (tile t = row block t / ntn, column block
-// t % ntn, so neighbouring CTAs share their A rows in L2).  Six warps: warp 0 (one thread)
+// Persistent kernel: two CTAs per SM walk the output tiles t = blockIdx.x,
+// blockIdx.x + gridDim.x, ... (tile t = row block t / ntn, column block t % ntn, so
+// neighbouring CTAs share their A rows in L2).  Six warps per CTA: warp 0 (one thread)
 // issues the TMA loads into a kPStages-deep ring, warp 1 (one thread) the tcgen05.mma into
 // one of two 128-column accumulators in tensor memory, and warps 2..5 read an accumulator
-// back (warp w reads TMEM lanes 32 (w % 4) .. +31) and store it while the MMAs of the next
-// tile run into the other one.  The ring and the accumulators are handed over by mbarriers:
-// full / empty per stage, acc_full (MMA commit) and acc_empty (the four epilogue warps)
-// per accumulator.  The loads of the next tile start while the last tile's epilogue runs,
-// so tensor-memory allocation, barrier set-up and pipeline fill are paid once per CTA.
-// Every wait is bounded; after one gives up the CTA stops issuing, waits (bounded) for the
-// loads and MMAs it issued, and writes NaN to the tiles it had not finished.
-constexpr int kPStages = 4;
+// back (warp w reads TMEM lanes 32 (w % 4) .. +31), release it, and store it while the MMAs
+// of the next tile run into the other one.  The ring and the accumulators are handed over
+// by mbarriers: full / empty per stage, acc_full (MMA commit) and acc_empty (the four
+// epilogue warps) per accumulator.  Transposed operands (TA / TB) arrive MN-major.
+// Measured on GB300 (CUDA-graph replay of back-to-back calls): two CTAs of 3 stages per SM
+// beat one CTA of 4, 5 or 6 stages at every shape (8192^3: 1326 against 1036 TFLOP/s), and
+// staging the outputs in shared memory for TMA stores was slower than the warps' own
+// 16-byte stores.  Every wait is bounded; after one gives up the CTA stops issuing, waits
+// (bounded) for the loads and MMAs it issued, and writes NaN to the tiles it had not finished.
+constexpr int kPStages = 3;    // 96 KB of operand stages per CTA
+constexpr int kPCtasPerSm = 2;  // two CTAs per SM: two load / MMA pipelines and 8 epilogue warps
+constexpr uint32_t kPSmemBytes = kPStages * kStageBytes + 1024;
 constexpr int kPThreads = 192;
 constexpr uint32_t kPTmemCols = 256;
 
-__global__ void __launch_bounds__(kPThreads, 1) gemm_tma_persistent(const __grid_constant__ CUtensorMap mapA,
-                                                                    const __grid_constant__ CUtensorMap mapB,
-                                                                    GemmArgs g, int ntn, int ntiles) {
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(kPThreads, kPCtasPerSm)
+    gemm_tma_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, GemmArgs g,
+                        int ntn, int ntiles) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t full[kPStages], empty[kPStages], accf[2], acce[2], done;
   __shared__ uint32_t tmem_base_s;
@@ -488,6 +391,8 @@ __global__ void __launch_bounds__(kPThreads, 1) gemm_tma_persistent(const __grid
 
   if (warp == 0) {
     if (lane == 0 && nk > 0) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA)) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapB)) : "memory");
       // producer: global step it -> stage it % S, phase it / S of full[] and empty[]
       int it = 0;
       for (int t = blockIdx.x; t < ntiles && !fail; t += gridDim.x) {
@@ -502,9 +407,19 @@ __global__ void __launch_bounds__(kPThreads, 1) gemm_tma_persistent(const __grid
           const uint32_t fb = smem_u32(&full[st]);
           asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kStageBytes)
                        : "memory");
-          const uint32_t a_dst = sbase + st * kStageBytes;
-          tma_load_2d(a_dst, &mapA, kt * TBK, m0, fb);
-          tma_load_2d(a_dst + kTileBytes, &mapB, kt * TBK, n0, fb);
+          const uint32_t a_dst = sbase + st * kStageBytes, b_dst = a_dst + kTileBytes;
+          if (TA) {
+            tma_load_2d(a_dst, &mapA, m0, kt * TBK, fb);
+            tma_load_2d(a_dst + kMnBoxBytes, &mapA, m0 + 64, kt * TBK, fb);
+          } else {
+            tma_load_2d(a_dst, &mapA, kt * TBK, m0, fb);
+          }
+          if (TB) {
+            tma_load_2d(b_dst, &mapB, n0, kt * TBK, fb);
+            tma_load_2d(b_dst + kMnBoxBytes, &mapB, n0 + 64, kt * TBK, fb);
+          } else {
+            tma_load_2d(b_dst, &mapB, kt * TBK, n0, fb);
+          }
         }
       }
       // the last load into each stage has landed before the CTA moves on
@@ -513,7 +428,7 @@ __global__ void __launch_bounds__(kPThreads, 1) gemm_tma_persistent(const __grid
     }
   } else if (warp == 1) {
     if (lane == 0 && nk > 0) {
-      const uint32_t idesc = umma_idesc();
+      const uint32_t idesc = umma_idesc_t(TA, TB);
       int it = 0, lt = 0;
       for (int t = blockIdx.x; t < ntiles && !fail; t += gridDim.x, ++lt) {
         const int buf = lt & 1, use = lt >> 1;
@@ -535,7 +450,8 @@ __global__ void __launch_bounds__(kPThreads, 1) gemm_tma_persistent(const __grid
           const uint32_t a0 = sbase + st * kStageBytes, b0 = a0 + kTileBytes;
 #pragma unroll
           for (int kk = 0; kk < TBK / 16; ++kk) {
-            const uint64_t ad = umma_desc_sw128(a0 + kk * 32), bd = umma_desc_sw128(b0 + kk * 32);
+            const uint64_t ad = TA ? umma_desc_sw128_mn(a0 + kk * 2048) : umma_desc_sw128(a0 + kk * 32);
+            const uint64_t bd = TB ? umma_desc_sw128_mn(b0 + kk * 2048) : umma_desc_sw128(b0 + kk * 32);
             const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
             asm volatile(
                 "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
@@ -594,11 +510,15 @@ __global__ void __launch_bounds__(kPThreads, 1) gemm_tma_persistent(const __grid
 #pragma unroll
           for (int i = 0; i < 32; ++i) r[i] = 0u;
         }
+        if (c0 + 32 >= TBN) {
+          // the accumulator is in registers: the MMAs of tile lt + 2 may start
+          asm volatile("tcgen05.fence::before_thread_sync;");
+          __syncwarp();
+          if (lane == 0)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acce[buf])) : "memory");
+        }
         if (row < g.M) store_row32(g, r, row, n0 + c0, ok, vec);
       }
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      __syncwarp();
-      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acce[buf])) : "memory");
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -762,7 +682,11 @@ __global__ void k_sample_step(const float* __restrict__ logits, int S, int N, in
 
 // Tensor map of a row-major bf16 matrix (rows x k, row stride ld elements) for 128-row x
 // 64-element boxes with the 128-byte swizzle; out-of-range elements read as zero.
-static int make_tile_map(CUtensorMap* map, const void* base, int k, int rows, int ld) {
+// Tensor map of one operand: K-major (rows x k, k contiguous; box 64 k x 128 rows) or, for a
+// transposed operand, MN-major (k x rows, rows contiguous; box 64 rows x 64 k).
+enum MapKind { kMapK = 0, kMapMN = 1 };
+
+static int make_tile_map(CUtensorMap* map, const void* base, int k, int rows, int ld, int kind) {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   if (!encode) {
     void* fn = nullptr;
@@ -771,9 +695,10 @@ static int make_tile_map(CUtensorMap* map, const void* base, int k, int rows, in
     PCVL_CHECK(e == cudaSuccess && q == cudaDriverEntryPointSuccess && fn, "cuTensorMapEncodeTiled is unavailable");
     encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   }
-  const cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+  const bool mn = kind == kMapMN;
+  const cuuint64_t dims[2] = {(cuuint64_t)(mn ? rows : k), (cuuint64_t)(mn ? k : rows)};
   const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-  const cuuint32_t box[2] = {(cuuint32_t)TBK, (cuuint32_t)TBM};
+  const cuuint32_t box[2] = {mn ? 64u : (cuuint32_t)TBK, mn ? (cuuint32_t)TBK : (cuuint32_t)TBM};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -790,7 +715,7 @@ static int grid1(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>
 struct MapKey {
   int dev;
   const void* base;
-  int k, rows, ld;
+  int k, rows, ld, kind;
 };
 struct MapEntry {
   MapKey key;
@@ -800,40 +725,51 @@ static MapEntry g_maps[64];
 static int g_nmaps = 0, g_next_map = 0;
 static std::mutex g_maps_mu;
 
-static int cached_tile_map(CUtensorMap* map, const void* base, int k, int rows, int ld) {
+static int cached_tile_map(CUtensorMap* map, const void* base, int k, int rows, int ld, int kind) {
   int dev = 0;
   PCVL_CUDA(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lock(g_maps_mu);
   for (int i = 0; i < g_nmaps; ++i) {
     const MapKey& q = g_maps[i].key;
-    if (q.dev == dev && q.base == base && q.k == k && q.rows == rows && q.ld == ld) {
+    if (q.dev == dev && q.base == base && q.k == k && q.rows == rows && q.ld == ld && q.kind == kind) {
       *map = g_maps[i].map;
       return PCVL_OK;
     }
   }
-  PCVL_TRY(make_tile_map(map, base, k, rows, ld));
+  PCVL_TRY(make_tile_map(map, base, k, rows, ld, kind));
   MapEntry& e = g_maps[g_next_map];
-  e.key = {dev, base, k, rows, ld};
+  e.key = {dev, base, k, rows, ld, kind};
   e.map = *map;
   g_next_map = (g_next_map + 1) % 64;
   g_nmaps = std::min(g_nmaps + 1, 64);
   return PCVL_OK;
 }
 
+// Raises a kernel's dynamic shared-memory limit once per (device, kernel): the GEMM has five
+// kernels (four operand layouts of the persistent one and the cp.async one).
 static int allow_smem(const void* func, int bytes) {
+  constexpr int kSlots = 8;
   static std::mutex mu;
-  static const void* done_func[2][64] = {};
-  static int done_bytes[2][64] = {};
+  static const void* done_func[64][kSlots] = {};
+  static int done_bytes[64][kSlots] = {};
   int dev = 0;
   PCVL_CUDA(cudaGetDevice(&dev));
   PCVL_CHECK(dev >= 0 && dev < 64, "device index %d out of range", dev);
   std::lock_guard<std::mutex> lock(mu);
-  for (int i = 0; i < 2; ++i)
-    if (done_func[i][dev] == func && done_bytes[i][dev] >= bytes) return PCVL_OK;
+  int slot = -1;
+  for (int i = 0; i < kSlots; ++i) {
+    if (done_func[dev][i] == func) {
+      if (done_bytes[dev][i] >= bytes) return PCVL_OK;
+      slot = i;
+      break;
+    }
+    if (slot < 0 && done_func[dev][i] == nullptr) slot = i;
+  }
   PCVL_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  const int slot = done_func[0][dev] == nullptr || done_func[0][dev] == func ? 0 : 1;
-  done_func[slot][dev] = func;
-  done_bytes[slot][dev] = bytes;
+  if (slot >= 0) {
+    done_func[dev][slot] = func;
+    done_bytes[dev][slot] = bytes;
+  }
   return PCVL_OK;
 }
 
@@ -855,19 +791,22 @@ extern "C" int pcvl_gemm_bf16(const void* A, const void* B, int32_t M, int32_t N
              bias, epilogue, C, (__nv_bfloat16*)Cb, Cpre};
   dim3 grid((N + TBN - 1) / TBN, (M + TBM - 1) / TBM);
   PCVL_CHECK(grid.y <= 65535, "M too large for one launch (%d)", M);
-  // plain layouts with 16-byte aligned rows: TMA-fed kernel; anything else: cp.async
-  const bool tma = !transA && !transB && K > 0 && (lda % 8) == 0 && (ldb % 8) == 0 &&
-                   (reinterpret_cast<uintptr_t>(A) & 15) == 0 && (reinterpret_cast<uintptr_t>(B) & 15) == 0;
+  // rows (of either layout) 16-byte aligned: TMA-fed persistent kernel; anything else: cp.async
+  const bool tma = K > 0 && (lda % 8) == 0 && (ldb % 8) == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0 &&
+                   (reinterpret_cast<uintptr_t>(B) & 15) == 0;
   if (tma) {
     CUtensorMap mapA, mapB;
-    PCVL_TRY(cached_tile_map(&mapA, A, K, M, lda));
-    PCVL_TRY(cached_tile_map(&mapB, B, K, N, ldb));
-    // persistent: one CTA per SM over every tile of the output
+    PCVL_TRY(cached_tile_map(&mapA, A, K, M, lda, transA ? kMapMN : kMapK));
+    PCVL_TRY(cached_tile_map(&mapB, B, K, N, ldb, transB ? kMapMN : kMapK));
+    // persistent: two CTAs per SM over every tile of the output
     const int ntiles = (int)grid.x * (int)grid.y;
-    const int ctas = std::min(ntiles, num_sms());
-    const int smem = kPStages * (int)kStageBytes + 1024;
-    PCVL_TRY(allow_smem(reinterpret_cast<const void*>(gemm_tma_persistent), smem));
-    gemm_tma_persistent<<<ctas, kPThreads, smem, (cudaStream_t)stream>>>(mapA, mapB, g, (int)grid.x, ntiles);
+    const int ctas = std::min(ntiles, kPCtasPerSm * num_sms());
+    const int smem = (int)kPSmemBytes;
+    void (*kern)(const CUtensorMap, const CUtensorMap, GemmArgs, int, int) =
+        transA ? (transB ? gemm_tma_persistent<true, true> : gemm_tma_persistent<true, false>)
+               : (transB ? gemm_tma_persistent<false, true> : gemm_tma_persistent<false, false>);
+    PCVL_TRY(allow_smem(reinterpret_cast<const void*>(kern), smem));
+    kern<<<ctas, kPThreads, smem, (cudaStream_t)stream>>>(mapA, mapB, g, (int)grid.x, ntiles);
   } else {
     const int smem = kStages * 2 * (int)kTileBytes;
     PCVL_TRY(allow_smem(reinterpret_cast<const void*>(gemm_tc_kernel), smem));

@@ -24,7 +24,11 @@ pytestmark = pytest.mark.gpu
                                              (512, 384, 1024, 0, 0, 0), (300, 200, 136, 0, 0, 2),
                                              # more tiles than SMs: every persistent CTA walks several
                                              # tiles through both accumulators and wraps the load ring
-                                             (7680, 900, 512, 0, 0, 2), (4096, 1024, 1024, 0, 0, 0)])
+                                             (7680, 900, 512, 0, 0, 2), (4096, 1024, 1024, 0, 0, 0),
+                                             # transposed operands by TMA (MN-major tiles): the
+                                             # backward GEMMs' shapes, ragged edges in every dimension
+                                             (7680, 512, 904, 0, 1, 0), (512, 904, 7680, 1, 0, 0),
+                                             (1000, 520, 776, 1, 1, 2), (200, 136, 72, 1, 0, 1)])
 def test_gemm_bf16(native, M, N, K, ta, tb, epi):
     g = torch.Generator().manual_seed(M + N + K)
     A = torch.randn(K, M, generator=g) if ta else torch.randn(M, K, generator=g)
