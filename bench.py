@@ -350,17 +350,21 @@ def run_ours(args):
     k_ms = statistics.median(kt)
     fp64_peak = measured_fp64_peak(torch)
     achieved = len(sel) * glynn_flops(24) / (k_ms * 1e-3) / 1e12
+    ki = (2 * 24) // 3  # rows of each n = 24 product multiplied on the integer pipes
     roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp64_peak, "traffic": traffic_from_profile("perm_bin_fx_n24"),
                 "kernel": "perm_bin_fx<24> (the n=24 bin of the batch)",
                 "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 on this GPU (the measured peaks file "
                                "has no FP64 entry)",
                 "algorithmic_flops_per_permanent": "2^(n-1) (8n - 4)",
-                "note": "FP64 arithmetic with exact fixed-point row sums on the integer pipe (one rounding "
-                        "to FP64 each); per sign vector the FP64 pipe issues 4n - 4 instructions (products "
-                        "and the accumulation) for 8n - 4 algorithmic flops, so frac can reach "
-                        "(8n-4)/(2(4n-4)) = 1.02 at n = 24; with FP64 row sums (secondary "
-                        "perm_batch_fp64_dadd) 6n - 4 instructions, frac <= 0.67",
+                "note": f"FP64-class arithmetic on two pipes at once: exact fixed-point row sums on the "
+                        f"integer pipe; of each sign vector's product of 24 row sums, {24 - ki} are multiplied "
+                        f"in FP64 and {ki} in 64-bit block floating point on the integer pipes (62 significant "
+                        f"bits, finer than FP64), and the halves meet in the compensated FP64 accumulation. "
+                        f"The FP64 pipe issues 4 (n - {ki}) = {4 * (24 - ki)} instructions per sign vector for "
+                        f"8n - 4 = 188 algorithmic flops, so frac above 1 is the integer pipes' share; with "
+                        f"every product in FP64 the kernel reached 1.04 of this peak, with FP64 row sums "
+                        f"(secondary perm_batch_fp64_dadd) 6n - 4 instructions, frac <= 0.67",
                 "step_tflops": flops_total / (ms / args.steps * 1e-3) / 1e12}
 
     line = {"metric": METRIC, "value": value, "unit": "perms/s", "n_gpus": ws, "steps": args.steps,

@@ -369,12 +369,14 @@ __global__ void __launch_bounds__(kPermThreads) perm_bin_f64(PermBinArgs a) {
 // The FP64 default (perm_bin_fx) keeps every row sum exact: the prepared matrix holds
 // each scaled element as a 64-bit fixed-point integer (value 2^F x element, F = 62 - c,
 // so every row sum, |r| < 2^c, stays below 2^62), the lo table, the hi parts and their
-// Gray-code updates are integer additions on the integer pipe, and each row sum is
-// converted to FP64 once, rounded to nearest even, by integer operations on its bits.
-// The product tree and the compensated accumulation are the FP64 ones above, so every
-// rounding of the sum is an FP64 rounding and the row sums carry none (FP64 row sums
-// round at every addition).  Per sign vector the FP64 pipe then issues 4n - 4
-// instructions instead of 6n - 4.
+// Gray-code updates are integer additions on the integer pipe.  The product of a sign
+// vector's row sums splits in two (fx_int_rows below): the first rows are converted to
+// FP64 once, rounded to nearest even, by integer operations on their bits, and multiplied
+// by the FP64 tree above; the others are multiplied in 64-bit block floating point on the
+// integer pipes (62 significant bits) and converted once.  The two halves meet in the
+// compensated FP64 accumulation, so the row sums carry no rounding and every product at
+// most an FP64 one.  Per sign vector the FP64 pipe issues 4 (n - KI) instructions instead of
+// the 6n - 4 of FP64 row sums.
 template <int N>
 struct FixedPoint {
   static constexpr int c = 20 < 120 / N ? 20 : 120 / N;  // row l1 norms in [2^(c-1), 2^c)
@@ -412,14 +414,98 @@ struct RowProdFX {
   }
 };
 
+// 64-bit block floating point on the integer pipes: the complex value (re + i im) 2^e with
+// |re|, |im| < 2^62 and, after bf_norm, the larger magnitude's leading one at bit 61.  A
+// product takes the high 64 bits of the four 128-bit products (__mul64hi) and shifts back:
+// 62 significant bits, truncated once per product (relative error below 2^-59, under the
+// 2^-53 of an FP64 product).  Exact row sums enter with e = -F.
+struct BFC {
+  long long re, im;
+  int e;
+};
+
+__device__ __forceinline__ BFC bf_norm(long long re, long long im, int e) {
+  const unsigned long long ar = re < 0 ? 0ull - (unsigned long long)re : (unsigned long long)re;
+  const unsigned long long ai = im < 0 ? 0ull - (unsigned long long)im : (unsigned long long)im;
+  const int sh = __clzll((long long)(ar | ai)) - 2;  // >= 0 below 2^62; 62 for zero
+  BFC z;
+  z.re = (long long)((unsigned long long)re << sh);
+  z.im = (long long)((unsigned long long)im << sh);
+  z.e = e - sh;
+  return z;
+}
+
+__device__ __forceinline__ BFC bf_mul(const BFC& a, const BFC& b) {
+  const long long rr = __mul64hi(a.re, b.re), ii = __mul64hi(a.im, b.im);
+  const long long ri = __mul64hi(a.re, b.im), ir = __mul64hi(a.im, b.re);
+  return bf_norm(rr - ii, ri + ir, a.e + b.e + 64);  // |rr|, |ii| <= 2^60: no overflow
+}
+
+// x 2^e as a double, rounded to nearest even (x from bf_norm / bf_mul: |x| < 2^62).  The
+// product of many small row sums can fall below the normal FP64 range (a row sum is at
+// least 2^-F when not zero, and 26 rows of n = 40 reach 2^-1534); such a term is flushed
+// to zero, beside the terms whose FP64 roundings are larger by hundreds of binades.
+__device__ __forceinline__ double bf_to_f64(long long x, int e) {
+  const unsigned long long ux = (unsigned long long)x;
+  const unsigned long long sgn = ux & 0x8000000000000000ull;
+  const unsigned long long ax = x < 0 ? 0ull - ux : ux;
+  const int lz = __clzll((long long)ax);
+  const int be = 1023 + 63 + e - lz;  // biased exponent of the leading one
+  if (ax == 0 || be <= 0) return 0.0;
+  const unsigned long long mn = ax << (lz & 63);
+  unsigned long long mant = mn >> 11;
+  const unsigned int rem = (unsigned int)mn & 0x7ffu;
+  mant += (rem + (unsigned int)(mant & 1ull) + 0x3ffu) >> 11;
+  const unsigned long long bits = sgn | (((unsigned long long)be << 52) + mant - (1ull << 52));
+  return __longlong_as_double((long long)bits);
+}
+
+template <int LO, int HI, int F>
+struct RowProdBF {
+  static __device__ __forceinline__ BFC run(const longlong2* H, const longlong2* Tb) {
+    if constexpr (HI - LO == 1) {
+      const longlong2 t = Tb[LO];
+      return bf_norm(H[LO].x + t.x, H[LO].y + t.y, -F);
+    } else {
+      constexpr int MID = (LO + HI) / 2;
+      return bf_mul(RowProdBF<LO, MID, F>::run(H, Tb), RowProdBF<MID, HI, F>::run(H, Tb));
+    }
+  }
+};
+
+// Rows whose product goes to the integer pipes in the FP64 kernel: rows [0, N - KI) are
+// multiplied in FP64 (4 DFMA per complex product; GB300's FP64 pipe retires 2 per SM per
+// clock), rows [N - KI, N) in 64-bit block floating point on the integer pipes (a product
+// measured at 2.3x the FP64 product's rate), and the two partial products meet in the
+// FP64 multiply-add that accumulates the sign vector's term, so both pipes work at once.
+// Measured on the 8192-matrix batch (FP64 perms/s, built-in launch shapes): KI = 0: 6710,
+// N/4: 8262, N/3: 8828, N/2: 9411, 3N/5: 9665, 2N/3: 9798, 3N/4: 9181, N - 1: 7666 (the
+// integer pipes then bound it).
+template <int N>
+__host__ __device__ constexpr int fx_int_rows() {
+  return N >= 2 ? (2 * N) / 3 : 0;
+}
+
 template <int N>
 __device__ __forceinline__ void lo_sweep_fx(const longlong2* H, const longlong2* T, int nsteps, uint32_t hsign,
                                             double& sr, double& si) {
   constexpr int F = FixedPoint<N>::F;
+  constexpr int KI = fx_int_rows<N>();
+  static_assert(KI >= 0 && KI < N, "at least one row of the product stays in FP64");
   for (int b = 0; b < nsteps; ++b) {
     const longlong2* Tb = T + b * N;
     const uint32_t s = (((uint32_t)__popc(b) ^ hsign) & 1u) << 31;
-    if constexpr (N == 1) {
+    if constexpr (KI > 0 && N > 1) {
+      double2 x = RowProdFX<0, N - KI, F>::run(H, Tb);
+      const BFC z = RowProdBF<N - KI, N, F>::run(H, Tb);
+      const double2 y = make_double2(bf_to_f64(z.re, z.e), bf_to_f64(z.im, z.e));
+      x.x = flip64(x.x, s);
+      x.y = flip64(x.y, s);
+      sr = fma(x.x, y.x, sr);
+      sr = fma(-x.y, y.y, sr);
+      si = fma(x.x, y.y, si);
+      si = fma(x.y, y.x, si);
+    } else if constexpr (N == 1) {
       sr += flip64(fx_to_f64(H[0].x + Tb[0].x, F), s);
       si += flip64(fx_to_f64(H[0].y + Tb[0].y, F), s);
     } else {
