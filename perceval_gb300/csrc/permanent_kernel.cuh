@@ -460,6 +460,23 @@ __device__ __forceinline__ double bf_to_f64(long long x, int e) {
   return __longlong_as_double((long long)bits);
 }
 
+// The FP64 rows of the split product, unscaled: each exact row sum (an integer, value x
+// 2^F) is converted by the hardware's round-to-nearest-even int64 -> FP64 conversion, and
+// the common factor 2^(-F (n - KI)) is applied once to the CTA's partial sums (a power of
+// two: no rounding).  At most 14 rows of magnitude below 2^62 keep the product below 2^868.
+template <int LO, int HI>
+struct RowProdCV {
+  static __device__ __forceinline__ double2 run(const longlong2* H, const longlong2* Tb) {
+    if constexpr (HI - LO == 1) {
+      const longlong2 t = Tb[LO];
+      return make_double2(__ll2double_rn(H[LO].x + t.x), __ll2double_rn(H[LO].y + t.y));
+    } else {
+      constexpr int MID = (LO + HI) / 2;
+      return cmul64(RowProdCV<LO, MID>::run(H, Tb), RowProdCV<MID, HI>::run(H, Tb));
+    }
+  }
+};
+
 template <int LO, int HI, int F>
 struct RowProdBF {
   static __device__ __forceinline__ BFC run(const longlong2* H, const longlong2* Tb) {
@@ -478,9 +495,11 @@ struct RowProdBF {
 // clock), rows [N - KI, N) in 64-bit block floating point on the integer pipes (a product
 // measured at 2.3x the FP64 product's rate), and the two partial products meet in the
 // FP64 multiply-add that accumulates the sign vector's term, so both pipes work at once.
-// Measured on the 8192-matrix batch (FP64 perms/s, built-in launch shapes): KI = 0: 6710,
-// N/4: 8262, N/3: 8828, N/2: 9411, 3N/5: 9665, 2N/3: 9798, 3N/4: 9181, N - 1: 7666 (the
-// integer pipes then bound it).
+// Measured on the 8192-matrix batch (FP64 perms/s, built-in launch shapes), with the FP64
+// rows converted by integer operations on their bits: KI = 0: 6710, N/4: 8262, N/3: 8828,
+// N/2: 9411, 3N/5: 9665, 2N/3: 9798, 3N/4: 9181, N - 1: 7666 (the integer pipes then bound
+// it); with the hardware conversion of RowProdCV, which takes that work off the integer
+// pipes: 2N/3: 10917, 3N/4: 10742, 4N/5: 10827.
 template <int N>
 __host__ __device__ constexpr int fx_int_rows() {
   return N >= 2 ? (2 * N) / 3 : 0;
@@ -492,11 +511,13 @@ __device__ __forceinline__ void lo_sweep_fx(const longlong2* H, const longlong2*
   constexpr int F = FixedPoint<N>::F;
   constexpr int KI = fx_int_rows<N>();
   static_assert(KI >= 0 && KI < N, "at least one row of the product stays in FP64");
+  static_assert(KI == 0 || 62 * (N - KI) + FixedPoint<N>::c * KI < 1000,
+                "unscaled terms stay inside the FP64 range");
   for (int b = 0; b < nsteps; ++b) {
     const longlong2* Tb = T + b * N;
     const uint32_t s = (((uint32_t)__popc(b) ^ hsign) & 1u) << 31;
     if constexpr (KI > 0 && N > 1) {
-      double2 x = RowProdFX<0, N - KI, F>::run(H, Tb);
+      double2 x = RowProdCV<0, N - KI>::run(H, Tb);
       const BFC z = RowProdBF<N - KI, N, F>::run(H, Tb);
       const double2 y = make_double2(bf_to_f64(z.re, z.e), bf_to_f64(z.im, z.e));
       x.x = flip64(x.x, s);
@@ -633,7 +654,10 @@ __global__ void __launch_bounds__(kPermThreads) perm_bin_fx(PermBinArgs a) {
       ci += red[3][w];
       comp_add(si, ci, red[2][w]);
     }
-    a.partials[item] = make_double2(sr + cr, si + ci);
+    // the FP64 rows of the split product were multiplied unscaled
+    constexpr int KI = fx_int_rows<N>();
+    const double sc = KI > 0 && N > 1 ? ldexp(1.0, -FixedPoint<N>::F * (N - KI)) : 1.0;
+    a.partials[item] = make_double2((sr + cr) * sc, (si + ci) * sc);
   }
 }
 
