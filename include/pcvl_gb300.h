@@ -27,11 +27,13 @@ extern "C" {
 #define PCVL_ERR_TIMEOUT 4  /* a bounded device-side wait gave up */
 
 /* Arithmetic of the permanent, SLOS and sampler kernels (`precision` arguments).
- * PCVL_PREC_FP64: native FP64, the reference's own arithmetic (complex128 in
+ * PCVL_PREC_FP64: FP64 precision, the reference's own arithmetic (complex128 in
  * exqalibur); the default of the Python layer.  For permanents every row sum is exact
- * (64-bit fixed point on the integer pipe, rounded once to FP64) and every product and
- * sum is an FP64 operation.  PCVL_PREC_FP64_DADD (permanents only): the same with the
- * row sums too in FP64 additions, one rounding per addition.  PCVL_PREC_FLOAT_FLOAT:
+ * (64-bit fixed point on the integer pipe), a third of each sign vector's product is
+ * taken in FP64 and the rest in 64-bit block floating point on the integer pipes (62
+ * significant bits), and the sums are compensated FP64 sums: no step rounds more coarsely
+ * than FP64.  PCVL_PREC_FP64_DADD (permanents only): every row sum and product an FP64
+ * operation, one rounding per addition.  PCVL_PREC_FLOAT_FLOAT:
  * every value an unevaluated pair of FP32 numbers (~48 significant bits) on the FP32
  * pipe, several times faster on GB300, whose FP64 rate is a small fraction of its FP32
  * rate.  PCVL_PREC_FP32: FP32 with compensated sums (sampler only). */

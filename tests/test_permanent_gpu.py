@@ -138,6 +138,18 @@ def test_glynn_ryser_agree_large(native, prec):
     assert np.max(np.abs(g - r) / np.abs(g)) <= 1e-6
 
 
+def test_every_large_size_fp64_vs_float_float(native):
+    """Sizes 31, 33, 34, 35, whose FP64 kernels (each size its own split of the product
+    between the FP64 and integer pipes) no other test runs on Haar data: FP64 against the
+    independent float-float kernel on one seeded submatrix each, at the float-float
+    accuracy (about 20 s)."""
+    for n in (31, 33, 34, 35):
+        a = haar_submatrices(1, n, n, seed=200 + n)[0]
+        f = gpu_perms(native, [a], 0, "fp64")[0]
+        ff = gpu_perms(native, [a], 0, "float-float")[0]
+        assert abs(f - ff) <= 1e-8 * abs(f), (n, f, ff)
+
+
 def _abs_term_sum(r, ryser):
     """Exact sum of |term| over Glynn's sign vectors (delta_0 = +1) or Ryser's subsets for
     a matrix whose rows all equal the positive integer vector r (dynamic programme over
