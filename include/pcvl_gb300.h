@@ -254,9 +254,10 @@ int pcvl_fock_mask_ranks(int32_t m, int32_t n, int32_t n_masks, const int8_t* di
  * out_counts_d[s * m .. s * m + m - 1] (int32).  Sample s uses Philox4x32-10 with
  * key (seed, 0) and counters (first_sample + s, step, draw), so results are
  * reproducible and independent of scheduling.  precision: PCVL_PREC_FLOAT_FLOAT
- * (FP64-class pairs on the FP32 pipe), PCVL_PREC_FP64 (native FP64 sub-permanent sums)
- * or PCVL_PREC_FP32 (FP32 with compensated sums); the weights and the draw are FP64 in
- * every case.
+ * (FP64-class pairs on the FP32 pipe), PCVL_PREC_FP64 (FP64 precision: exact fixed-point
+ * column sums, 64-bit block-floating products on the integer pipes, FP64 sums of the
+ * terms) or PCVL_PREC_FP32 (FP32 with compensated sums); the weights and the draw are FP64
+ * in every case.
  */
 int pcvl_cc2017_sample(const double* u_d, int32_t m, const int32_t* input_state_h, int64_t count,
                        uint64_t seed, uint64_t first_sample, int32_t precision,

@@ -26,7 +26,8 @@ class Clifford2017Backend(ASamplingBackend):
                  "fp64": _native.PREC_FP64, "single": _native.PREC_FP32, "fp32": _native.PREC_FP32}
         if precision not in names:
             raise ValueError("precision must be 'double' / 'float-float' (FP64-class pairs, the default), "
-                             "'fp64' (native FP64) or 'single' / 'fp32'")
+                             "'fp64' (FP64 precision: exact fixed-point sums, block-floating products on "
+                             "the integer pipes, FP64 sums) or 'single' / 'fp32'")
         self._precision = names[precision]
         self._u_dev = None
 

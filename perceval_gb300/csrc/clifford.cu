@@ -36,6 +36,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "blockfloat.cuh"
 #include "runtime.cuh"
 
 namespace pcvl {
@@ -46,6 +47,8 @@ __device__ __forceinline__ float shx(float v, int mask) { return __shfl_xor_sync
 struct ArDD {  // float-float (FP64-class): lazy products and sums in the pattern loop,
                // exact two_sum accumulation of the high parts
   using C = cdd;
+  static constexpr bool kFixed = false;
+  static __device__ __forceinline__ C fix(C a, int) { return a; }
   struct Acc {
     float rh, rl, ih, il;
   };
@@ -92,6 +95,8 @@ struct ArDD {  // float-float (FP64-class): lazy products and sums in the patter
 
 struct ArF32 {  // FP32 with Kahan-compensated accumulation
   using C = float2;
+  static constexpr bool kFixed = false;
+  static __device__ __forceinline__ C fix(C a, int) { return a; }
   struct Acc {
     float sr, cr, si, ci;  // sums and compensations
   };
@@ -136,33 +141,75 @@ struct ArF32 {  // FP32 with Kahan-compensated accumulation
   }
 };
 
-struct Ar64 {  // native FP64: row sums, products and the sums of the sign patterns
-  using C = double2;
+// FP64 precision on two pipes (the sampler's FP64 mode): every element of the (k-1) x k
+// matrix is turned, after its column's power-of-two scaling, into 64-bit fixed point
+// (value x 2^F, F = 62 - c0, with c0 the bound on the scaled column l1 norms), so the lo
+// table, the hi parts and the column sums of every sign pattern are exact integer sums;
+// each column sum is then normalised to 64-bit block floating point and every product of
+// the leave-one-out products is a block-floating product on the integer pipes (62
+// significant bits); the terms are converted to FP64 once and summed in FP64.  The fixed
+// point keeps every element to 2^-F of its column's l1 norm, the normwise accuracy of an
+// FP64 column sum.
+struct ArFX {
+  using C = BFC;
+  static constexpr bool kFixed = true;
   struct Acc {
     double r, i;
   };
-  static __device__ __forceinline__ C zero() { return make_double2(0.0, 0.0); }
-  static __device__ __forceinline__ C one() { return make_double2(1.0, 0.0); }
-  static __device__ __forceinline__ C add(C a, C b) { return make_double2(a.x + b.x, a.y + b.y); }
-  static __device__ __forceinline__ C add_n(C a, C b) { return add(a, b); }
-  static __device__ __forceinline__ C sub_n(C a, C b) { return make_double2(a.x - b.x, a.y - b.y); }
-  static __device__ __forceinline__ C mul(C a, C b) {
-    return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+  static __device__ __forceinline__ C zero() { return {0, 0, 0}; }
+  static __device__ __forceinline__ C one() { return {1ll << 61, 0, -61}; }
+  // fixed-point sums (equal exponents), in two's-complement arithmetic
+  static __device__ __forceinline__ C add_n(C a, C b) {
+    return {(long long)((unsigned long long)a.re + (unsigned long long)b.re),
+            (long long)((unsigned long long)a.im + (unsigned long long)b.im), a.e};
   }
-  static __device__ __forceinline__ C neg(C a) { return make_double2(-a.x, -a.y); }
-  static __device__ __forceinline__ C twice(C a) { return make_double2(2.0 * a.x, 2.0 * a.y); }
-  static __device__ __forceinline__ C from(double2 v) { return v; }
-  static __device__ __forceinline__ C scale(C a, int e) { return make_double2(ldexp(a.x, e), ldexp(a.y, e)); }
-  static __device__ __forceinline__ float mag(C a) { return (float)(fabs(a.x) + fabs(a.y)); }
-  static __device__ __forceinline__ double shd(double v, int mask) { return __shfl_xor_sync(0xffffffffu, v, mask); }
-  static __device__ __forceinline__ C shfl(C v, int mask) { return make_double2(shd(v.x, mask), shd(v.y, mask)); }
+  static __device__ __forceinline__ C sub_n(C a, C b) {
+    return {(long long)((unsigned long long)a.re - (unsigned long long)b.re),
+            (long long)((unsigned long long)a.im - (unsigned long long)b.im), a.e};
+  }
+  static __device__ __forceinline__ C twice(C a) {
+    return {(long long)((unsigned long long)a.re << 1), (long long)((unsigned long long)a.im << 1), a.e};
+  }
+  // a column sum of one sign pattern: exact, then normalised for the products
+  static __device__ __forceinline__ C add(C a, C b) {
+    const C s = add_n(a, b);
+    return bf_norm(s.re, s.im, s.e);
+  }
+  static __device__ __forceinline__ C mul(C a, C b) { return bf_mul(a, b); }
+  static __device__ __forceinline__ C neg(C a) {
+    return {(long long)(0ull - (unsigned long long)a.re), (long long)(0ull - (unsigned long long)a.im), a.e};
+  }
+  // an element of U: both parts on the exponent of the larger (rounded to 62 bits below it)
+  static __device__ __forceinline__ C from(double2 v) {
+    const double mx = fmax(fabs(v.x), fabs(v.y));
+    if (mx == 0.0) return {0, 0, 0};
+    int e0;
+    frexp(mx, &e0);  // mx in [2^(e0-1), 2^e0)
+    return {__double2ll_rn(ldexp(v.x, 61 - e0)), __double2ll_rn(ldexp(v.y, 61 - e0)), e0 - 61};
+  }
+  static __device__ __forceinline__ C scale(C a, int e) { return {a.re, a.im, a.e + e}; }
+  static __device__ __forceinline__ float mag(C a) {
+    return ldexpf((float)llabs(a.re) + (float)llabs(a.im), a.e);
+  }
+  // the element as fixed point with F fraction bits (|value| < 2^(62 - F) after scaling)
+  static __device__ __forceinline__ C fix(C a, int F) {
+    const int sh = a.e + F;
+    if (sh >= 0) return {(long long)((unsigned long long)a.re << sh), (long long)((unsigned long long)a.im << sh), -F};
+    if (sh <= -63) return {0, 0, -F};
+    return {a.re >> -sh, a.im >> -sh, -F};
+  }
+  static __device__ __forceinline__ C shfl(C v, int mask) {
+    return {__shfl_xor_sync(0xffffffffu, v.re, mask), __shfl_xor_sync(0xffffffffu, v.im, mask),
+            __shfl_xor_sync(0xffffffffu, v.e, mask)};
+  }
   static __device__ __forceinline__ Acc acc_zero() { return {0.0, 0.0}; }
   static __device__ __forceinline__ void acc_add(Acc& a, C x) {
-    a.r += x.x;
-    a.i += x.y;
+    a.r += bf_to_f64(x.re, x.e);
+    a.i += bf_to_f64(x.im, x.e);
   }
   static __device__ __forceinline__ void acc_fold(Acc&) {}
   static __device__ __forceinline__ Acc acc_merge(Acc a, Acc b) { return {a.r + b.r, a.i + b.i}; }
+  static __device__ __forceinline__ double shd(double v, int mask) { return __shfl_xor_sync(0xffffffffu, v, mask); }
   static __device__ __forceinline__ Acc acc_shfl(Acc v, int mask) { return {shd(v.r, mask), shd(v.i, mask)}; }
   static __device__ __forceinline__ double2 acc_value(Acc a) { return make_double2(a.r, a.i); }
 };
@@ -245,6 +292,9 @@ __global__ void __launch_bounds__(kCCThreads) cc_sub_kernel(CCSubArgs a) {
     float l1 = 0.f;
     for (int r = 0; r < d; ++r) l1 += Ar::mag(Bs[r * K + tt]);
     const int c0 = min(4, (120 - (k - 2)) / (k - 1));
+    // fixed point: every column sum must stay below 2^62, so the FP32 l1 (a few ulps of
+    // rounding) is nudged up before the binade is taken
+    if (Ar::kFixed) l1 *= 1.f + 0x1p-16f;
     int ex = 0;
     if (l1 > 0.f) frexpf(l1, &ex);
     const int e = l1 > 0.f ? c0 - ex : 0;
@@ -252,6 +302,11 @@ __global__ void __launch_bounds__(kCCThreads) cc_sub_kernel(CCSubArgs a) {
     for (int r = 0; r < d; ++r) Bs[r * K + tt] = Ar::scale(Bs[r * K + tt], e);
   }
   team_sync<TW>();
+  if constexpr (Ar::kFixed) {  // every element (padding included) into fixed point
+    const int F = 62 - min(4, (120 - (k - 2)) / (k - 1));
+    for (int e = tt; e < d * K; e += NT) Bs[e] = Ar::fix(Bs[e], F);
+    team_sync<TW>();
+  }
   // lo table over rows 1..L: T[b][c] = sum_l (bit l of b ? -1 : +1) B[1 + l][c]
   for (int c = tt; c < K; c += NT) {
     C t0 = Ar::zero();
@@ -603,7 +658,7 @@ static int cc2017_run(const double* u_d, int32_t m, int32_t nstates, const int32
   const int64_t last = count - (waves - 1) * W;
   for (int k = 2; k <= n; ++k) max_chunks = std::max(max_chunks, plan_step(k, last, target_ctas).chunks);
 
-  const size_t csz = precision == kPrecFloatFloat ? sizeof(cdd) : precision == kPrecFP64 ? sizeof(double2)
+  const size_t csz = precision == kPrecFloatFloat ? sizeof(cdd) : precision == kPrecFP64 ? sizeof(BFC)
                                                                                           : sizeof(float2);
   const size_t o_cols0 = align_up((size_t)m * m * csz, 256);
   const size_t o_soff = o_cols0 + align_up(cols.size() * sizeof(int32_t), 256);
@@ -628,7 +683,7 @@ static int cc2017_run(const double* u_d, int32_t m, int32_t nstates, const int32
   if (precision == kPrecFloatFloat)
     cc_convert<ArDD><<<cgrid, 256, 0, s>>>((const double2*)u_d, m, (cdd*)base);
   else if (precision == kPrecFP64)
-    cc_convert<Ar64><<<cgrid, 256, 0, s>>>((const double2*)u_d, m, (double2*)base);
+    cc_convert<ArFX><<<cgrid, 256, 0, s>>>((const double2*)u_d, m, (BFC*)base);
   else
     cc_convert<ArF32><<<cgrid, 256, 0, s>>>((const double2*)u_d, m, (float2*)base);
   PCVL_CUDA(cudaGetLastError());
@@ -673,7 +728,7 @@ static int cc2017_run(const double* u_d, int32_t m, int32_t nstates, const int32
         sa.Hb = p.Hb;
         sa.chunks = p.chunks;
         const int rc = precision == kPrecFloatFloat ? sub_dispatch<ArDD>(p, sa, s)
-                       : precision == kPrecFP64     ? sub_dispatch<Ar64>(p, sa, s)
+                       : precision == kPrecFP64     ? sub_dispatch<ArFX>(p, sa, s)
                                                     : sub_dispatch<ArF32>(p, sa, s);
         if (rc != 0) {
           set_error("CC2017 sub-permanent launch failed: %s", cudaGetErrorString((cudaError_t)rc));

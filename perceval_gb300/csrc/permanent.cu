@@ -6,14 +6,16 @@
 //  1. perm_prepare: every row i of every matrix is scaled by an exact power of two
 //     2^{e_i} so that its l1 norm lies in [2^{c-1}, 2^c), c = min(20, 120 / n); then
 //     every |row sum| <= 2^c and every row-sum product stays inside the FP32 range
-//     (and far inside the FP64 range).  The scaled matrix is stored as double2 (FP64)
-//     or float-float pairs; sum_i e_i is kept.
-//  2. one bin launch per distinct size n (perm_bin_f64<n> or perm_bin_kernel<n>),
-//     each CTA handling a chunk of hi sign patterns of one matrix and writing one FP64
-//     partial.
+//     (and far inside the FP64 range).  The scaled matrix is stored as 64-bit fixed
+//     point (FP64), double2 (FP64 with FP64 row sums) or float-float pairs; sum_i e_i
+//     is kept.
+//  2. one bin launch per distinct size n (perm_bin_fx<n>, perm_bin_f64<n> or
+//     perm_bin_kernel<n>), each CTA handling a chunk of hi sign patterns of one matrix
+//     and writing one FP64 partial.
 //  3. perm_reduce: per matrix, Neumaier-compensated FP64 sum of its partials, times
 //     2^{1-n} (Glynn) or (-1)^n (Ryser), times 2^{-sum e_i}.
 #include <algorithm>
+#include <type_traits>
 #include <atomic>
 #include <cstring>
 #include <mutex>
@@ -61,6 +63,11 @@ __global__ void perm_prepare(const double2* __restrict__ src, const int64_t* __r
       const double2 v = src[off + (int64_t)i * n + j];
       l1 += hypot(v.x, v.y);
     }
+    // Fixed point (the FP64 default): |every row sum| <= l1 must stay below 2^62 in the
+    // block-floating products, so l1 is nudged up by far more than its rounding error and
+    // the elements' roundings (a row whose l1 lies within 2^-40 below a power of two is
+    // scaled one binade lower).
+    if constexpr (std::is_same<E, longlong2>::value) l1 *= 1.0 + 0x1p-40;
     int e = 0;
     if (l1 > 0.0 && isfinite(l1)) {
       int x;
