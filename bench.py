@@ -598,6 +598,9 @@ def secondary(torch, _native, random_unitary, dev, flush, fp64_peak_tflops):
     cnt = 100000  # the configuration's 1e5 samples
     t_cc = timed(lambda: _native.cc2017_sample(U4, [1] * 20 + [0] * 380, cnt, seed=1), reps=1)
     res["cc2017_n20_m400"] = {"samples_per_s": cnt / (t_cc * 1e-3), "samples": cnt, "precision": "float-float"}
+    # the same in the FP64 mode (fixed-point column sums, block-floating products), 1e4 samples
+    t_cc64 = timed(lambda: _native.cc2017_sample(U4, [1] * 20 + [0] * 380, 10000, seed=1, precision=2), reps=1)
+    res["cc2017_n20_m400"]["fp64"] = {"samples_per_s": 10000 / (t_cc64 * 1e-3), "samples": 10000}
     # many input states (the per-input loop of a samples provider): 64 distinct 6-photon inputs
     # on m = 64, 1000 samples each, one wavefront against one call per input
     rng = np.random.default_rng(5)
