@@ -922,7 +922,8 @@ def run_learned(args):
 
 def run_large_perm(args):
     """One n = 40 Haar-submatrix permanent (Glynn, 1.74e14 FP64-equivalent flops), the
-    largest single-permanent size of the benchmark configurations; about a minute."""
+    largest single-permanent size of the benchmark configurations, in FP64 and in
+    float-float (about three minutes together)."""
     import torch
     from perceval_gb300 import _native
     from perceval_gb300.utils.matrix import random_unitary
@@ -932,17 +933,21 @@ def run_large_perm(args):
     n = 40
     a = np.ascontiguousarray(Ubig[np.ix_(rng.choice(1024, n, False), rng.choice(1024, n, False))])
     ad = torch.from_numpy(a).cuda()
-    o = torch.empty(1, dtype=torch.complex128, device="cuda")
-    s0, e0 = torch.cuda.Event(True), torch.cuda.Event(True)
-    s0.record()
-    _native.permanent_batch(ad, np.array([0]), np.array([n]), o, 0)
-    e0.record()
-    e0.synchronize()
-    ms = s0.elapsed_time(e0)
-    v = complex(o.cpu().item())
-    print(json.dumps({"perm_single_n40": {"glynn": [v.real, v.imag], "glynn_ms": ms,
-                                          "glynn_tflops_fp64_equiv": glynn_flops(n) / (ms * 1e-3) / 1e12}}),
-          flush=True)
+    res = {}
+    for prec in ("fp64", "float-float"):
+        o = torch.empty(1, dtype=torch.complex128, device="cuda")
+        s0, e0 = torch.cuda.Event(True), torch.cuda.Event(True)
+        s0.record()
+        _native.permanent_batch(ad, np.array([0]), np.array([n]), o, 0, precision=prec)
+        e0.record()
+        e0.synchronize()
+        ms = s0.elapsed_time(e0)
+        v = complex(o.cpu().item())
+        res[prec] = {"glynn": [v.real, v.imag], "glynn_ms": ms,
+                     "glynn_tflops_fp64_equiv": glynn_flops(n) / (ms * 1e-3) / 1e12}
+    f, ff = complex(*res["fp64"]["glynn"]), complex(*res["float-float"]["glynn"])
+    res["float_float_rel_diff_vs_fp64"] = abs(ff - f) / abs(f)
+    print(json.dumps({"perm_single_n40": res}), flush=True)
 
 
 def profile_case(name: str):
@@ -1022,7 +1027,8 @@ def main():
     ap.add_argument("--learned", action="store_true",
                     help="run the learned-proposal sampler workload (n=30, m=900 and n=8, m=64) and exit")
     ap.add_argument("--learned-train", type=int, default=2048, help="exact training samples at n=30")
-    ap.add_argument("--large-perm", action="store_true", help="one n = 40 permanent (about a minute)")
+    ap.add_argument("--large-perm", action="store_true",
+                    help="one n = 40 permanent in FP64 and in float-float (about three minutes)")
     ap.add_argument("--profile-case", choices=["perm24", "perm24dadd", "perm24ff", "slos20", "slos20ff", "slos20p", "slosmask22", "slap1024", "slos16b256",
                                                "cc2017", "gurvits20", "gemm"],
                     help="run one small untimed case of a single kernel (for ncu) and exit")
