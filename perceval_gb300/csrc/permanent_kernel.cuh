@@ -372,12 +372,14 @@ __global__ void __launch_bounds__(kPermThreads) perm_bin_f64(PermBinArgs a) {
 // so every row sum, |r| < 2^c, stays below 2^62), the lo table, the hi parts and their
 // Gray-code updates are integer additions on the integer pipe.  The product of a sign
 // vector's row sums splits in two (fx_int_rows below): the first rows are converted to
-// FP64 once, rounded to nearest even, by integer operations on their bits, and multiplied
-// by the FP64 tree above; the others are multiplied in 64-bit block floating point on the
-// integer pipes (62 significant bits) and converted once.  The two halves meet in the
-// compensated FP64 accumulation, so the row sums carry no rounding and every product at
-// most an FP64 one.  Per sign vector the FP64 pipe issues 4 (n - KI) instructions instead of
-// the 6n - 4 of FP64 row sums.
+// FP64 once by the hardware's round-to-nearest-even conversion (RowProdCV, unscaled) and
+// multiplied by the FP64 tree above; the others are multiplied in 64-bit block floating
+// point on the integer pipes (62 significant bits) and converted once.  The two halves
+// meet in the compensated FP64 accumulation, so the row sums carry no rounding and every
+// product at most an FP64 one.  Per sign vector the FP64 pipe issues 4 (n - KI)
+// multiplies and n - KI conversions instead of the 6n - 4 instructions of FP64 row sums.
+// With KI = 0 (every product in FP64, the configuration measured as the baseline of the
+// split) the rows go through fx_to_f64 and RowProdFX instead.
 template <int N>
 struct FixedPoint {
   static constexpr int c = 20 < 120 / N ? 20 : 120 / N;  // row l1 norms in [2^(c-1), 2^c)
