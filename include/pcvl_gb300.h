@@ -43,7 +43,7 @@ extern "C" {
 #define PCVL_PREC_FP64_DADD 3
 
 /* ------------------------------------------------------------------ errors */
-/* Library version string, e.g. "pcvl_gb300 0.2.0 sm_103a". */
+/* Library version string, e.g. "pcvl_gb300 0.3.0 sm_103a". */
 const char* pcvl_version(void);
 /* Copies the calling thread's last error message into buf (NUL-terminated). */
 int pcvl_last_error(char* buf, size_t len);

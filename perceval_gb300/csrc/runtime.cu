@@ -100,7 +100,7 @@ int stage_h2d(const void* src, size_t bytes, void* dst_d, cudaStream_t stream) {
 
 }  // namespace pcvl
 
-extern "C" const char* pcvl_version(void) { return "pcvl_gb300 0.2.0 sm_103a"; }
+extern "C" const char* pcvl_version(void) { return "pcvl_gb300 0.3.0 sm_103a"; }
 
 extern "C" int pcvl_last_error(char* buf, size_t len) {
   if (!buf || len == 0) return PCVL_ERR_ARG;
