@@ -457,9 +457,14 @@ struct RowProdBF {
 // N/2: 9411, 3N/5: 9665, 2N/3: 9798, 3N/4: 9181, N - 1: 7666 (the integer pipes then bound
 // it); with the hardware conversion of RowProdCV, which takes that work off the integer
 // pipes: 2N/3: 10917, 3N/4: 10742, 4N/5: 10827.
+// Per size, the best of a second sweep over the FP64 rows d = N - KI in 4..8 (TFLOP/s of the
+// size's bin in the batch, built-in launch shapes): n = 16: d = 5 (1.66 against 1.52 at 2N/3),
+// 20: 6 (1.94 / 1.85), 22: 5 (1.90 / 1.79), 23: 7 (1.94 / 1.85); at 18, 21 and 24, 2N/3 was
+// best or level.  The rates move irregularly with d (n = 22: 1.90, 1.61, 1.70, 1.79 for
+// d = 5..8), the same in both sweeps, with how the two product trees split the rows.
 template <int N>
 __host__ __device__ constexpr int fx_int_rows() {
-  return N >= 2 ? (2 * N) / 3 : 0;
+  return N == 16 ? 11 : N == 20 ? 14 : N == 22 ? 17 : N == 23 ? 16 : N >= 2 ? (2 * N) / 3 : 0;
 }
 
 template <int N>
