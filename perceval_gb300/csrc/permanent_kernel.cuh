@@ -461,10 +461,13 @@ struct RowProdBF {
 // size's bin in the batch, built-in launch shapes): n = 16: d = 5 (1.66 against 1.52 at 2N/3),
 // 20: 6 (1.94 / 1.85), 22: 5 (1.90 / 1.79), 23: 7 (1.94 / 1.85); at 18, 21 and 24, 2N/3 was
 // best or level.  The rates move irregularly with d (n = 22: 1.90, 1.61, 1.70, 1.79 for
-// d = 5..8), the same in both sweeps, with how the two product trees split the rows.
+// d = 5..8), the same in both sweeps, with how the two product trees split the rows.  Among
+// single large permanents (d in {6, 8, 11, 13} against 2N/3): n = 26: d = 8 (1.88 against
+// 1.82), 28: 6 (1.74 / 1.65), 34: 8 (1.52 / 1.47); at 30 and 32, 2N/3 was best.
 template <int N>
 __host__ __device__ constexpr int fx_int_rows() {
-  return N == 16 ? 11 : N == 20 ? 14 : N == 22 ? 17 : N == 23 ? 16 : N >= 2 ? (2 * N) / 3 : 0;
+  return N == 16 ? 11 : N == 20 ? 14 : N == 22 ? 17 : N == 23 ? 16 : N == 26 ? 18 : N == 28 ? 22 : N == 34 ? 26
+         : N >= 2 ? (2 * N) / 3 : 0;
 }
 
 template <int N>
