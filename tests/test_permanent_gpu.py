@@ -138,6 +138,24 @@ def test_glynn_ryser_agree_large(native, prec):
     assert np.max(np.abs(g - r) / np.abs(g)) <= 1e-6
 
 
+@pytest.mark.parametrize("prec", PRECS)
+def test_rows_summing_to_one(native, oracle, prec):
+    """Doubly stochastic matrices |U_ij|^2 of Haar unitaries: non-negative real rows whose
+    l1 norm is 1 up to rounding, the case where the fixed-point scaling needs its margin
+    below 2^62 (every Glynn row sum with all signs + equals the row's l1)."""
+    rng = np.random.default_rng(13)
+    mats = []
+    for n in range(8, 21):
+        U = np.linalg.qr(rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)))[0]
+        mats.append(np.ascontiguousarray(np.abs(U) ** 2).astype(complex))
+    flat, offs, sizes = pack(mats)
+    ref = oracle.perm_batch(flat, offs, sizes)
+    for method in (0, 1):
+        got = gpu_perms(native, mats, method, prec)
+        rel = np.abs(got - ref) / np.abs(ref)
+        assert rel.max() <= RTOL, (method, rel.max(), sizes[rel.argmax()])
+
+
 def test_every_large_size_fp64_vs_float_float(native):
     """Sizes 31, 33, 34, 35, whose FP64 kernels (each size its own split of the product
     between the FP64 and integer pipes) no other test runs on Haar data: FP64 against the
