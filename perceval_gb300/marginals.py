@@ -1,6 +1,6 @@
 """Exact one- and two-mode marginal distributions of boson sampling outputs.
 
-No counterpart in the reference; these are the judges of a sampler at sizes where the
+No counterpart in the reference; they measure a sampler's accuracy at sizes where the
 full output distribution cannot be enumerated (n = 30 photons on m = 900 modes has
 about 10^56 outputs).
 

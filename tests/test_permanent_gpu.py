@@ -101,7 +101,7 @@ def test_config_sizes_vs_oracle(native, oracle, prec):
 
 
 @pytest.mark.parametrize("prec", PRECS)
-def test_north_star_sizes_vs_oracle(native, oracle, prec):
+def test_scale_up_sizes_vs_oracle(native, oracle, prec):
     """n = 25..30, one seeded Haar submatrix each (the scale-up sizes of the plain
     permanent target), against the oracle's FP64 Glynn sum at 1e-10 (about 15 s of
     oracle time on 16 cores)."""
