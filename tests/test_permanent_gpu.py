@@ -150,10 +150,16 @@ def test_rows_summing_to_one(native, oracle, prec):
         mats.append(np.ascontiguousarray(np.abs(U) ** 2).astype(complex))
     flat, offs, sizes = pack(mats)
     ref = oracle.perm_batch(flat, offs, sizes)
-    for method in (0, 1):
-        got = gpu_perms(native, mats, method, prec)
-        rel = np.abs(got - ref) / np.abs(ref)
-        assert rel.max() <= RTOL, (method, rel.max(), sizes[rel.argmax()])
+    got = gpu_perms(native, mats, 0, prec)
+    rel = np.abs(got - ref) / np.abs(ref)
+    assert rel.max() <= RTOL, (rel.max(), sizes[rel.argmax()])
+    # Ryser's alternating subset sums of a positive matrix cancel from O(1) terms down to a
+    # permanent near n!/n^n (2e-8 at n = 20): held to 1e-10 up to n = 12 and to its
+    # conditioning above
+    got = gpu_perms(native, mats, 1, prec)
+    rel = np.abs(got - ref) / np.abs(ref)
+    assert rel[sizes <= 12].max() <= RTOL, rel[sizes <= 12].max()
+    assert rel.max() <= (1e-5 if prec == "float-float" else 1e-7), (rel.max(), sizes[rel.argmax()])
 
 
 def test_every_large_size_fp64_vs_float_float(native):
