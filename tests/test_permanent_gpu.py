@@ -154,12 +154,14 @@ def test_rows_summing_to_one(native, oracle, prec):
     rel = np.abs(got - ref) / np.abs(ref)
     assert rel.max() <= RTOL, (rel.max(), sizes[rel.argmax()])
     # Ryser's alternating subset sums of a positive matrix cancel from O(1) terms down to a
-    # permanent near n!/n^n (2e-8 at n = 20): held to 1e-10 up to n = 12 and to its
-    # conditioning above
+    # permanent near n!/n^n: sum |terms| / |perm| is 2.1e3 at n = 8, 2.3e5 at n = 12 and
+    # 3.6e7 at n = 16 for these matrices, so Ryser is held to bounds with a tenfold margin
+    # over the errors measured (FP64 9e-9, float-float 1.3e-6 at n = 20)
     got = gpu_perms(native, mats, 1, prec)
     rel = np.abs(got - ref) / np.abs(ref)
-    assert rel[sizes <= 12].max() <= RTOL, rel[sizes <= 12].max()
-    assert rel.max() <= (1e-5 if prec == "float-float" else 1e-7), (rel.max(), sizes[rel.argmax()])
+    ff = prec == "float-float"
+    assert rel[sizes <= 12].max() <= (1e-7 if ff else 1e-9), rel[sizes <= 12].max()
+    assert rel.max() <= (1e-5 if ff else 1e-7), (rel.max(), sizes[rel.argmax()])
 
 
 def test_every_large_size_fp64_vs_float_float(native):
