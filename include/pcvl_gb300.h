@@ -61,8 +61,9 @@ int pcvl_release_workspace(void);
  * out_d[i] (complex128).  method: 0 = Glynn (sum over the 2^(n-1) sign vectors),
  * 1 = Ryser (over the 2^n column subsets).  The sign bits split into "lo" bits that
  * every thread enumerates from a shared-memory table of row-sum parts and "hi" bits
- * spread over threads and CTAs (walked in Gray-code order in FP64), so one large
- * matrix uses every SM; matrices are binned by size, one launch per size.  precision:
+ * spread over threads and CTAs (walked in Gray-code order: exact integer updates of
+ * fixed-point row sums in the FP64 default), so one large matrix uses every SM; matrices
+ * are binned by size, one launch per size.  precision:
  * PCVL_PREC_FP64, PCVL_PREC_FP64_DADD or PCVL_PREC_FLOAT_FLOAT.  The matrices must not overlap in mats_d,
  * except as identical entries (same offset and size): each is rescaled in place in
  * the library's scratch at its own offsets.  offsets_h and sizes_h are host arrays.
