@@ -625,7 +625,10 @@ def secondary(torch, _native, random_unitary, dev, flush, fp64_peak_tflops):
     # companion
     res["learned_mis_n30_m900"] = learned_case(torch, _native, random_unitary, 900, 30, 1024, 4, 8, 8, 96,
                                                tvd=False, n_ref64=32)
-    res["learned_mis_n8_m64"] = learned_case(torch, _native, random_unitary, 64, 8, 20000, 10, 64, 200, 25600)
+    # n = 8, m = 64 with enough samples of both samplers to resolve the marginals to 1e-3:
+    # 2048 chains x 4096 steps (8.4 M proposals) and 4 M exact samples
+    res["learned_mis_n8_m64"] = learned_case(torch, _native, random_unitary, 64, 8, 20000, 10, 2048, 4096,
+                                             4_000_000, mis_batch=16384)
     # small case: SLOS m=12, n=6 and 1000 Naive amplitudes (latency-bound)
     from perceval_gb300 import BackendFactory, BasicState
     U12 = random_unitary(12, seed=0)
@@ -773,7 +776,7 @@ def secondary(torch, _native, random_unitary, dev, flush, fp64_peak_tflops):
 
 
 def learned_case(torch, _native, random_unitary, m, n, n_train, epochs, chains, steps, n_ref, tvd=True,
-                 marginal_modes=8, n_ref64=None):
+                 marginal_modes=8, n_ref64=None, mis_batch=512, tvd_samples=25600):
     """Learned-proposal Metropolised sampler against the plain GPU exact sampler on one
     Haar unitary (seed 0, input photons in modes 0..n-1).
 
@@ -784,13 +787,16 @@ def learned_case(torch, _native, random_unitary, m, n, n_train, epochs, chains, 
     one-mode distributions P(n_i = a) of the most occupied modes and two-mode
     distributions P(n_i = a, n_j = b) of pairs among them (generating-function
     permanents, perceval_gb300.marginals) against each sampler's empirical ones, with
-    the binomial standard error of the largest probability at that sample count."""
+    the binomial standard error of the largest probability at that sample count (for the
+    MIS, at its ESS)."""
     from perceval_gb300.learned import ProposalMLP, ess, exact_moments, run_mis, tvd_estimate
     from perceval_gb300.marginals import (empirical_one_mode, empirical_two_mode, one_mode_marginal,
                                           two_mode_marginal)
     U = random_unitary(m, seed=0)
     inp = [1] * n + [0] * (m - n)
     Ud = torch.from_numpy(U).cuda()
+    A, E2 = exact_moments(U, inp)
+    modes = [int(i) for i in np.argsort(-A)[:marginal_modes]]
     t0 = time.perf_counter()
     train = _native.cc2017_sample(Ud, inp, n_train, seed=101, precision=1).cpu().numpy()
     t_train_samples = time.perf_counter() - t0
@@ -800,55 +806,60 @@ def learned_case(torch, _native, random_unitary, m, n, n_train, epochs, chains, 
     losses = net.train(train[n_val:], epochs=epochs, batch=256, lr=1e-3, val=train[:n_val])
     torch.cuda.synchronize()
     t_fit = time.perf_counter() - t0
-    res = run_mis(net, U, inp, chains=chains, steps=steps, seed=7, batch=512)
+    res = run_mis(net, U, inp, chains=chains, steps=steps, seed=7, batch=mis_batch)
     ess_mis = float(sum(ess(x) for x in res.log_pi))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    ref = _native.cc2017_sample(Ud, inp, n_ref, seed=202, precision=0).cpu().numpy()
-    t_ref = time.perf_counter() - t0
-    # the same sampler with native FP64 sub-permanent sums, the acceptance's arithmetic
-    n_ref64 = n_ref if n_ref64 is None else n_ref64
-    t0 = time.perf_counter()
-    ref64 = _native.cc2017_sample(Ud, inp, n_ref64, seed=303, precision=2).cpu().numpy()
-    t_ref64 = time.perf_counter() - t0
-    A, E2 = exact_moments(U, inp)
-    st = res.samples.reshape(-1, m)
-    modes = [int(i) for i in np.argsort(-A)[:marginal_modes]]
-    one = {i: one_mode_marginal(U, inp, i) for i in modes}
-    pairs = [(modes[a], modes[b]) for a in range(len(modes)) for b in range(a + 1, len(modes))][:12]
-    two = {p: two_mode_marginal(U, inp, *p) for p in pairs}
+    seqs = res.sequences.reshape(-1, n)
+    mis_occ = np.stack([(seqs == i).sum(axis=1) for i in modes], axis=1)
+    mis_mean = np.bincount(seqs.reshape(-1).astype(np.int64), minlength=m)[:m] / len(seqs)
 
-    def marg_err(samples):
-        e1 = max(float(np.abs(empirical_one_mode(samples, i, n) - one[i]).max()) for i in modes)
-        e2 = max(float(np.abs(empirical_two_mode(samples, i, j, n) - two[(i, j)]).max()) for i, j in pairs)
+    def exact(count, seed, precision):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        x = _native.cc2017_sample(Ud, inp, count, seed=seed, precision=precision)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        return dt, x[:, modes].cpu().numpy(), x.double().mean(0).cpu().numpy(), x[:tvd_samples].cpu().numpy()
+    t_ref, ref_occ, ref_mean, ref_head = exact(n_ref, 202, 0)
+    # the same sampler in its FP64 mode, the acceptance's arithmetic
+    n_ref64 = n_ref if n_ref64 is None else n_ref64
+    t_ref64, ref64_occ, ref64_mean, _ = exact(n_ref64, 303, 2)
+    one = {i: one_mode_marginal(U, inp, i) for i in modes}
+    pairs = [(a, b) for a in range(len(modes)) for b in range(a + 1, len(modes))][:12]
+    two = {p: two_mode_marginal(U, inp, modes[p[0]], modes[p[1]]) for p in pairs}
+
+    def marg_err(occ, eff=None):
+        # occ: occupations of the selected modes (column k = mode modes[k])
+        e1 = max(float(np.abs(empirical_one_mode(occ, k, n) - one[i]).max()) for k, i in enumerate(modes))
+        e2 = max(float(np.abs(empirical_two_mode(occ, a, b, n) - two[(a, b)]).max()) for a, b in pairs)
         pmax = max(float(one[i].max()) for i in modes)
-        return {"max_abs_err_one_mode": e1, "max_abs_err_two_mode": e2, "samples": int(len(samples)),
-                "binomial_stderr_at_max_p": math.sqrt(pmax * (1 - pmax) / len(samples))}
+        neff = len(occ) if eff is None else eff
+        return {"max_abs_err_one_mode": e1, "max_abs_err_two_mode": e2, "samples": int(len(occ)),
+                "binomial_stderr_at_max_p": math.sqrt(pmax * (1 - pmax) / neff)}
     row = {"m": m, "n": n, "train_samples": n_train, "train_sampling_s": t_train_samples,
            "fit_s": t_fit, "nll_first_last": [losses[0], losses[-1]],
            "held_out_nll": net.val_nll, "kept_epoch": net.best_epoch,
            "mis": {"chains": chains, "steps": steps, "proposals": res.proposals, "seconds": res.seconds,
                    "acceptance_arithmetic": "fp64 permanents",
                    "accept_rate": res.accept_rate, "ess": ess_mis, "ess_per_s": ess_mis / res.seconds,
-                   "max_abs_err_E_n": float(np.abs(st.astype(float).mean(0) - A).max()),
-                   "marginals": marg_err(st)},
+                   "max_abs_err_E_n": float(np.abs(mis_mean - A).max()),
+                   "marginals": marg_err(mis_occ, ess_mis)},
            "exact_sampler": {"samples": n_ref, "seconds": t_ref, "ess_per_s": n_ref / t_ref,
                              "arithmetic": "float-float",
-                             "max_abs_err_E_n": float(np.abs(ref.astype(float).mean(0) - A).max()),
-                             "marginals": marg_err(ref)},
+                             "max_abs_err_E_n": float(np.abs(ref_mean - A).max()),
+                             "marginals": marg_err(ref_occ)},
            "exact_sampler_fp64": {"samples": n_ref64, "seconds": t_ref64, "ess_per_s": n_ref64 / t_ref64,
                                   "arithmetic": "fp64",
-                                  "max_abs_err_E_n": float(np.abs(ref64.astype(float).mean(0) - A).max()),
-                                  "marginals": marg_err(ref64)},
-           "marginal_modes": modes, "marginal_pairs": [list(p) for p in pairs]}
+                                  "max_abs_err_E_n": float(np.abs(ref64_mean - A).max()),
+                                  "marginals": marg_err(ref64_occ)},
+           "marginal_modes": modes, "marginal_pairs": [[modes[a], modes[b]] for a, b in pairs]}
     row["ess_per_s_ratio"] = row["mis"]["ess_per_s"] / row["exact_sampler"]["ess_per_s"]
     row["ess_per_s_ratio_vs_fp64_exact"] = row["mis"]["ess_per_s"] / row["exact_sampler_fp64"]["ess_per_s"]
     if tvd:
         # TVD(q, pi) on photon sequences from the exact samples: trained vs untrained network
         untrained = ProposalMLP(m, n, D=128, H=512, layers=3, seed=0)
-        t, te = tvd_estimate(net, U, inp, ref, seed=5)
-        u0, ue = tvd_estimate(untrained, U, inp, ref, seed=5)
-        row["tvd_q_pi_sequences"] = {"samples": int(len(ref)), "trained": t, "trained_stderr": te,
+        t, te = tvd_estimate(net, U, inp, ref_head, seed=5)
+        u0, ue = tvd_estimate(untrained, U, inp, ref_head, seed=5)
+        row["tvd_q_pi_sequences"] = {"samples": int(len(ref_head)), "trained": t, "trained_stderr": te,
                                      "untrained": u0, "untrained_stderr": ue}
     return row
 

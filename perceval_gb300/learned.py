@@ -223,11 +223,12 @@ def counts_to_sequences(samples: np.ndarray, rng: np.random.Generator) -> list[n
 
 
 def sequences_to_counts(seq: np.ndarray, m: int) -> np.ndarray:
+    """Occupation counts (rows x m) of photon sequences (rows x n)."""
     seq = np.asarray(seq)
-    out = np.zeros((seq.shape[0], m), dtype=np.int32)
-    for i, s in enumerate(seq):
-        np.add.at(out[i], s, 1)
-    return out
+    rows = seq.reshape(-1, seq.shape[-1])
+    out = np.zeros((rows.shape[0], m), dtype=np.int32)
+    np.add.at(out, (np.repeat(np.arange(rows.shape[0]), rows.shape[1]), rows.reshape(-1).astype(np.int64)), 1)
+    return out.reshape(seq.shape[:-1] + (m,))
 
 
 _PERM_PLANS: dict = {}
@@ -259,11 +260,17 @@ def log_abs_perm2(U_dev: torch.Tensor, cols: np.ndarray, seq: torch.Tensor) -> n
 
 @dataclass
 class MISResult:
-    samples: np.ndarray            # chain states (counts), chains x steps x m
+    sequences: np.ndarray          # chain states as photon sequences, chains x steps x n
+    m: int
     accept_rate: float
     proposals: int
     seconds: float
     log_pi: np.ndarray = field(default_factory=lambda: np.zeros(0))
+
+    @property
+    def samples(self) -> np.ndarray:
+        """Chain states as occupation counts, chains x steps x m."""
+        return sequences_to_counts(self.sequences, self.m)
 
 
 def run_mis(proposal: ProposalMLP, U: np.ndarray, input_state, chains: int, steps: int, seed: int = 0,
@@ -287,21 +294,25 @@ def run_mis(proposal: ProposalMLP, U: np.ndarray, input_state, chains: int, step
     seq = np.concatenate(seqs).reshape(chains, steps + 1, -1)
     lq = np.concatenate(logq).reshape(chains, steps + 1)
     lp = np.concatenate(logpi).reshape(chains, steps + 1)
-    states = np.empty((chains, steps, seq.shape[2]), dtype=np.int32)
+    # the accept / reject scan, all chains at once (uniform u[c, t] in the order of a
+    # chain-by-chain scan)
+    u = np.log(rng.random((chains, steps)))
+    lw = lp - lq
+    cur = np.zeros(chains, dtype=np.int64)  # index of each chain's current proposal
+    cur_lw = lw[:, 0].copy()
+    state_idx = np.empty((chains, steps), dtype=np.int64)
     state_lp = np.empty((chains, steps))
     accepted = 0
-    for c in range(chains):
-        cur, cur_lw = seq[c, 0], lp[c, 0] - lq[c, 0]
-        for t in range(steps):
-            prop_lw = lp[c, t + 1] - lq[c, t + 1]
-            if np.log(rng.random()) < prop_lw - cur_lw:
-                cur, cur_lw = seq[c, t + 1], prop_lw
-                accepted += 1
-            states[c, t] = cur
-            state_lp[c, t] = cur_lw
+    for t in range(steps):
+        acc = u[:, t] < lw[:, t + 1] - cur_lw
+        accepted += int(acc.sum())
+        cur = np.where(acc, t + 1, cur)
+        cur_lw = np.where(acc, lw[:, t + 1], cur_lw)
+        state_idx[:, t] = cur
+        state_lp[:, t] = cur_lw
+    states = seq[np.arange(chains)[:, None], state_idx]
     secs = time.perf_counter() - t0
-    counts = np.stack([sequences_to_counts(states[c], m) for c in range(chains)])
-    return MISResult(counts, accepted / (chains * steps), total, secs, state_lp)
+    return MISResult(states, m, accepted / (chains * steps), total, secs, state_lp)
 
 
 def tvd_estimate(proposal: "ProposalMLP", U: np.ndarray, input_state, exact_counts: np.ndarray,
