@@ -1019,9 +1019,10 @@ def profile_case(name: str):
         B = torch.randn(N, K, device="cuda").to(torch.bfloat16)
         C = torch.empty(M, N, device="cuda", dtype=torch.float32)
         _native.gemm_bf16(A, B, M, N, K, K, K, C=C)
-    elif name == "cc2017":
+    elif name in ("cc2017", "cc2017fp64"):
+        # n = 20 photons on m = 400, 608 samples (float-float, or the FP64 mode)
         U4 = torch.from_numpy(random_unitary(400, seed=0)).to(dev)
-        _native.cc2017_sample(U4, [1] * 20 + [0] * 380, 608, seed=1)
+        _native.cc2017_sample(U4, [1] * 20 + [0] * 380, 608, seed=1, precision=2 if name == "cc2017fp64" else 0)
     else:
         raise SystemExit(f"unknown profile case {name}")
     torch.cuda.synchronize()
@@ -1041,7 +1042,7 @@ def main():
     ap.add_argument("--large-perm", action="store_true",
                     help="one n = 40 permanent in FP64 and in float-float (about three minutes)")
     ap.add_argument("--profile-case", choices=["perm24", "perm24dadd", "perm24ff", "slos20", "slos20ff", "slos20p", "slosmask22", "slap1024", "slos16b256",
-                                               "cc2017", "gurvits20", "gemm"],
+                                               "cc2017", "cc2017fp64", "gurvits20", "gemm"],
                     help="run one small untimed case of a single kernel (for ncu) and exit")
     args = ap.parse_args()
     if args.profile_case:
