@@ -30,6 +30,8 @@
 //   cc_draw_kernel  one CTA per sample: adds the chunk partials, undoes the column
 //                   scaling, forms w_i in FP64 for every mode, and a block scan over
 //                   the modes locates the draw.
+// The sub-permanents run in one of three arithmetic policies: float-float (ArDD, the
+// default), FP64 precision on the integer pipes (ArFX) or FP32 (ArF32).
 #include <algorithm>
 #include <climits>
 #include <cstring>

@@ -8,17 +8,21 @@
 // so Y = X W^T (forward), dX = dY W (transB), dW = dY^T X (transA, transB) are all one
 // kernel with the weight matrices in torch Linear layout (out x in, row-major).
 //
-// The GEMM runs on the 5th-generation tensor cores: one CTA (4 warps) per 128 x 128
-// tile of C with the FP32 accumulator in tensor memory (128 lanes x 128 columns).  Per
-// 64-wide K step the CTA stages the A and B tiles in shared memory in the canonical
-// K-major layout without swizzle (8 x 16-byte core matrices; 128 B between core
-// matrices along K, 1024 B between 8-row groups), then one thread issues four
-// tcgen05.mma.kind::f16 (M = 128, N = 128, K = 16) with BF16 inputs and commits them to
-// an mbarrier.  Three stages filled by 16-byte cp.async: the tiles of steps k + 1 and
-// k + 2 are in flight while the MMAs of step k run.  The epilogue reads the accumulator with tcgen05.ld (warp w owns TMEM lanes
-// 32w..32w+31 = rows of the tile) and applies alpha, beta, bias and GELU.  Every mbarrier
-// wait is bounded; a CTA whose wait gives up waits (bounded) for its last commit, frees
-// its tensor memory and writes NaN to its tile.
+// The GEMM runs on the 5th-generation tensor cores.  Operands whose rows start on
+// 16-byte boundaries (either layout) go to gemm_tma_persistent: TMA-loaded 128-byte
+// swizzled tiles, one tcgen05.mma issuer, two 128-column FP32 accumulators in tensor
+// memory and four epilogue warps per CTA, two CTAs per SM walking the output tiles (see
+// its comment below).  Others go to gemm_tc_kernel: one CTA (4 warps) per 128 x 128 tile
+// of C with the FP32 accumulator in tensor memory (128 lanes x 128 columns); per 64-wide
+// K step the CTA stages the A and B tiles in shared memory in the canonical K-major
+// layout without swizzle (8 x 16-byte core matrices; 128 B between core matrices along
+// K, 1024 B between 8-row groups), then one thread issues four tcgen05.mma.kind::f16
+// (M = 128, N = 128, K = 16) with BF16 inputs and commits them to an mbarrier; three
+// stages filled by 16-byte cp.async keep the tiles of steps k + 1 and k + 2 in flight
+// while the MMAs of step k run.  Both epilogues read the accumulator with tcgen05.ld
+// (warp w owns TMEM lanes 32 (w % 4) .. +31 = rows of the tile) and apply alpha, beta,
+// bias and GELU.  Every mbarrier wait is bounded; a CTA whose wait gives up waits
+// (bounded) for what it issued, frees its tensor memory and writes NaN to its tiles.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>

@@ -21,9 +21,10 @@
 // factors.
 //
 // Three arithmetics share this layout (16 bytes per prepared element in each):
-//  * FP64 (perm_bin_fx, the default): exact fixed-point row sums on the integer pipe,
-//    each converted once to FP64; the product tree by DMUL/DFMA with the last product
-//    fused into the signed accumulation; each hi pattern's lo sweep added to a
+//  * FP64 precision (perm_bin_fx, the default): exact fixed-point row sums on the
+//    integer pipe; each sign vector's product split between an FP64 DMUL/DFMA tree and
+//    a 64-bit block-floating tree on the integer pipes (blockfloat.cuh), the two halves
+//    meeting in the signed accumulation; each hi pattern's lo sweep added to a
 //    Neumaier-compensated FP64 sum.  The hi patterns of a thread are walked in
 //    Gray-code order, so consecutive patterns differ in one column.
 //  * FP64 with FP64 row sums (perm_bin_f64): the same with the row sums and their
