@@ -620,10 +620,10 @@ def secondary(torch, _native, random_unitary, dev, flush, fp64_peak_tflops):
     res["cc2017_64_inputs_m64_n6"] = {"samples": 64000, "one_wavefront_ms": t_many, "per_input_loop_ms": t_loop,
                                       "samples_per_s": 64000 / (t_many * 1e-3)}
     # the learned-proposal sampler, bounded for the default run: n = 30, m = 900 trained on
-    # 1024 exact samples (FP32 sampler), 8 chains x 8 steps of FP64-permanent acceptances
+    # 1024 exact samples (FP32 sampler), 8 chains x 16 steps of FP64-permanent acceptances
     # against 96 exact float-float samples and 32 exact FP64 samples; and the n = 8, m = 64
     # companion
-    res["learned_mis_n30_m900"] = learned_case(torch, _native, random_unitary, 900, 30, 1024, 4, 8, 8, 96,
+    res["learned_mis_n30_m900"] = learned_case(torch, _native, random_unitary, 900, 30, 1024, 4, 8, 16, 96,
                                                tvd=False, n_ref64=32)
     # n = 8, m = 64 with enough samples of both samplers to resolve the marginals to 1e-3:
     # 2048 chains x 4096 steps (8.4 M proposals) and 4 M exact samples
