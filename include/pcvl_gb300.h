@@ -87,8 +87,8 @@ int pcvl_permanent_batch(const double* mats_d, const int64_t* offsets_h, const i
  * (pcvl_perm_set_tuning) can reach it with a few large matrices in each of many size
  * bins.  Larger requests are refused with PCVL_ERR_ARG and a message naming the
  * limit.  The first call on a device looks up the scratch's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.  Every
- * call copies its descriptors (about 24 bytes per matrix) from a static host buffer.
+ * (cudaGetSymbolAddress).  Every call copies its descriptors (about 24 bytes per
+ * matrix) from a static host buffer.
  * Every call reuses the same scratch and
  * rewrites every part of it that it reads, so nothing needs clearing; but calls whose
  * GPU work overlaps (different streams, or different host threads without ordering)
