@@ -142,8 +142,12 @@ _PREC_NAMES = {"fp64": PREC_FP64, "float64": PREC_FP64, "float-float": PREC_FLOA
 
 
 def precision_code(precision) -> int:
-    """ABI code of a precision given as a code or a name ("fp64", "float-float", "fp32";
-    permanents also take "fp64-dadd": FP64 with the row sums in FP64 additions too)."""
+    """ABI code of a precision given as a code or a name.  "fp64" (the default
+    everywhere): FP64 precision, no step rounding more coarsely than an FP64 operation
+    (permanents and the sampler take exact fixed-point sums and run part of their products
+    in 64-bit block floating point on the integer pipes); "float-float": pairs of FP32
+    numbers, about 48 significant bits, faster; "fp32": the sampler's FP32 mode;
+    "fp64-dadd" (permanents): every row sum and product an FP64 operation."""
     if isinstance(precision, str):
         try:
             return _PREC_NAMES[precision.lower()]
