@@ -156,7 +156,8 @@ def traffic_from_profile(name: str):
 # ----------------------------------------------------------------------------- CPU
 def cpu_perm_baseline(budget_s: float = 15.0) -> dict:
     """The host-tuned FP64 Glynn of the CPU restatement (C, OpenMP over every (matrix,
-    chunk) task on all host threads, vectorisable row-sum updates) on a stratified sample:
+    chunk) task on all host threads, sixteen Gray-code steps at once in vector lanes) on a
+    stratified sample:
     per size n, batches of the batch's own matrices of that size, doubling until they take
     about budget / 17 seconds; the full-batch time is extrapolated by the size counts."""
     from oracle import oracle
@@ -212,7 +213,7 @@ def cpu_context() -> dict:
     U64 = random_unitary(64, seed=0)
     out["all_outputs_m64_n4_ms"] = 1e3 * t(lambda: oracle.slos(U64, [1] * 4 + [0] * 60))
     U400 = random_unitary(400, seed=0)
-    ns = 4 * oracle.num_threads()
+    ns = 32 * oracle.num_threads()
     # the sampler in parallel over samples, all k sub-permanents of a step from one Glynn sum
     out["cc2017_n20_m400_samples_per_s"] = ns / t(lambda: oracle.cc2017_fast(U400, [1] * 20 + [0] * 380, ns, seed=1))
     Ubig = random_unitary(1024, seed=0)

@@ -105,8 +105,8 @@ def perm_batch(mats: np.ndarray, offsets, sizes, method: str = "glynn") -> np.nd
 
 def perm_batch_fast(mats: np.ndarray, offsets, sizes) -> np.ndarray:
     """Glynn permanents of a packed batch by the host-tuned path (the CPU baseline):
-    vectorisable row-sum updates, four product chains, one OpenMP task per 2^12-step
-    chunk of every matrix, chunks added in order with compensation (FP64)."""
+    sixteen consecutive Gray-code steps at once in vector lanes, one OpenMP task per
+    2^12-step chunk of every matrix, chunks added in order with compensation (FP64)."""
     mats = _c128(mats)
     offsets = np.ascontiguousarray(offsets, dtype=np.int64)
     sizes = _i32(sizes)
@@ -118,7 +118,8 @@ def perm_batch_fast(mats: np.ndarray, offsets, sizes) -> np.ndarray:
 
 def cc2017_fast(U, input_state, count: int, seed: int, first: int = 0) -> np.ndarray:
     """Clifford & Clifford samples drawn in parallel over samples, the k sub-permanents of
-    a step from one Glynn sum (the CPU baseline; same Philox stream and draws as cc2017)."""
+    a step from one Glynn sum over sixteen Gray-code steps at once in vector lanes (the CPU
+    baseline; same Philox stream and draws as cc2017)."""
     U = _c128(U)
     m = U.shape[0]
     inp = _i32(input_state)

@@ -544,11 +544,12 @@ void oracle_set_threads(int t) {
  *
  * Batched Glynn: the sign vectors of every matrix are cut into chunks of 2^12 consecutive
  * Gray-code steps; one OpenMP task per (matrix, chunk), so small matrices use every core
- * too.  Within a chunk the row sums live as separate real and imaginary arrays, so the
- * update of a step (one column, +-2 a_ij for every row) is one vectorisable loop, and
- * the product of the n row sums runs as four independent chains.  A chunk's terms are
- * summed plainly; the chunks of a matrix are added in order with Neumaier compensation,
- * so results do not depend on the thread count.  FP64 throughout. */
+ * too.  For n >= 5 a chunk runs sixteen consecutive steps at once in vector lanes
+ * (glynn_chunk16); for n <= 4 one step at a time (glynn_chunk: the row sums as separate
+ * real and imaginary arrays, the update of a step one vectorisable loop, the product in
+ * four independent chains).  A chunk's terms are summed plainly; the chunks of a matrix
+ * are added in order with Neumaier compensation, so results do not depend on the thread
+ * count.  FP64 throughout. */
 /* Multiply-adds may fuse (FMA) here: this is the timed baseline, not the pinned restatement. */
 __attribute__((optimize("fp-contract=fast")))
 static void glynn_chunk(int n, const double* ar, const double* ai, uint64_t g0, uint64_t g1, double* rr, double* ri,
@@ -608,6 +609,84 @@ static void glynn_chunk(int n, const double* ar, const double* ai, uint64_t g0, 
   out[1] = si;
 }
 
+/* Sixteen consecutive Gray-code steps k..k+15 (k a multiple of 16) at once, as eight
+ * two-lane vectors per row (GCC's generic vectors; one 128-bit operation each on NEON and
+ * SSE2).  The lanes start as the row sums of the sixteen steps, walked from k.  The Gray code
+ * is reflected: the next block's steps are this block's in reverse order with one more
+ * column flipped, t = ctz(k + 16) >= 4, so the lanes stay in place, each block adds
+ * +-x_{t+1} to all of them, and the lane order, hence the lanes' sign-vector parities, alternates
+ * from block to block (the parity of gray(j) is that of j: +, - within each vector in step
+ * order).  Per row and block: one column update and one complex multiply per lane, sixteen
+ * independent product chains. */
+typedef double v2d __attribute__((vector_size(16)));
+enum { kGlynnVecs = 8, kGlynnLanes = 2 * kGlynnVecs };
+
+__attribute__((optimize("fp-contract=fast")))
+static void glynn_chunk16(int n, const double* ar, const double* ai, uint64_t g0, uint64_t g1, v2d* lr, v2d* li,
+                          double* out) {
+  const uint64_t gc0 = g0 ^ (g0 >> 1);
+  for (int i = 0; i < n; ++i) {
+    double vr = 0.5 * ar[i], vi = 0.5 * ai[i];
+    for (int j = 1; j < n; ++j) {
+      const double s = ((gc0 >> (j - 1)) & 1) ? -0.5 : 0.5;
+      vr += s * ar[j * n + i];
+      vi += s * ai[j * n + i];
+    }
+    double er[kGlynnLanes], ei[kGlynnLanes];
+    uint64_t gc = gc0;
+    er[0] = vr;
+    ei[0] = vi;
+    for (int l = 1; l < kGlynnLanes; ++l) {
+      const int t = __builtin_ctzll(g0 + l);
+      gc ^= 1ull << t;
+      const double c = ((gc >> t) & 1) ? -1.0 : 1.0;
+      vr += c * ar[(t + 1) * n + i];
+      vi += c * ai[(t + 1) * n + i];
+      er[l] = vr;
+      ei[l] = vi;
+    }
+    for (int q = 0; q < kGlynnVecs; ++q) {
+      lr[kGlynnVecs * i + q] = (v2d){er[2 * q], er[2 * q + 1]};
+      li[kGlynnVecs * i + q] = (v2d){ei[2 * q], ei[2 * q + 1]};
+    }
+  }
+  const v2d one = {1, 1}, zero = {0, 0};
+  v2d ls = {1, -1}, sr = zero, si = zero;
+  for (uint64_t k = g0; k < g1; k += kGlynnLanes) {
+    double cn = 0;
+    const double *xr = ar + n, *xi = ai + n;
+    if (k > g0) {
+      const int t = __builtin_ctzll(k);
+      cn = (((k ^ (k >> 1)) >> t) & 1) ? -1.0 : 1.0;
+      xr = ar + (size_t)(t + 1) * n;
+      xi = ai + (size_t)(t + 1) * n;
+      ls = -ls;
+    }
+    v2d pr[kGlynnVecs], pi[kGlynnVecs];
+    for (int q = 0; q < kGlynnVecs; ++q) {
+      pr[q] = one;
+      pi[q] = zero;
+    }
+    for (int i = 0; i < n; ++i) {
+      const double dr = cn * xr[i], di = cn * xi[i];
+      for (int q = 0; q < kGlynnVecs; ++q) {
+        const v2d u = lr[kGlynnVecs * i + q] + dr, v = li[kGlynnVecs * i + q] + di;
+        lr[kGlynnVecs * i + q] = u;
+        li[kGlynnVecs * i + q] = v;
+        const v2d x = pr[q];
+        pr[q] = x * u - pi[q] * v;
+        pi[q] = x * v + pi[q] * u;
+      }
+    }
+    for (int q = 0; q < kGlynnVecs; ++q) {
+      sr += ls * pr[q];
+      si += ls * pi[q];
+    }
+  }
+  out[0] = sr[0] + sr[1];
+  out[1] = si[0] + si[1];
+}
+
 void oracle_perm_batch_fast(const double* mats, const int64_t* offs, const int32_t* sizes, int count, double* out) {
   const uint64_t chunk = 1ull << 12;
   int64_t* first = (int64_t*)malloc(sizeof(int64_t) * (count + 1));
@@ -622,6 +701,7 @@ void oracle_perm_batch_fast(const double* mats, const int64_t* offs, const int32
 #pragma omp parallel
   {
     double* buf = (double*)malloc(sizeof(double) * (4 * 40 + 4 * 40 * 40));
+    v2d* lanes = (v2d*)aligned_alloc(16, sizeof(v2d) * 2 * kGlynnVecs * 40);
     int cur = -1;
     double *ar = buf + 160, *ai = ar + 1600, *rr = buf, *ri = buf + 40;
 #pragma omp for schedule(dynamic, 1)
@@ -645,9 +725,13 @@ void oracle_perm_batch_fast(const double* mats, const int64_t* offs, const int32
       const uint64_t total = 1ull << (n - 1);
       const uint64_t g0 = (uint64_t)(q - first[mat]) * chunk;
       const uint64_t g1 = g0 + chunk < total ? g0 + chunk : total;
-      glynn_chunk(n, ar, ai, g0, g1, rr, ri, part + 2 * q);
+      if (n >= 5)  /* chunks of 2^12 steps or of the whole 2^(n-1): multiples of 16 */
+        glynn_chunk16(n, ar, ai, g0, g1, lanes, lanes + kGlynnVecs * 40, part + 2 * q);
+      else
+        glynn_chunk(n, ar, ai, g0, g1, rr, ri, part + 2 * q);
     }
     free(buf);
+    free(lanes);
   }
   for (int i = 0; i < count; ++i) {
     const int n = sizes[i];
@@ -720,6 +804,100 @@ static void sub_perms_all(int k, const cplx* U, int m, const int* rows, const in
   for (int l = 0; l < k; ++l) sub[l] = ldexp(accr[l], -(d - 1)) + I * ldexp(acci[l], -(d - 1));
 }
 
+/* The same sum with 2 kSubVecs consecutive Gray-code steps in vector lanes (kSubVecs two-lane
+ * vectors per column; as glynn_chunk16 does for permanents): the lanes start as the column
+ * sums of steps 0, 1, ..., walked from t = 0; each later block adds +-x_{b+1}, b = ctz(t)
+ * (x_i = 2 U[row_i, cols]), to every lane and reverses the lanes' step order, hence their
+ * parity pattern.  Per block the prefix and suffix products run as 2 kSubVecs independent
+ * chains.  For k >= kSubMinK (at least one block of steps). */
+enum { kSubVecs = 8, kSubLanes = 2 * kSubVecs, kSubMinK = 6 };  /* 2^(kSubMinK - 2) = kSubLanes */
+
+__attribute__((optimize("fp-contract=fast")))
+static void sub_perms_lanes(int k, const cplx* U, int m, const int* rows, const int* cols, cplx* sub) {
+  const int d = k - 1, V = kSubVecs;
+  double ur[d * k], ui[d * k];  /* 2 U[rows[i], cols[j]] */
+  for (int i = 0; i < d; ++i)
+    for (int j = 0; j < k; ++j) {
+      const cplx z = U[rows[i] * m + cols[j]];
+      ur[i * k + j] = 2.0 * creal(z);
+      ui[i * k + j] = 2.0 * cimag(z);
+    }
+  v2d cr[k * V], ci[k * V], pr[(k + 1) * V], pi[(k + 1) * V], ar[k * V], ai[k * V];
+  const v2d one = {1, 1}, zero = {0, 0};
+  for (int j = 0; j < k; ++j) {
+    double er[kSubLanes], ei[kSubLanes];
+    double vr = 0, vi = 0;
+    for (int i = 0; i < d; ++i) {
+      vr += 0.5 * ur[i * k + j];
+      vi += 0.5 * ui[i * k + j];
+    }
+    uint64_t gc = 0;
+    er[0] = vr;
+    ei[0] = vi;
+    for (int l = 1; l < kSubLanes; ++l) {
+      const int b = __builtin_ctzll((uint64_t)l);
+      gc ^= 1ull << b;
+      const double c = ((gc >> b) & 1) ? -1.0 : 1.0;
+      vr += c * ur[(b + 1) * k + j];
+      vi += c * ui[(b + 1) * k + j];
+      er[l] = vr;
+      ei[l] = vi;
+    }
+    for (int q = 0; q < V; ++q) {
+      cr[j * V + q] = (v2d){er[2 * q], er[2 * q + 1]};
+      ci[j * V + q] = (v2d){ei[2 * q], ei[2 * q + 1]};
+      ar[j * V + q] = ai[j * V + q] = zero;
+    }
+  }
+  v2d ls = {1, -1};
+  const uint64_t total = 1ull << (d - 1);
+  for (uint64_t t = 0; t < total; t += kSubLanes) {
+    if (t > 0) {
+      const int b = __builtin_ctzll(t);
+      const double c = (((t ^ (t >> 1)) >> b) & 1) ? -1.0 : 1.0;
+      const double *xr = ur + (size_t)(b + 1) * k, *xi = ui + (size_t)(b + 1) * k;
+      for (int j = 0; j < k; ++j) {
+        const double dr = c * xr[j], di = c * xi[j];
+        for (int q = 0; q < V; ++q) {
+          cr[j * V + q] += dr;
+          ci[j * V + q] += di;
+        }
+      }
+      ls = -ls;
+    }
+    v2d Pr[kSubVecs], Pi[kSubVecs], Sr[kSubVecs], Si[kSubVecs];
+    for (int q = 0; q < V; ++q) {
+      Pr[q] = Sr[q] = pr[q] = one;
+      Pi[q] = Si[q] = pi[q] = zero;
+    }
+    for (int j = 0; j < k; ++j)  /* prefix products */
+      for (int q = 0; q < V; ++q) {
+        const v2d x = Pr[q], u = cr[j * V + q], v = ci[j * V + q];
+        Pr[q] = x * u - Pi[q] * v;
+        Pi[q] = x * v + Pi[q] * u;
+        pr[(j + 1) * V + q] = Pr[q];
+        pi[(j + 1) * V + q] = Pi[q];
+      }
+    for (int j = k - 1; j >= 0; --j)  /* suffix products, and prefix x suffix into the sums */
+      for (int q = 0; q < V; ++q) {
+        const v2d a = pr[j * V + q], b = pi[j * V + q];
+        ar[j * V + q] += ls * (a * Sr[q] - b * Si[q]);
+        ai[j * V + q] += ls * (a * Si[q] + b * Sr[q]);
+        const v2d x = Sr[q], u = cr[j * V + q], v = ci[j * V + q];
+        Sr[q] = x * u - Si[q] * v;
+        Si[q] = x * v + Si[q] * u;
+      }
+  }
+  for (int l = 0; l < k; ++l) {
+    v2d tr = zero, ti = zero;
+    for (int q = 0; q < V; ++q) {
+      tr += ar[l * V + q];
+      ti += ai[l * V + q];
+    }
+    sub[l] = ldexp(tr[0] + tr[1], -(d - 1)) + I * ldexp(ti[0] + ti[1], -(d - 1));
+  }
+}
+
 void oracle_cc2017_fast(const double* U_, int m, const int* in, int64_t count, uint64_t seed, uint64_t first,
                         int32_t* out) {
   const cplx* U = (const cplx*)U_;
@@ -747,7 +925,10 @@ void oracle_cc2017_fast(const double* U_, int m, const int* in, int64_t count, u
         cols[j] = t;
       }
       for (int k = 1; k <= n; ++k) {
-        sub_perms_all(k, U, m, rows, cols, sub);
+        if (k >= kSubMinK)
+          sub_perms_lanes(k, U, m, rows, cols, sub);
+        else
+          sub_perms_all(k, U, m, rows, cols, sub);
         double W = 0;
         for (int i = 0; i < m; ++i) {
           cplx z = 0;
