@@ -190,9 +190,10 @@ def cpu_perm_baseline(budget_s: float = 15.0) -> dict:
 
 
 def cpu_context() -> dict:
-    """The oracle (C; SLOS, permanents and the exact sampler with OpenMP on all host
-    threads, the Gurvits estimator on one thread) on bounded samples of the secondary
-    workloads, for context beside the GPU lines: about 20 s of host time."""
+    """The oracle's host-tuned paths (C; SLOS and its gradient, permanents and the exact
+    sampler with OpenMP on all host threads, the Gurvits estimator on one thread) on bounded
+    samples of the secondary workloads, for context beside the GPU lines: a few seconds of
+    host time."""
     from oracle import oracle
     from perceval_gb300.utils.matrix import random_unitary
     out = {"threads_openmp": oracle.num_threads()}
@@ -202,16 +203,16 @@ def cpu_context() -> dict:
         fn()
         return time.perf_counter() - t0
     U12 = random_unitary(12, seed=0)
-    out["slos_m12_n6_ms"] = 1e3 * t(lambda: oracle.slos(U12, [1] * 6 + [0] * 6))
+    out["slos_m12_n6_ms"] = 1e3 * t(lambda: oracle.slos_fast(U12, [1] * 6 + [0] * 6))
     U20 = random_unitary(20, seed=0)
-    out["slos_m20_n10_ms"] = 1e3 * t(lambda: oracle.slos(U20, [1] * 10 + [0] * 10))
+    out["slos_m20_n10_ms"] = 1e3 * t(lambda: oracle.slos_fast(U20, [1] * 10 + [0] * 10))
     U16 = random_unitary(16, seed=0)
     inp16 = [1] * 8 + [0] * 8
-    out["slos_m16_n8_one_circuit_ms"] = 1e3 * t(lambda: oracle.slos(U16, inp16))
+    out["slos_m16_n8_one_circuit_ms"] = 1e3 * t(lambda: oracle.slos_fast(U16, inp16))
     w = np.random.default_rng(1).normal(size=math.comb(23, 8))
-    out["slos_grad_m16_n8_one_circuit_ms"] = 1e3 * t(lambda: oracle.slos_grad(U16, inp16, w))
+    out["slos_grad_m16_n8_one_circuit_ms"] = 1e3 * t(lambda: oracle.slos_grad_fast(U16, inp16, w))
     U64 = random_unitary(64, seed=0)
-    out["all_outputs_m64_n4_ms"] = 1e3 * t(lambda: oracle.slos(U64, [1] * 4 + [0] * 60))
+    out["all_outputs_m64_n4_ms"] = 1e3 * t(lambda: oracle.slos_fast(U64, [1] * 4 + [0] * 60))
     U400 = random_unitary(400, seed=0)
     ns = 32 * oracle.num_threads()
     # the sampler in parallel over samples, all k sub-permanents of a step from one Glynn sum

@@ -58,6 +58,10 @@ def lib():
         L.oracle_slos.argtypes = [i32, vp, vp, vp, vp]
         L.oracle_slos_grad.restype = i32
         L.oracle_slos_grad.argtypes = [i32, vp, vp, vp, vp]
+        L.oracle_slos_fast.restype = i32
+        L.oracle_slos_fast.argtypes = [i32, vp, vp, vp, vp]
+        L.oracle_slos_grad_fast.restype = i32
+        L.oracle_slos_grad_fast.argtypes = [i32, vp, vp, vp, vp]
         L.oracle_philox.argtypes = [ctypes.c_uint32] * 6 + [vp]
         L.oracle_cc2017.argtypes = [vp, i32, vp, i64, u64, u64, vp]
         L.oracle_glynn_term.argtypes = [i32, vp, vp, vp]
@@ -177,6 +181,31 @@ def slos_grad(U, input_state, w) -> np.ndarray:
     w = np.ascontiguousarray(w, dtype=np.float64)
     g = np.zeros_like(U)
     lib().oracle_slos_grad(len(s), s.ctypes.data, U.ctypes.data, w.ctypes.data, g.ctypes.data)
+    return g
+
+
+def slos_fast(U, input_state) -> tuple[np.ndarray, np.ndarray]:
+    """(probabilities, amplitudes) like slos, by the host-tuned path (the CPU baseline):
+    layers parallel over contiguous rank ranges, parent ranks from one O(m) pass per state."""
+    U = _c128(U)
+    s = _i32(input_state)
+    m, n = len(s), int(s.sum())
+    N = math.comb(m + n - 1, n)
+    probs = np.zeros(N)
+    amps = np.zeros(N, dtype=np.complex128)
+    if lib().oracle_slos_fast(m, s.ctypes.data, U.ctypes.data, probs.ctypes.data, amps.ctypes.data):
+        raise ValueError("oracle SLOS: more than 63 photons")
+    return probs, amps
+
+
+def slos_grad_fast(U, input_state, w) -> np.ndarray:
+    """dL/dU like slos_grad, by the host-tuned path (parallel reverse sweep)."""
+    U = _c128(U)
+    s = _i32(input_state)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    g = np.zeros_like(U)
+    if lib().oracle_slos_grad_fast(len(s), s.ctypes.data, U.ctypes.data, w.ctypes.data, g.ctypes.data):
+        raise ValueError("oracle SLOS: more than 63 photons")
     return g
 
 

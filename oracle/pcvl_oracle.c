@@ -958,3 +958,210 @@ void oracle_cc2017_fast(const double* U_, int m, const int* in, int64_t count, u
     free(w);
   }
 }
+
+/* Host-tuned SLOS (FP64).  Ranks in descending-lex order are sum_i G[i][R_i], R_i the
+ * photons after mode i and G[i][r] = C(m - i + r - 2, r - 1) (0 for r = 0), so removing a
+ * photon from mode j lowers the rank by sum_{i<j} (G[i][R_i] - G[i][R_i - 1]) and adding
+ * one raises it by sum_{i<j} (G[i][R_i + 1] - G[i][R_i]): one O(m) pass per state gives
+ * the ranks of all its parents (or children), with no per-lookup rank computation.  Each
+ * OpenMP thread walks a contiguous rank range in order (one unrank per range, then
+ * fock_next).  Same sums as slos_layer, in the same order per state. */
+typedef struct {
+  int m, n;
+  uint64_t* g; /* g[i * (n + 2) + r], r = 0..n + 1 */
+} RankTable;
+
+static RankTable rank_table(int m, int n) {
+  RankTable t = {m, n, (uint64_t*)malloc(sizeof(uint64_t) * m * (n + 2))};
+  for (int i = 0; i < m; ++i)
+    for (int r = 0; r <= n + 1; ++r) t.g[i * (n + 2) + r] = r > 0 ? fock_count(m - i, r - 1) : 0;
+  return t;
+}
+
+enum { kSlosRange = 8192 };
+
+static void slos_layer_fast(const RankTable* T, int k, const cplx* U, int mk, const cplx* prev, cplx* cur) {
+  const int m = T->m, w = T->n + 2;
+  const int64_t nc = (int64_t)fock_count(m, k);
+  const int64_t nr = (nc + kSlosRange - 1) / kSlosRange;
+#pragma omp parallel
+  {
+    int* s = (int*)malloc(sizeof(int) * m);
+    int* R = (int*)malloc(sizeof(int) * m);
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t q = 0; q < nr; ++q) {
+      const int64_t c0 = q * kSlosRange, c1 = c0 + kSlosRange < nc ? c0 + kSlosRange : nc;
+      oracle_fock_unrank(m, k, (uint64_t)c0, s);
+      for (int64_t c = c0; c < c1; ++c) {
+        R[m - 1] = 0;
+        for (int i = m - 2; i >= 0; --i) R[i] = R[i + 1] + s[i + 1];
+        cplx acc = 0;
+        uint64_t d = 0;
+        for (int j = 0; j < m; ++j) {
+          if (s[j] > 0) acc += U[j * m + mk] * prev[(uint64_t)c - d];
+          if (R[j] == 0) break;
+          d += T->g[j * w + R[j]] - T->g[j * w + R[j] - 1];
+        }
+        cur[c] = acc;
+        if (c + 1 < c1) fock_next(m, s);
+      }
+    }
+    free(R);
+    free(s);
+  }
+}
+
+static double factorial_table[64];
+
+static void fill_factorials(void) {
+  factorial_table[0] = 1;
+  for (int i = 1; i < 64; ++i) factorial_table[i] = factorial_table[i - 1] * i;
+}
+
+/* all n-photon layers from the input (order of _Path), into the last one */
+static cplx** slos_layers_fast(int m, const int* in, const cplx* U, int n, const int* order, int keep_all) {
+  RankTable T = rank_table(m, n);
+  cplx** L = (cplx**)calloc(n + 1, sizeof(cplx*));
+  L[0] = (cplx*)malloc(sizeof(cplx));
+  L[0][0] = 1;
+  for (int k = 1; k <= n; ++k) {
+    L[k] = (cplx*)malloc(sizeof(cplx) * fock_count(m, k));
+    slos_layer_fast(&T, k, U, order[k - 1], L[k - 1], L[k]);
+    if (!keep_all) {
+      free(L[k - 1]);
+      L[k - 1] = NULL;
+    }
+  }
+  free(T.g);
+  return L;
+}
+
+/* probabilities and amplitudes like oracle_slos, by the host-tuned layers */
+int oracle_slos_fast(int m, const int* in, const double* U_, double* probs, double* amps) {
+  const cplx* U = (const cplx*)U_;
+  int n = 0;
+  for (int i = 0; i < m; ++i) n += in[i];
+  if (n > 63) return 1;
+  fill_factorials();
+  int* order = (int*)malloc(sizeof(int) * (n + 1));
+  oracle_slos_order(m, in, order);
+  cplx** L = slos_layers_fast(m, in, U, n, order, 0);
+  const cplx* c = L[n];
+  double pin = 1;
+  for (int i = 0; i < m; ++i) pin *= factorial_table[in[i]];
+  const int64_t N = (int64_t)fock_count(m, n);
+  const int64_t nr = (N + kSlosRange - 1) / kSlosRange;
+#pragma omp parallel
+  {
+    int* s = (int*)malloc(sizeof(int) * m);
+#pragma omp for schedule(static)
+    for (int64_t q = 0; q < nr; ++q) {
+      const int64_t r0 = q * kSlosRange, r1 = r0 + kSlosRange < N ? r0 + kSlosRange : N;
+      oracle_fock_unrank(m, n, (uint64_t)r0, s);
+      for (int64_t r = r0; r < r1; ++r) {
+        double f = 1;
+        for (int i = 0; i < m; ++i) f *= factorial_table[s[i]];
+        f /= pin;
+        const double re = creal(c[r]), im = cimag(c[r]);
+        if (probs) probs[r] = (re * re + im * im) * f;
+        if (amps) {
+          amps[2 * r] = re * sqrt(f);
+          amps[2 * r + 1] = im * sqrt(f);
+        }
+        if (r + 1 < r1) fock_next(m, s);
+      }
+    }
+    free(s);
+  }
+  free(L[n]);
+  free(L);
+  free(order);
+  return 0;
+}
+
+/* dL/dU like oracle_slos_grad, by the host-tuned layers and a parallel reverse sweep (each
+ * thread accumulates its parents' share of the layer's gradient column, then the shares
+ * are added) */
+int oracle_slos_grad_fast(int m, const int* in, const double* U_, const double* w, double* grad_) {
+  const cplx* U = (const cplx*)U_;
+  cplx* grad = (cplx*)grad_;
+  int n = 0;
+  for (int i = 0; i < m; ++i) n += in[i];
+  if (n > 63) return 1;
+  fill_factorials();
+  int* order = (int*)malloc(sizeof(int) * (n + 1));
+  oracle_slos_order(m, in, order);
+  cplx** L = slos_layers_fast(m, in, U, n, order, 1);
+  RankTable T = rank_table(m, n);
+  const int tw = n + 2;
+  for (int i = 0; i < m * m; ++i) grad[i] = 0;
+  double pin = 1;
+  for (int i = 0; i < m; ++i) pin *= factorial_table[in[i]];
+  const int64_t N = (int64_t)fock_count(m, n);
+  cplx* adj = (cplx*)malloc(sizeof(cplx) * N);
+  {
+    const int64_t nr = (N + kSlosRange - 1) / kSlosRange;
+#pragma omp parallel
+    {
+      int* s = (int*)malloc(sizeof(int) * m);
+#pragma omp for schedule(static)
+      for (int64_t q = 0; q < nr; ++q) {
+        const int64_t r0 = q * kSlosRange, r1 = r0 + kSlosRange < N ? r0 + kSlosRange : N;
+        oracle_fock_unrank(m, n, (uint64_t)r0, s);
+        for (int64_t r = r0; r < r1; ++r) {
+          double f = 1;
+          for (int i = 0; i < m; ++i) f *= factorial_table[s[i]];
+          adj[r] = 2.0 * w[r] * (f / pin) * L[n][r];
+          if (r + 1 < r1) fock_next(m, s);
+        }
+      }
+      free(s);
+    }
+  }
+  for (int k = n; k >= 1; --k) {
+    const int mk = order[k - 1];
+    const int64_t np = (int64_t)fock_count(m, k - 1);
+    const int64_t nr = (np + kSlosRange - 1) / kSlosRange;
+    cplx* pa = (cplx*)malloc(sizeof(cplx) * (np > 0 ? np : 1));
+    const cplx* prev = L[k - 1];
+#pragma omp parallel
+    {
+      int* s = (int*)malloc(sizeof(int) * m);
+      int* R = (int*)malloc(sizeof(int) * m);
+      cplx* gcol = (cplx*)calloc(m, sizeof(cplx));
+#pragma omp for schedule(dynamic, 1)
+      for (int64_t q = 0; q < nr; ++q) {
+        const int64_t p0 = q * kSlosRange, p1 = p0 + kSlosRange < np ? p0 + kSlosRange : np;
+        oracle_fock_unrank(m, k - 1, (uint64_t)p0, s);
+        for (int64_t p = p0; p < p1; ++p) {
+          R[m - 1] = 0;
+          for (int i = m - 2; i >= 0; --i) R[i] = R[i + 1] + s[i + 1];
+          cplx acc = 0;
+          const cplx lp = conj(prev[p]);
+          uint64_t d = 0;
+          for (int j = 0; j < m; ++j) {
+            const cplx x = adj[(uint64_t)p + d];
+            acc += conj(U[j * m + mk]) * x;
+            gcol[j] += lp * x;
+            d += T.g[j * tw + R[j] + 1] - T.g[j * tw + R[j]];
+          }
+          pa[p] = acc;
+          if (p + 1 < p1) fock_next(m, s);
+        }
+      }
+#pragma omp critical
+      for (int j = 0; j < m; ++j) grad[j * m + mk] += gcol[j];
+      free(gcol);
+      free(R);
+      free(s);
+    }
+    free(adj);
+    adj = pa;
+  }
+  free(adj);
+  for (int k = 0; k <= n; ++k) free(L[k]);
+  free(L);
+  free(T.g);
+  free(order);
+  return 0;
+}

@@ -202,8 +202,9 @@ def test_mlp_reference_gradient_finite_differences():
 
 
 def test_host_tuned_paths_equal_the_restatements(oracle):
-    """The CPU baseline's batched Glynn and parallel sampler compute what the plain
-    restatements compute: permanents to 1e-12 relative, samples one for one."""
+    """The CPU baseline's batched Glynn, parallel sampler and SLOS compute what the plain
+    restatements compute: permanents to 1e-12 relative, samples one for one, SLOS outputs
+    bit for bit and its gradient to 1e-12."""
     from perceval_gb300.utils.matrix import random_unitary
     U = random_unitary(64, seed=3)
     rng = np.random.default_rng(3)
@@ -224,3 +225,13 @@ def test_host_tuned_paths_equal_the_restatements(oracle):
     V = random_unitary(24, seed=6)
     inp = [1] * 10 + [0] * 14
     assert np.array_equal(oracle.cc2017_fast(V, inp, 120, seed=8), oracle.cc2017(V, inp, 120, seed=8))
+    # SLOS: the same sums per state (bit for bit), the gradient up to the order in which the
+    # threads' shares of a column are added; ranges of 8192 states split the larger layers
+    for m, inp in ((7, [0, 3, 0, 0, 1, 0, 2]), (12, [1] * 6 + [0] * 6), (16, [2, 1, 1, 0, 1, 1] + [0] * 10)):
+        V = random_unitary(m, seed=m)
+        p, a = oracle.slos(V, inp)
+        pf, af = oracle.slos_fast(V, inp)
+        assert np.array_equal(p, pf) and np.array_equal(a, af)
+        w = np.random.default_rng(m).normal(size=len(p))
+        g, gf = oracle.slos_grad(V, inp, w), oracle.slos_grad_fast(V, inp, w)
+        assert np.max(np.abs(gf - g)) <= 1e-12 * np.max(np.abs(g))
