@@ -190,10 +190,9 @@ def cpu_perm_baseline(budget_s: float = 15.0) -> dict:
 
 
 def cpu_context() -> dict:
-    """The oracle's host-tuned paths (C; SLOS and its gradient, permanents and the exact
-    sampler with OpenMP on all host threads, the Gurvits estimator on one thread) on bounded
-    samples of the secondary workloads, for context beside the GPU lines: a few seconds of
-    host time."""
+    """The oracle's host-tuned paths (C, OpenMP on all host threads: SLOS and its gradient,
+    the exact sampler, Gurvits estimates) on bounded samples of the secondary workloads, for
+    context beside the GPU lines: a few seconds of host time."""
     from oracle import oracle
     from perceval_gb300.utils.matrix import random_unitary
     out = {"threads_openmp": oracle.num_threads()}
@@ -220,9 +219,9 @@ def cpu_context() -> dict:
     Ubig = random_unitary(1024, seed=0)
     rng = np.random.default_rng(11)
     gm = [Ubig[np.ix_(rng.choice(1024, 20, False), rng.choice(1024, 20, False))] for _ in range(20)]
-    draws = 2000
-    dt = t(lambda: [oracle.gurvits(a, draws, seed=1, first=i * draws) for i, a in enumerate(gm)])
-    out["gurvits_n20_draws_per_s_1thread"] = 20 * draws / dt
+    draws = 20000
+    dt = t(lambda: oracle.gurvits_batch_fast(gm, draws, 1, [i * draws for i in range(len(gm))]))
+    out["gurvits_n20_draws_per_s"] = 20 * draws / dt
     return out
 
 

@@ -66,6 +66,7 @@ def lib():
         L.oracle_cc2017.argtypes = [vp, i32, vp, i64, u64, u64, vp]
         L.oracle_glynn_term.argtypes = [i32, vp, vp, vp]
         L.oracle_gurvits.argtypes = [i32, vp, i64, u64, u64, vp]
+        L.oracle_gurvits_batch_fast.argtypes = [vp, vp, vp, i32, i64, u64, vp, vp]
         L.oracle_num_threads.restype = i32
         L.oracle_set_threads.argtypes = [i32]
         _lib = L
@@ -241,6 +242,20 @@ def gurvits(a, iterations: int, seed: int, first: int = 0) -> complex:
     lib().oracle_gurvits(a.shape[0], a.ctypes.data, int(iterations), int(seed) & (2**64 - 1), int(first),
                          out.ctypes.data)
     return complex(out[0], out[1])
+
+
+def gurvits_batch_fast(mats, iterations: int, seed: int, firsts) -> np.ndarray:
+    """gurvits for each matrix of a list (matrix b's draws start at index firsts[b]) by the
+    host-tuned path (the CPU baseline): OpenMP over (matrix, 256 draws) on all threads."""
+    mats = [_c128(a) for a in mats]
+    sizes = np.array([a.shape[0] for a in mats], dtype=np.int32)
+    offs = np.concatenate([[0], np.cumsum([a.size for a in mats])[:-1]]).astype(np.int64)
+    flat = np.ascontiguousarray(np.concatenate([a.reshape(-1) for a in mats]))
+    firsts = np.ascontiguousarray(firsts, dtype=np.uint64)
+    out = np.zeros(len(mats), dtype=np.complex128)
+    lib().oracle_gurvits_batch_fast(flat.ctypes.data, offs.ctypes.data, sizes.ctypes.data, len(mats),
+                                    int(iterations), int(seed) & (2**64 - 1), firsts.ctypes.data, out.ctypes.data)
+    return out
 
 
 # ---------------------------------------------------------------- brute force

@@ -959,6 +959,98 @@ void oracle_cc2017_fast(const double* U_, int m, const int* in, int64_t count, u
   }
 }
 
+/* Gurvits estimates of a batch of matrices (the CPU baseline of NaiveApprox): one OpenMP task
+ * per (matrix, 256 draws), the draws' signs from the same Philox counters as oracle_gurvits
+ * (draw k of matrix b has index firsts[b] + k); a draw's column sums y_j = sum_i x_i a_ij run
+ * row by row over contiguous real and imaginary arrays (vectorisable over j), the product of
+ * the n sums in four chains.  Each task's terms are added with Neumaier compensation and the
+ * tasks of a matrix in order, so results do not depend on the thread count. */
+enum { kGurvitsTask = 256 };
+
+__attribute__((optimize("fp-contract=fast")))
+void oracle_gurvits_batch_fast(const double* mats, const int64_t* offs, const int32_t* sizes, int count,
+                               int64_t iterations, uint64_t seed, const uint64_t* firsts, double* out) {
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  const int64_t per = (iterations + kGurvitsTask - 1) / kGurvitsTask;
+  double* part = (double*)malloc(sizeof(double) * 4 * (size_t)(per * count > 0 ? per * count : 1));
+#pragma omp parallel
+  {
+    double* buf = (double*)malloc(sizeof(double) * (2 * 64 * 64 + 4 * 64));
+    double *ar = buf, *ai = buf + 64 * 64, *yr = ai + 64 * 64, *yi = yr + 64;
+    int cur = -1;
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t q = 0; q < per * count; ++q) {
+      const int b = (int)(q / per), n = sizes[b];
+      if (b != cur) {
+        const double* a = mats + 2 * offs[b];
+        for (int e = 0; e < n * n; ++e) {
+          ar[e] = a[2 * e];
+          ai[e] = a[2 * e + 1];
+        }
+        cur = b;
+      }
+      const int64_t d0 = (q % per) * kGurvitsTask;
+      const int64_t d1 = d0 + kGurvitsTask < iterations ? d0 + kGurvitsTask : iterations;
+      double sr = 0, cr = 0, si = 0, ci = 0;
+      for (int64_t k = d0; k < d1; ++k) {
+        const uint64_t idx = firsts[b] + (uint64_t)k;
+        const u4 r = philox((u4){(uint32_t)idx, (uint32_t)(idx >> 32), 0x67757276u, 0u}, k0, k1);
+        const uint64_t bits = (uint64_t)r.x | ((uint64_t)r.y << 32);
+        for (int j = 0; j < n; ++j) yr[j] = yi[j] = 0;
+        for (int i = 0; i < n; ++i) {
+          const double sg = ((bits >> i) & 1) ? -1.0 : 1.0;
+          const double* xr = ar + i * n;
+          const double* xi = ai + i * n;
+          for (int j = 0; j < n; ++j) {
+            yr[j] += sg * xr[j];
+            yi[j] += sg * xi[j];
+          }
+        }
+        double pr[4] = {1, 1, 1, 1}, pi[4] = {0, 0, 0, 0};
+        int j = 0;
+        for (; j + 4 <= n; j += 4)
+          for (int c = 0; c < 4; ++c) {
+            const double x = pr[c], y = pi[c];
+            pr[c] = x * yr[j + c] - y * yi[j + c];
+            pi[c] = x * yi[j + c] + y * yr[j + c];
+          }
+        for (; j < n; ++j) {
+          const double x = pr[0], y = pi[0];
+          pr[0] = x * yr[j] - y * yi[j];
+          pi[0] = x * yi[j] + y * yr[j];
+        }
+        const double r01 = pr[0] * pr[1] - pi[0] * pi[1], i01 = pr[0] * pi[1] + pi[0] * pr[1];
+        const double r23 = pr[2] * pr[3] - pi[2] * pi[3], i23 = pr[2] * pi[3] + pi[2] * pr[3];
+        double tr = r01 * r23 - i01 * i23, ti = r01 * i23 + i01 * r23;
+        if (__builtin_popcountll(bits & (n == 64 ? ~0ull : ((1ull << n) - 1))) & 1) {
+          tr = -tr;
+          ti = -ti;
+        }
+        neumaier(&sr, &cr, tr);
+        neumaier(&si, &ci, ti);
+      }
+      part[4 * q] = sr;
+      part[4 * q + 1] = cr;
+      part[4 * q + 2] = si;
+      part[4 * q + 3] = ci;
+    }
+    free(buf);
+  }
+  for (int b = 0; b < count; ++b) {
+    double sr = 0, cr = 0, si = 0, ci = 0;
+    for (int64_t t = 0; t < per; ++t) {
+      const double* x = part + 4 * (b * per + t);
+      neumaier(&sr, &cr, x[0]);
+      neumaier(&sr, &cr, x[1]);
+      neumaier(&si, &ci, x[2]);
+      neumaier(&si, &ci, x[3]);
+    }
+    out[2 * b] = (sr + cr) / (double)iterations;
+    out[2 * b + 1] = (si + ci) / (double)iterations;
+  }
+  free(part);
+}
+
 /* Host-tuned SLOS (FP64).  Ranks in descending-lex order are sum_i G[i][R_i], R_i the
  * photons after mode i and G[i][r] = C(m - i + r - 2, r - 1) (0 for r = 0), so removing a
  * photon from mode j lowers the rank by sum_{i<j} (G[i][R_i] - G[i][R_i - 1]) and adding

@@ -202,9 +202,9 @@ def test_mlp_reference_gradient_finite_differences():
 
 
 def test_host_tuned_paths_equal_the_restatements(oracle):
-    """The CPU baseline's batched Glynn, parallel sampler and SLOS compute what the plain
-    restatements compute: permanents to 1e-12 relative, samples one for one, SLOS outputs
-    bit for bit and its gradient to 1e-12."""
+    """The CPU baseline's batched Glynn, parallel sampler, SLOS and Gurvits estimates compute
+    what the plain restatements compute: permanents to 1e-12 relative, samples one for one,
+    SLOS outputs bit for bit and its gradient to 1e-12, estimates to 1e-13."""
     from perceval_gb300.utils.matrix import random_unitary
     U = random_unitary(64, seed=3)
     rng = np.random.default_rng(3)
@@ -235,3 +235,9 @@ def test_host_tuned_paths_equal_the_restatements(oracle):
         w = np.random.default_rng(m).normal(size=len(p))
         g, gf = oracle.slos_grad(V, inp, w), oracle.slos_grad_fast(V, inp, w)
         assert np.max(np.abs(gf - g)) <= 1e-12 * np.max(np.abs(g))
+    # Gurvits: the same draws, added in another order (both compensated)
+    gm = [np.ascontiguousarray(U[np.ix_(rng.choice(64, n, False), rng.choice(64, n, False))]) for n in (1, 5, 20, 33)]
+    firsts = [0, 7, 1000, 5]
+    got = oracle.gurvits_batch_fast(gm, 1000, 9, firsts)
+    ref = np.array([oracle.gurvits(a, 1000, seed=9, first=f) for a, f in zip(gm, firsts)])
+    assert np.max(np.abs(got - ref)) <= 1e-13
