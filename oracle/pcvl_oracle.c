@@ -340,8 +340,9 @@ int oracle_slos_grad(int m, const int* in, const double* U_, const double* w, do
   int* order = (int*)malloc(sizeof(int) * (n + 1));
   oracle_slos_order(m, in, order);
   cplx** L = (cplx**)malloc(sizeof(cplx*) * (n + 1));
-  for (int k = 0; k <= n; ++k) L[k] = (cplx*)malloc(sizeof(cplx) * fock_count(m, k));
+  L[0] = (cplx*)malloc(sizeof(cplx));
   L[0][0] = 1;
+  for (int k = 1; k <= n; ++k) L[k] = (cplx*)malloc(sizeof(cplx) * fock_count(m, k));
   for (int k = 1; k <= n; ++k) slos_layer(m, k, U, order[k - 1], L[k - 1], L[k]);
   for (int i = 0; i < m * m; ++i) grad[i] = 0;
   const double pin = prodfact(m, in);
@@ -1111,9 +1112,9 @@ static void fill_factorials(void) {
 }
 
 /* all n-photon layers from the input (order of _Path), into the last one */
-static cplx** slos_layers_fast(int m, const int* in, const cplx* U, int n, const int* order, int keep_all) {
+static cplx** slos_layers_fast(int m, const cplx* U, int n, const int* order, int keep_all) {
   RankTable T = rank_table(m, n);
-  cplx** L = (cplx**)calloc(n + 1, sizeof(cplx*));
+  cplx** L = (cplx**)calloc(n > 0 ? (size_t)n + 1 : 1, sizeof(cplx*));
   L[0] = (cplx*)malloc(sizeof(cplx));
   L[0][0] = 1;
   for (int k = 1; k <= n; ++k) {
@@ -1133,11 +1134,11 @@ int oracle_slos_fast(int m, const int* in, const double* U_, double* probs, doub
   const cplx* U = (const cplx*)U_;
   int n = 0;
   for (int i = 0; i < m; ++i) n += in[i];
-  if (n > 63) return 1;
+  if (n < 0 || n > 63) return 1;
   fill_factorials();
   int* order = (int*)malloc(sizeof(int) * (n + 1));
   oracle_slos_order(m, in, order);
-  cplx** L = slos_layers_fast(m, in, U, n, order, 0);
+  cplx** L = slos_layers_fast(m, U, n, order, 0);
   const cplx* c = L[n];
   double pin = 1;
   for (int i = 0; i < m; ++i) pin *= factorial_table[in[i]];
@@ -1179,11 +1180,11 @@ int oracle_slos_grad_fast(int m, const int* in, const double* U_, const double* 
   cplx* grad = (cplx*)grad_;
   int n = 0;
   for (int i = 0; i < m; ++i) n += in[i];
-  if (n > 63) return 1;
+  if (n < 0 || n > 63) return 1;
   fill_factorials();
   int* order = (int*)malloc(sizeof(int) * (n + 1));
   oracle_slos_order(m, in, order);
-  cplx** L = slos_layers_fast(m, in, U, n, order, 1);
+  cplx** L = slos_layers_fast(m, U, n, order, 1);
   RankTable T = rank_table(m, n);
   const int tw = n + 2;
   for (int i = 0; i < m * m; ++i) grad[i] = 0;
