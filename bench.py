@@ -627,9 +627,10 @@ def secondary(torch, _native, random_unitary, dev, flush, fp64_peak_tflops):
     res["learned_mis_n30_m900"] = learned_case(torch, _native, random_unitary, 900, 30, 1024, 4, 8, 16, 96,
                                                tvd=False, n_ref64=32)
     # n = 8, m = 64 with enough samples of both samplers to resolve the marginals to 1e-3:
-    # 2048 chains x 4096 steps (8.4 M proposals) and 4 M exact samples
+    # 2048 chains x 4096 steps (8.4 M proposals) and 4 M exact samples; and the exact TVD of
+    # both samplers' empirical distributions
     res["learned_mis_n8_m64"] = learned_case(torch, _native, random_unitary, 64, 8, 20000, 10, 2048, 4096,
-                                             4_000_000, mis_batch=16384)
+                                             4_000_000, mis_batch=16384, exact_tvd=True)
     # small case: SLOS m=12, n=6 and 1000 Naive amplitudes (latency-bound)
     from perceval_gb300 import BackendFactory, BasicState
     U12 = random_unitary(12, seed=0)
@@ -777,7 +778,7 @@ def secondary(torch, _native, random_unitary, dev, flush, fp64_peak_tflops):
 
 
 def learned_case(torch, _native, random_unitary, m, n, n_train, epochs, chains, steps, n_ref, tvd=True,
-                 marginal_modes=8, n_ref64=None, mis_batch=512, tvd_samples=25600):
+                 marginal_modes=8, n_ref64=None, mis_batch=512, tvd_samples=25600, exact_tvd=False):
     """Learned-proposal Metropolised sampler against the plain GPU exact sampler on one
     Haar unitary (seed 0, input photons in modes 0..n-1).
 
@@ -789,8 +790,12 @@ def learned_case(torch, _native, random_unitary, m, n, n_train, epochs, chains, 
     distributions P(n_i = a, n_j = b) of pairs among them (generating-function
     permanents, perceval_gb300.marginals) against each sampler's empirical ones, with
     the binomial standard error of the largest probability at that sample count (for the
-    MIS, at its ESS)."""
-    from perceval_gb300.learned import ProposalMLP, ess, exact_moments, run_mis, tvd_estimate
+    MIS, at its ESS).  With ``exact_tvd``: the exact TVD between each sampler's empirical
+    output distribution and the exact law (every observed output's probability from an FP64
+    permanent, the unobserved mass as one minus their sum), for the MIS's chain states and
+    for the exact sampler at its full count and at the MIS's ESS."""
+    from perceval_gb300.learned import (ProposalMLP, counts_to_sorted_modes, ess, exact_empirical_tvd,
+                                        exact_moments, run_mis, tvd_estimate)
     from perceval_gb300.marginals import (empirical_one_mode, empirical_two_mode, one_mode_marginal,
                                           two_mode_marginal)
     U = random_unitary(m, seed=0)
@@ -813,12 +818,16 @@ def learned_case(torch, _native, random_unitary, m, n, n_train, epochs, chains, 
     mis_occ = np.stack([(seqs == i).sum(axis=1) for i in modes], axis=1)
     mis_mean = np.bincount(seqs.reshape(-1).astype(np.int64), minlength=m)[:m] / len(seqs)
 
+    ref_sorted = []
+
     def exact(count, seed, precision):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         x = _native.cc2017_sample(Ud, inp, count, seed=seed, precision=precision)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
+        if exact_tvd and not ref_sorted:
+            ref_sorted.append(counts_to_sorted_modes(x, n).cpu().numpy())
         return dt, x[:, modes].cpu().numpy(), x.double().mean(0).cpu().numpy(), x[:tvd_samples].cpu().numpy()
     t_ref, ref_occ, ref_mean, ref_head = exact(n_ref, 202, 0)
     # the same sampler in its FP64 mode, the acceptance's arithmetic
@@ -855,6 +864,11 @@ def learned_case(torch, _native, random_unitary, m, n, n_train, epochs, chains, 
            "marginal_modes": modes, "marginal_pairs": [[modes[a], modes[b]] for a, b in pairs]}
     row["ess_per_s_ratio"] = row["mis"]["ess_per_s"] / row["exact_sampler"]["ess_per_s"]
     row["ess_per_s_ratio_vs_fp64_exact"] = row["mis"]["ess_per_s"] / row["exact_sampler_fp64"]["ess_per_s"]
+    if exact_tvd:
+        n_ess = max(1, min(n_ref, int(round(ess_mis))))
+        row["exact_tvd"] = {"mis": exact_empirical_tvd(U, inp, seqs),
+                            "exact_sampler": exact_empirical_tvd(U, inp, ref_sorted[0]),
+                            "exact_sampler_at_mis_ess": exact_empirical_tvd(U, inp, ref_sorted[0][:n_ess])}
     if tvd:
         # TVD(q, pi) on photon sequences from the exact samples: trained vs untrained network
         untrained = ProposalMLP(m, n, D=128, H=512, layers=3, seed=0)
@@ -876,7 +890,8 @@ def run_learned(args):
     out = {}
     for (m, n, n_train, epochs, chains, steps, n_ref) in ((900, 30, args.learned_train, 6, 16, 32, 152),
                                                            (64, 8, 20000, 10, 64, 400, 25600)):
-        out[f"n{n}_m{m}"] = learned_case(torch, _native, random_unitary, m, n, n_train, epochs, chains, steps, n_ref)
+        out[f"n{n}_m{m}"] = learned_case(torch, _native, random_unitary, m, n, n_train, epochs, chains, steps, n_ref,
+                                         exact_tvd=(n == 8))
     # tensor-pipe rate of the network's GEMM kernel (pcvl_gemm_bf16: tcgen05 MMA from TMA-staged
     # tiles, FP32 accumulation in tensor memory) at the training shapes of n = 30, m = 900 (256 sequences x 30 steps)
     # and at 8192^3, against the measured cuBLAS BF16 burst peak

@@ -181,3 +181,15 @@ def test_seed_reproducible_counters():
     b = _random.take_samples(3)
     random_seed(5)
     assert _random.take_samples(10) == a and a == (5, 0) and b == (5, 10)
+
+
+def test_counts_to_sorted_modes():
+    """Occupation rows -> photon modes in ascending order (the keys of the exact empirical
+    TVD), against a repeat of each mode by its count."""
+    from perceval_gb300.learned import counts_to_sorted_modes
+    rng = np.random.default_rng(3)
+    for m, n in ((6, 3), (64, 8), (5, 9)):
+        occ = np.array([np.bincount(rng.integers(0, m, n), minlength=m) for _ in range(200)], dtype=np.int32)
+        got = counts_to_sorted_modes(torch.from_numpy(occ), n).numpy()
+        want = np.array([np.repeat(np.arange(m), r) for r in occ])
+        assert np.array_equal(got, want)

@@ -147,6 +147,27 @@ def test_tvd_estimate_matches_enumeration(native, oracle):
     assert abs(est - exact) < 5 * se + 1e-3, (est, se, exact)
 
 
+@pytest.mark.parametrize("inp", [[1, 0, 1, 0, 1, 0], [2, 0, 1, 0, 0, 0]])
+def test_exact_empirical_tvd_matches_enumeration(native, oracle, inp):
+    # m = 6, n = 3: every output's probability from the oracle's SLOS; the empirical TVD of
+    # GPU exact samples (sorted modes recovered from occupations on the device) computed
+    # without enumeration equals the enumerated one, for a few and for many samples
+    from perceval_gb300.learned import counts_to_sorted_modes, exact_empirical_tvd
+    from perceval_gb300.utils.states import fock_rank_array
+    m, n = 6, 3
+    U = random_unitary(m, seed=13)
+    p, _ = oracle.slos(U, inp)
+    x = native.cc2017_sample(torch.from_numpy(U).cuda(), inp, 4000, seed=21)
+    for N in (7, 4000):
+        occ = x[:N].cpu().numpy()
+        f = np.bincount(fock_rank_array(occ), minlength=len(p)) / N
+        want = 0.5 * np.abs(p - f).sum()
+        got = exact_empirical_tvd(U, inp, counts_to_sorted_modes(x[:N], n).cpu().numpy())
+        assert got["samples"] == N and got["distinct_outputs"] == int((f > 0).sum())
+        assert abs(got["tvd"] - want) < 1e-12, (got, want)
+        assert abs(got["observed_mass"] - p[f > 0].sum()) < 1e-12
+
+
 def test_early_stopping_keeps_the_best_epoch(native):
     # 200 samples, 12 epochs: the held-out NLL rises once the network memorises; training
     # keeps the epoch with the lowest held-out NLL, never worse than the start
