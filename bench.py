@@ -219,7 +219,7 @@ def cpu_context() -> dict:
     Ubig = random_unitary(1024, seed=0)
     rng = np.random.default_rng(11)
     gm = [Ubig[np.ix_(rng.choice(1024, 20, False), rng.choice(1024, 20, False))] for _ in range(20)]
-    draws = 20000
+    draws = 100000
     dt = t(lambda: oracle.gurvits_batch_fast(gm, draws, 1, [i * draws for i in range(len(gm))]))
     out["gurvits_n20_draws_per_s"] = 20 * draws / dt
     return out
