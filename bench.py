@@ -154,13 +154,10 @@ def traffic_from_profile(name: str):
 
 
 # ----------------------------------------------------------------------------- CPU
-def cpu_perm_baseline(budget_s: float = 15.0) -> dict:
-    """The host-tuned FP64 Glynn of the CPU restatement (C, OpenMP over every (matrix,
-    chunk) task on all host threads, sixteen Gray-code steps at once in vector lanes) on a
-    stratified sample:
+def _cpu_perm_rate(oracle, budget_s: float) -> tuple[float, dict, float]:
+    """Whole-batch perms/s of the host-tuned Glynn, extrapolated from a stratified sample:
     per size n, batches of the batch's own matrices of that size, doubling until they take
-    about budget / 17 seconds; the full-batch time is extrapolated by the size counts."""
-    from oracle import oracle
+    about budget / 17 seconds; the full-batch time is the per-size times x the size counts."""
     _, flat, offs, sizes = make_batch(seed=0)
     counts = np.bincount(sizes, minlength=25)
     per_n, used = {}, {}
@@ -181,7 +178,25 @@ def cpu_perm_baseline(budget_s: float = 15.0) -> dict:
         per_n[n] = dt / len(sel)
         used[n] = len(sel)
     total = sum(counts[n] * per_n[n] for n in range(8, 25))
-    return {"value": N_MATS / total, "unit": "perms/s", "cores": oracle.num_threads(), "kind": "port",
+    return N_MATS / total, used, spent
+
+
+def cpu_perm_baseline(budget_s: float = 15.0, single_thread_s: float = 0.0) -> dict:
+    """The host-tuned FP64 Glynn of the CPU restatement (C, OpenMP over every (matrix,
+    chunk) task on all host threads, sixteen Gray-code steps at once in vector lanes) on a
+    stratified sample of the batch (``_cpu_perm_rate``); with ``single_thread_s`` also the
+    same on one thread, on a sample of about that many seconds."""
+    from oracle import oracle
+    value, used, spent = _cpu_perm_rate(oracle, budget_s)
+    threads = oracle.num_threads()
+    extra = {}
+    if single_thread_s > 0:
+        oracle.set_threads(1)
+        try:
+            extra["single_thread_value"] = _cpu_perm_rate(oracle, single_thread_s)[0]
+        finally:
+            oracle.set_threads(threads)
+    return {"value": value, "unit": "perms/s", "cores": threads, "kind": "port", **extra,
             "flags": "gcc -O3 -std=c11 -fopenmp (portable: on the Arm host NEON, 128-bit like its SVE, is the "
                      "baseline ISA), multiply-adds fused in the timed kernel",
             "sample": f"{sum(used.values())} matrices of the batch, every size n=8..24 "
@@ -422,7 +437,7 @@ def run_ours(args):
         sec.update(secondary(torch, _native, random_unitary, dev, flush, fp64_peak))
         line["secondary"] = sec
     if rank == 0 and ws == 1 and not args.skip_cpu:
-        line["cpu_baseline"] = cpu_perm_baseline()
+        line["cpu_baseline"] = cpu_perm_baseline(single_thread_s=4.0)
         if "secondary" in line:
             line["secondary"]["cpu_context"] = cpu_context()
     if rank == 0:
