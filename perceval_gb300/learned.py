@@ -278,6 +278,9 @@ def exact_empirical_tvd(U: np.ndarray, input_state, sequences: np.ndarray, chunk
     bits = max(1, int(m - 1).bit_length())
     if bits * n > 63:
         raise ValueError("outputs do not fit a 63-bit key")
+    if n == 0:  # the vacuum is the only output
+        N = int(np.asarray(sequences).shape[0])
+        return {"samples": N, "distinct_outputs": int(N > 0), "observed_mass": float(N > 0), "tvd": float(N == 0)}
     seq = np.sort(np.asarray(sequences).reshape(-1, n).astype(np.int64), axis=1)
     shifts = np.arange(n, dtype=np.int64) * bits
     keys = np.bitwise_or.reduce(seq << shifts, axis=1)
