@@ -193,3 +193,10 @@ def test_counts_to_sorted_modes():
         got = counts_to_sorted_modes(torch.from_numpy(occ), n).numpy()
         want = np.array([np.repeat(np.arange(m), r) for r in occ])
         assert np.array_equal(got, want)
+
+
+def test_exact_empirical_tvd_without_photons():
+    """No photons: the vacuum is the only output, so any samples match the law exactly."""
+    from perceval_gb300.learned import exact_empirical_tvd
+    got = exact_empirical_tvd(np.eye(3, dtype=complex), [0, 0, 0], np.zeros((5, 0), dtype=np.int64))
+    assert got == {"samples": 5, "distinct_outputs": 1, "observed_mass": 1.0, "tvd": 0.0}
