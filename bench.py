@@ -206,8 +206,9 @@ def cpu_perm_baseline(budget_s: float = 15.0, single_thread_s: float = 0.0) -> d
 
 def cpu_context() -> dict:
     """The oracle's host-tuned paths (C, OpenMP on all host threads: SLOS and its gradient,
-    the exact sampler, Gurvits estimates) on bounded samples of the secondary workloads, for
-    context beside the GPU lines: a few seconds of host time."""
+    the exact sampler, Gurvits estimates; SLOS and the sampler also on one thread) on bounded
+    samples of the secondary workloads, for context beside the GPU lines: a few seconds of
+    host time."""
     from oracle import oracle
     from perceval_gb300.utils.matrix import random_unitary
     out = {"threads_openmp": oracle.num_threads()}
@@ -237,6 +238,15 @@ def cpu_context() -> dict:
     draws = 100000
     dt = t(lambda: oracle.gurvits_batch_fast(gm, draws, 1, [i * draws for i in range(len(gm))]))
     out["gurvits_n20_draws_per_s"] = 20 * draws / dt
+    # single-thread rates of the SLOS and sampler legs
+    threads = oracle.num_threads()
+    oracle.set_threads(1)
+    try:
+        out["slos_m20_n10_ms_1thread"] = 1e3 * t(lambda: oracle.slos_fast(U20, [1] * 10 + [0] * 10))
+        out["cc2017_n20_m400_samples_per_s_1thread"] = 16 / t(
+            lambda: oracle.cc2017_fast(U400, [1] * 20 + [0] * 380, 16, seed=1))
+    finally:
+        oracle.set_threads(threads)
     return out
 
 
