@@ -8,7 +8,7 @@ Perm(U_{s,t}) / sqrt(prod s! prod t!) in descending-lexicographic order.
 
 Under a mask, the outputs are the states ``xq.FSArray(m, n, mask)`` keeps
 (_slap.py:30-36), selected on the device (``pcvl_fock_mask_ranks``).  Feed-forward
-(_slap.py:82-194) belongs to the processor front-end and is not part of this build:
+(_slap.py:82-194) belongs to the processor front-end and is not part of this package:
 ``can_simulate_feed_forward`` answers False so callers take their default path.
 """
 from __future__ import annotations

@@ -58,7 +58,7 @@ class ACircuit:
 
     def compute_unitary(self, use_symbolic: bool = False) -> np.ndarray:
         if use_symbolic:
-            raise NotImplementedError("symbolic unitaries are not part of this build")
+            raise NotImplementedError("symbolic unitaries are not supported by perceval_gb300")
         return self._compute_unitary()
 
     @property

@@ -1,4 +1,4 @@
-"""Named circuit parameters (numeric only; the symbolic mode stays out of this build)."""
+"""Named circuit parameters (numeric only; the symbolic mode is not supported by this package)."""
 from __future__ import annotations
 
 import math
