@@ -1,7 +1,8 @@
 """Python side of the CPU oracle.  TEST INFRASTRUCTURE ONLY.
 
-Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use
-this module, and only as the checker: nothing in ``perceval_gb300`` imports it.
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline legs use
+this module, to check results and to time the CPU baseline: nothing in ``perceval_gb300``
+imports it.
 
 Two layers:
 * ``liboracle.so`` (``pcvl_oracle.c``): FP64 restatements of the reference's

@@ -1,7 +1,7 @@
 /*
  * CPU oracle for the linear-optics hot path.  TEST INFRASTRUCTURE ONLY: the
- * library's product path never calls into this file; tests, the smoke check and
- * the benchmark's CPU baseline use it as the checker.
+ * library's product path never calls into this file; tests and the smoke check use
+ * it to check results, the benchmark to time the CPU baseline.
  *
  * Plain FP64 restatement of the reference semantics (the reference's arithmetic
  * lives in the closed exqalibur~=1.1.0 library; its call sites and tests fix what
